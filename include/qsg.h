@@ -1,0 +1,242 @@
+/*
+ * qsg.h -- C ABI of the GB300 cycle-tracking library (libqsg.so).
+ *
+ * The library replaces the per-vault tracking launch inside Quicksilver's
+ * cycleTracking() (main.cc:155-236): CycleTrackingKernel / CycleTrackingGuts
+ * (main.cc:126-134, CycleTracking.cc:14-120) and everything they call
+ * (MC_Segment_Outcome.cc, MCT.cc, CollisionEvent.cc, NuclearData.cc,
+ * MacroscopicCrossSection.cc, MC_Facet_Crossing_Event.cc, Tallies.hh:350-354,
+ * ParticleVault.hh:86-93, ParticleVaultContainer.cc:340-400).
+ *
+ * Conventions
+ *   - Every entry point returns int: 0 (QSG_OK) or a QSG_ERR_* code.  The text
+ *     of the last error on the calling thread is available from
+ *     qsg_last_error().  Nothing throws or aborts across the ABI.  (The
+ *     reference's qs_assert only prints and carries on, qs_assert.hh:9-26; this
+ *     library reports the same conditions as error codes instead.)
+ *   - Plain pointers and sizes only.  Host arrays passed in are read during
+ *     the call and may be freed afterwards.
+ *   - One thread at a time per handle; handles are independent.
+ *   - Calls that take a cudaStream_t-compatible `stream` (passed as void*) are
+ *     asynchronous on that stream; everything else is synchronous.
+ */
+#ifndef QSG_H
+#define QSG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QSG_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    QSG_OK = 0,
+    QSG_ERR_INVALID = 1,      /* bad argument or malformed problem / deck     */
+    QSG_ERR_CUDA = 2,         /* a CUDA runtime call failed                   */
+    QSG_ERR_CAPACITY = 3,     /* a particle store is too small                */
+    QSG_ERR_DEVICE = 4,       /* the kernel raised its device error flag      */
+    QSG_ERR_UNSUPPORTED = 5,  /* feature outside the single-domain hot path   */
+    QSG_ERR_IO = 6,           /* file could not be read                       */
+    QSG_ERR_NO_DEVICE = 7     /* no CUDA device visible                       */
+};
+
+/* Device error flag bits reported by qsg_device_status (QSG_ERR_DEVICE). */
+enum {
+    QSG_DEV_SEGMENT_LIMIT = 1u << 0,    /* a history exceeded max_segments    */
+    QSG_DEV_TRACKING_LIMIT = 1u << 1,   /* 10000 facet retries (MCT.cc:518)   */
+    QSG_DEV_NO_REACTION = 1u << 2,      /* reaction sampling found none       */
+    QSG_DEV_OFF_PROCESSOR = 1u << 3,    /* Transit_Off_Processor facet hit    */
+    QSG_DEV_STORE_OVERFLOW = 1u << 4,   /* census / extra store overflow      */
+    QSG_DEV_BAD_FACET = 1u << 5,        /* no facet bounds the particle       */
+    QSG_DEV_NEGATIVE_DISTANCE = 1u << 6 /* MC_Segment_Outcome.cc:265-276      */
+};
+
+/* ---- enums shared with the reference ------------------------------------ */
+/* MC_Tally_Event::Enum, Tallies.hh:22-34 (persisted in the particle record). */
+enum {
+    QSG_EVENT_COLLISION = 0,
+    QSG_EVENT_FACET_TRANSIT_EXIT = 1,
+    QSG_EVENT_CENSUS = 2,
+    QSG_EVENT_FACET_TRACKING_ERROR = 3,
+    QSG_EVENT_FACET_ESCAPE = 4,
+    QSG_EVENT_FACET_REFLECTION = 5,
+    QSG_EVENT_FACET_COMMUNICATION = 6
+};
+/* MC_Subfacet_Adjacency_Event::Enum, MC_Facet_Adjacency.hh:11-20. */
+enum {
+    QSG_ADJ_UNDEFINED = 0,
+    QSG_ADJ_BOUNDARY_ESCAPE = 1,
+    QSG_ADJ_BOUNDARY_REFLECTION = 2,
+    QSG_ADJ_TRANSIT_ON_PROCESSOR = 3,
+    QSG_ADJ_TRANSIT_OFF_PROCESSOR = 4
+};
+/* NuclearDataReaction::Enum, NuclearData.hh:33-40. */
+enum { QSG_REACT_UNDEFINED = 0, QSG_REACT_SCATTER = 1, QSG_REACT_ABSORPTION = 2, QSG_REACT_FISSION = 3 };
+
+/* Balance counter slots, in the order Tallies::CycleFinalize packs them for
+ * its allreduce (Tallies.cc:400-414). */
+enum {
+    QSG_BAL_ABSORB = 0, QSG_BAL_CENSUS, QSG_BAL_ESCAPE, QSG_BAL_COLLISION, QSG_BAL_END,
+    QSG_BAL_FISSION, QSG_BAL_PRODUCE, QSG_BAL_SCATTER, QSG_BAL_START, QSG_BAL_SOURCE,
+    QSG_BAL_RR, QSG_BAL_SPLIT, QSG_BAL_NUM_SEGMENTS, QSG_BAL_COUNT
+};
+
+/* ---- problem description ------------------------------------------------ */
+/*
+ * Read-only tables of one spatial domain, as built by initMC
+ * (initMC.cc:130-320).  The caller fills it from its own MonteCarlo object
+ * (NuclearData, MaterialDatabase, MC_Domain) or from qsg_deck_build().
+ * Cell-local node numbering: facet f of cell c uses the nodes
+ * cell_points[c*14 + facet_local_points[f*3 + k]] for k = 0,1,2 -- this is how
+ * MC_Domain.cc:41-46,292-303 builds facets; facet_local_points is shared by
+ * all cells and validated against facet_points when both are given.
+ */
+typedef struct QsgProblem {
+    int32_t num_groups;                 /* G                                  */
+    const double* energies;             /* [G+1] group edges (NuclearData.cc:105-119) */
+
+    int32_t num_isotopes;
+    const int32_t* isotope_reaction_offset; /* [num_isotopes+1]               */
+    const int32_t* reaction_type;       /* [R] QSG_REACT_*                    */
+    const double* reaction_nubar;       /* [R]                                */
+    const double* reaction_xs;          /* [R*G] microscopic cross sections   */
+
+    int32_t num_materials;
+    const int32_t* material_isotope_offset; /* [num_materials+1]              */
+    const int32_t* material_isotope_gid;    /* isotope index per entry        */
+    const double* material_atom_fraction;   /* per entry                      */
+    const double* material_mass;           /* [num_materials]                */
+
+    int32_t num_cells;
+    int32_t num_nodes;
+    const double* nodes;                /* [num_nodes*3]                      */
+    const int32_t* cell_points;         /* [num_cells*14] node indices        */
+    const int32_t* facet_local_points;  /* [24*3] indices into a cell's 14 points */
+    const double* facet_planes;         /* [num_cells*24*4] A,B,C,D           */
+    const int32_t* facet_event;         /* [num_cells*24] QSG_ADJ_*           */
+    const int32_t* facet_adjacent_cell; /* [num_cells*24]                     */
+    const int32_t* facet_adjacent_facet;/* [num_cells*24]                     */
+    const int32_t* cell_material;       /* [num_cells]                        */
+    const double* cell_number_density;  /* [num_cells]                        */
+    const double* cell_volume;          /* [num_cells]                        */
+    const uint64_t* cell_id;            /* [num_cells] MC_Cell_State::_id     */
+
+    double time_step;                   /* MC_Time_Info::time_step            */
+} QsgProblem;
+
+/* Structure-of-arrays view of MC_Base_Particle (MC_Base_Particle.hh:75-92).
+ * `cell` is the domain-local cell index. */
+typedef struct QsgParticleSoA {
+    double *x, *y, *z;
+    double *vx, *vy, *vz;
+    double *kinetic_energy, *weight, *time_to_census, *age, *num_mean_free_paths, *num_segments;
+    uint64_t *random_number_seed, *identifier;
+    int32_t *last_event, *num_collisions, *breed, *species, *domain, *cell;
+} QsgParticleSoA;
+
+/* Tuning and sizing knobs; zero-initialise and set what you need. */
+typedef struct QsgOptions {
+    int32_t device;              /* CUDA ordinal (default 0)                   */
+    int32_t block_size;          /* threads per block for tracking (0 = auto)  */
+    int32_t flux_replicas;       /* privatised flux copies (0 = 1)             */
+    int32_t balance_replicas;    /* privatised counter copies (0 = 1)          */
+    uint64_t particle_capacity;  /* per store (0 = grow on demand)             */
+    uint64_t max_segments;       /* per history per launch guard (0 = 2^40)    */
+} QsgOptions;
+
+typedef struct QsgHandle QsgHandle;
+
+/* ---- library ------------------------------------------------------------ */
+int qsg_abi_version(void);
+/* Copies the last error text of the calling thread (always NUL-terminated). */
+int qsg_last_error(char* buf, size_t len);
+/* Number of visible CUDA devices (0 when none; never fails on a CPU host). */
+int qsg_device_count(int* count);
+
+/* ---- tracking handle ----------------------------------------------------- */
+/* Copies every table into device memory owned by the handle
+ * (replaces the UVM placement of initMC.cc:56-62,132-146). */
+int qsg_create(const QsgProblem* problem, const QsgOptions* options, QsgHandle** out);
+int qsg_destroy(QsgHandle* h);
+
+/* Start a cycle from n host particles (H2D copy): they replace the processing
+ * store and the processed (census) store is emptied.  Replaces handing the
+ * processing ParticleVaults to CycleTrackingKernel. */
+int qsg_set_particles(QsgHandle* h, const QsgParticleSoA* host, uint64_t n);
+/* Start a cycle from the census of the previous one without leaving the
+ * device: the processed store becomes the processing store
+ * (swapProcessingProcessedVaults, ParticleVaultContainer.cc:278-311). */
+int qsg_begin_cycle_from_census(QsgHandle* h, uint64_t* n);
+/* Number of particles in the processing / processed (census) stores. */
+int qsg_sizes(QsgHandle* h, uint64_t* processing, uint64_t* processed);
+/* Copy up to `cap` census particles to host arrays (D2H); *n_out = count.
+ * Replaces reading the processed ParticleVaults after the launch. */
+int qsg_get_census(QsgHandle* h, QsgParticleSoA* host, uint64_t cap, uint64_t* n_out);
+
+/* Track every particle of the processing store to census, escape, absorption
+ * or fission; fission products (ParticleVaultContainer::addExtraParticle) are
+ * tracked in follow-up passes inside the same call, as cycleTracking's
+ * while(!done) loop does (main.cc:155-299).  Census particles are appended to
+ * the processed store.  Asynchronous on `stream` (a cudaStream_t or NULL). */
+int qsg_track_cycle(QsgHandle* h, void* stream);
+/* Like qsg_track_cycle, but synchronous and reporting the device error flag
+ * as QSG_ERR_DEVICE. */
+int qsg_track_cycle_sync(QsgHandle* h);
+
+/* Balance counters summed over replicas (13 x u64, QSG_BAL_* order) and the
+ * scalar flux [num_cells*G] summed over replicas (Tallies.cc:16-23,75-96). */
+int qsg_read_tallies(QsgHandle* h, uint64_t* balance, double* flux);
+/* Zero counters and flux (Tallies::CycleFinalize reset, Tallies.cc:63-96). */
+int qsg_reset_tallies(QsgHandle* h);
+/* Device error flag bits (QSG_DEV_*) raised since the last reset, and clear. */
+int qsg_device_status(QsgHandle* h, uint32_t* flags, int clear);
+
+/* Device pointers of the stores, for zero-copy callers (e.g. torch). */
+int qsg_processing_view(QsgHandle* h, QsgParticleSoA* device_view, uint64_t* n);
+int qsg_processed_view(QsgHandle* h, QsgParticleSoA* device_view, uint64_t* n);
+
+/* ---- input deck (host only; no CUDA calls) ------------------------------- */
+/* Parser for Quicksilver's input-deck format (Parameters.cc:280-493,
+ * parseUtils.cc:17-87): blocks Simulation / Geometry / Material /
+ * CrossSection with `key: value` lines; unknown keys are ignored;
+ * supplyDefaults (Parameters.cc:350-379) applies when no Geometry is given. */
+typedef struct QsgDeck QsgDeck;
+int qsg_deck_parse_file(const char* path, QsgDeck** out);
+int qsg_deck_parse_string(const char* text, QsgDeck** out);
+/* Command-line style override of a Simulation key (Parameters.cc:230-255). */
+int qsg_deck_set(QsgDeck* deck, const char* key, const char* value);
+int qsg_deck_free(QsgDeck* deck);
+/* Simulation block values as a flat struct. */
+typedef struct QsgSimulation {
+    double dt, lx, ly, lz, e_min, e_max, low_weight_cutoff;
+    uint64_t n_particles, batch_size, n_batches;
+    int32_t n_steps, nx, ny, nz, seed, x_dom, y_dom, z_dom, n_groups;
+    int32_t load_balance, balance_replications, flux_replications, cell_replications, coral_benchmark;
+    int32_t boundary_condition; /* 0 reflect, 1 escape, 2 octant */
+} QsgSimulation;
+int qsg_deck_simulation(const QsgDeck* deck, QsgSimulation* out);
+
+/* Host-built problem tables (initNuclearData / initMesh restated,
+ * initMC.cc:130-320, NuclearData.cc:12-187, MC_Domain.cc:77-394,
+ * GlobalFccGrid.cc:17-131) for a single domain covering the whole grid. */
+typedef struct QsgHostProblem QsgHostProblem;
+int qsg_deck_build(const QsgDeck* deck, QsgHostProblem** out);
+int qsg_host_problem_view(const QsgHostProblem* hp, QsgProblem* view);
+/* Per-material source rate (MaterialParameters::sourceRate), indexed like
+ * QsgProblem materials. */
+int qsg_host_problem_source_rates(const QsgHostProblem* hp, double* rates, int32_t n);
+/* Scale reaction cross sections: for every isotope of `material`, every
+ * reaction of `reaction_type` and groups [g_lo, g_hi): xs *= factor. */
+int qsg_host_problem_scale_xs(QsgHostProblem* hp, int32_t material, int32_t reaction_type,
+                              int32_t g_lo, int32_t g_hi, double factor);
+int qsg_host_problem_free(QsgHostProblem* hp);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QSG_H */

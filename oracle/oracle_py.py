@@ -1,0 +1,172 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes binding of the C oracle (qs_oracle.c).
+
+Used by tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg as
+the checker.  Builds ``oracle/_build/libqs_oracle.so`` on first use with the
+recipe in ``oracle/Makefile``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ORACLE_DIR = Path(__file__).resolve().parent
+LIB_PATH = ORACLE_DIR / "_build" / "libqs_oracle.so"
+
+# same 136-byte record as MC_Base_Particle / quicksilver_gb300._native.PARTICLE_DTYPE
+PARTICLE_DTYPE = np.dtype([
+    ("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("vx", "<f8"), ("vy", "<f8"), ("vz", "<f8"),
+    ("kinetic_energy", "<f8"), ("weight", "<f8"), ("time_to_census", "<f8"), ("age", "<f8"),
+    ("num_mean_free_paths", "<f8"), ("num_segments", "<f8"),
+    ("random_number_seed", "<u8"), ("identifier", "<u8"),
+    ("last_event", "<i4"), ("num_collisions", "<i4"), ("breed", "<i4"), ("species", "<i4"),
+    ("domain", "<i4"), ("cell", "<i4"),
+])
+
+_lib = None
+
+
+def build() -> Path:
+    srcs = [ORACLE_DIR / "qs_oracle.c", ORACLE_DIR / "qs_oracle.h", ORACLE_DIR.parent / "include" / "qsg.h"]
+    if not LIB_PATH.exists() or any(s.stat().st_mtime > LIB_PATH.stat().st_mtime for s in srcs):
+        res = subprocess.run(["make", "-C", str(ORACLE_DIR), "port"], capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
+    return LIB_PATH
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        h = C.CDLL(str(LIB_PATH))
+        vp = C.c_void_p
+        h.oracle_create.argtypes = [vp, C.POINTER(C.c_double), C.c_uint64, C.c_double, C.c_double,
+                                    C.c_double, C.c_int]
+        h.oracle_create.restype = vp
+        h.oracle_destroy.argtypes = [vp]
+        h.oracle_destroy.restype = None
+        for name in ("oracle_cycle_init", "oracle_cycle_finalize"):
+            getattr(h, name).argtypes = [vp]
+            getattr(h, name).restype = C.c_int
+        h.oracle_cycle_tracking.argtypes = [vp, C.c_int]
+        h.oracle_cycle_tracking.restype = C.c_int
+        for name in ("oracle_num_processing", "oracle_num_processed", "oracle_warning_count"):
+            getattr(h, name).argtypes = [vp]
+            getattr(h, name).restype = C.c_uint64
+        for name in ("oracle_processing", "oracle_processed", "oracle_flux"):
+            getattr(h, name).argtypes = [vp]
+            getattr(h, name).restype = vp
+        h.oracle_set_processing.argtypes = [vp, vp, C.c_uint64]
+        h.oracle_set_processing.restype = C.c_int
+        for name in ("oracle_balance", "oracle_last_balance"):
+            getattr(h, name).argtypes = [vp, C.POINTER(C.c_uint64)]
+            getattr(h, name).restype = None
+        h.oracle_track.argtypes = [vp, vp, C.c_uint64, vp, C.c_uint64, C.POINTER(C.c_uint64),
+                                   C.POINTER(C.c_uint64), C.POINTER(C.c_double), C.c_int]
+        h.oracle_track.restype = C.c_int
+        h.oracle_rng_sample.argtypes = [C.POINTER(C.c_uint64)]
+        h.oracle_rng_sample.restype = C.c_double
+        h.oracle_rng_spawn.argtypes = [C.POINTER(C.c_uint64)]
+        h.oracle_rng_spawn.restype = C.c_uint64
+        _lib = h
+    return _lib
+
+
+class OracleRun:
+    """Whole-cycle CPU restatement over a QsgProblem (keeps `keepalive` alive)."""
+
+    def __init__(self, problem_ptr, num_cells: int, num_groups: int, source_rates: np.ndarray,
+                 n_particles: int, e_min: float, e_max: float, low_weight_cutoff: float,
+                 load_balance: int, keepalive=None):
+        self._keep = (keepalive, source_rates)
+        self._rates = np.ascontiguousarray(source_rates, dtype=np.float64)
+        self.num_cells, self.num_groups = num_cells, num_groups
+        self._h = lib().oracle_create(problem_ptr, self._rates.ctypes.data_as(C.POINTER(C.c_double)),
+                                      n_particles, e_min, e_max, low_weight_cutoff, load_balance)
+        if not self._h:
+            raise MemoryError("oracle_create failed")
+
+    def close(self):
+        if self._h:
+            lib().oracle_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def cycle_init(self):
+        if lib().oracle_cycle_init(self._h):
+            raise RuntimeError("oracle_cycle_init failed")
+
+    def cycle_tracking(self, nthreads: int = 0):
+        if lib().oracle_cycle_tracking(self._h, nthreads):
+            raise RuntimeError("oracle_cycle_tracking failed")
+
+    def cycle_finalize(self):
+        lib().oracle_cycle_finalize(self._h)
+
+    def _particles(self, ptr, n) -> np.ndarray:
+        if n == 0:
+            return np.empty(0, dtype=PARTICLE_DTYPE)
+        buf = (C.c_char * (n * PARTICLE_DTYPE.itemsize)).from_address(ptr)
+        return np.frombuffer(buf, dtype=PARTICLE_DTYPE).copy()
+
+    def processing(self) -> np.ndarray:
+        return self._particles(lib().oracle_processing(self._h), lib().oracle_num_processing(self._h))
+
+    def processed(self) -> np.ndarray:
+        return self._particles(lib().oracle_processed(self._h), lib().oracle_num_processed(self._h))
+
+    def set_processing(self, recs: np.ndarray):
+        recs = np.ascontiguousarray(recs, dtype=PARTICLE_DTYPE)
+        if lib().oracle_set_processing(self._h, recs.ctypes.data, len(recs)):
+            raise MemoryError("oracle_set_processing failed")
+
+    def balance(self) -> np.ndarray:
+        out = (C.c_uint64 * 13)()
+        lib().oracle_balance(self._h, out)
+        return np.array(out, dtype=np.uint64)
+
+    def last_balance(self) -> np.ndarray:
+        out = (C.c_uint64 * 13)()
+        lib().oracle_last_balance(self._h, out)
+        return np.array(out, dtype=np.uint64)
+
+    def flux(self) -> np.ndarray:
+        n = self.num_cells * self.num_groups
+        buf = (C.c_double * n).from_address(lib().oracle_flux(self._h))
+        return np.frombuffer(buf, dtype=np.float64).copy().reshape(self.num_cells, self.num_groups)
+
+    def warnings(self) -> int:
+        return int(lib().oracle_warning_count(self._h))
+
+
+def track(problem_ptr, num_cells: int, num_groups: int, particles: np.ndarray, nthreads: int = 0):
+    """One-shot tracking: returns (census records, balance[13], flux[C, G])."""
+    recs = np.ascontiguousarray(particles, dtype=PARTICLE_DTYPE)
+    n = len(recs)
+    cap = max(4 * n + 16, 1024)
+    census = np.empty(cap, dtype=PARTICLE_DTYPE)
+    bal = (C.c_uint64 * 13)()
+    flux = np.zeros(num_cells * num_groups, dtype=np.float64)
+    n_census = C.c_uint64(0)
+    st = lib().oracle_track(problem_ptr, recs.ctypes.data if n else None, n, census.ctypes.data, cap,
+                            C.byref(n_census), bal, flux.ctypes.data_as(C.POINTER(C.c_double)), nthreads)
+    if st:
+        raise RuntimeError(f"oracle_track failed ({st})")
+    return census[: n_census.value].copy(), np.array(bal, dtype=np.uint64), flux.reshape(num_cells, num_groups)
+
+
+def rng_sample(seed: int):
+    s = C.c_uint64(seed)
+    v = lib().oracle_rng_sample(C.byref(s))
+    return v, s.value
+
+
+def rng_spawn(seed: int):
+    s = C.c_uint64(seed)
+    child = lib().oracle_rng_spawn(C.byref(s))
+    return child, s.value

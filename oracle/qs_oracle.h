@@ -1,0 +1,77 @@
+/*
+ * qs_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of Quicksilver's cycle (source, population control,
+ * roulette, and the cycle-tracking hot path) used as the checker for the
+ * CUDA library.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg may load it.  It is pinned against the reference itself:
+ * tests/golden/ holds vectors produced by the unmodified reference
+ * (oracle/ref_harness.cc, built by `make -C oracle ref`), and the tests check
+ * this oracle reproduces them (balance counters bit for bit, flux and census
+ * particle states to the last bit on the same host).
+ */
+#ifndef QS_ORACLE_H
+#define QS_ORACLE_H
+
+#include <stdint.h>
+#include "qsg.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same fields and order as MC_Base_Particle (MC_Base_Particle.hh:75-92):
+ * 12 doubles, 2 uint64, 6 int32 = 136 bytes. */
+typedef struct OracleParticle {
+    double x, y, z, vx, vy, vz;
+    double kinetic_energy, weight, time_to_census, age, num_mean_free_paths, num_segments;
+    uint64_t random_number_seed, identifier;
+    int32_t last_event, num_collisions, breed, species, domain, cell;
+} OracleParticle;
+
+typedef struct OracleRun OracleRun;
+
+/* Keeps pointers into `problem` and `source_rate` (the caller keeps them alive). */
+OracleRun* oracle_create(const QsgProblem* problem, const double* source_rate,
+                         uint64_t n_particles, double e_min, double e_max,
+                         double low_weight_cutoff, int load_balance);
+void oracle_destroy(OracleRun* run);
+
+/* cycleInit (main.cc:96-121): swap census into processing, MC_SourceNow,
+ * PopulationControl, RouletteLowWeightParticles. */
+int oracle_cycle_init(OracleRun* run);
+/* cycleTracking (main.cc:138-307) with `nthreads` OpenMP threads (0 = all). */
+int oracle_cycle_tracking(OracleRun* run, int nthreads);
+/* cycleFinalize (main.cc:310-324): records _end, keeps the finished cycle's
+ * counters for oracle_last_balance, resets counters and flux. */
+int oracle_cycle_finalize(OracleRun* run);
+
+uint64_t oracle_num_processing(const OracleRun* run);
+uint64_t oracle_num_processed(const OracleRun* run);
+const OracleParticle* oracle_processing(const OracleRun* run);
+const OracleParticle* oracle_processed(const OracleRun* run);
+int oracle_set_processing(OracleRun* run, const OracleParticle* p, uint64_t n);
+/* Current counters (13, QSG_BAL_* order) and flux [num_cells*G]. */
+void oracle_balance(const OracleRun* run, uint64_t* out13);
+const double* oracle_flux(const OracleRun* run);
+/* Counters of the cycle most recently finalised. */
+void oracle_last_balance(const OracleRun* run, uint64_t* out13);
+/* Warnings the reference would print and continue from (qs_assert). */
+uint64_t oracle_warning_count(const OracleRun* run);
+
+/* One-shot tracking of a particle set (no cycle init): census particles go to
+ * census_out (capacity cap), counters and flux accumulate into the outputs
+ * (flux must hold num_cells*G doubles, zeroed by the caller). */
+int oracle_track(const QsgProblem* problem, const OracleParticle* in, uint64_t n,
+                 OracleParticle* census_out, uint64_t cap, uint64_t* n_census,
+                 uint64_t* balance13, double* flux, int nthreads);
+
+/* MC_RNG_State restated (MC_RNG_State.hh:22-33, MC_RNG_State.cc:29-113). */
+double oracle_rng_sample(uint64_t* seed);
+uint64_t oracle_rng_spawn(uint64_t* parent_seed);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,187 @@
+"""ctypes binding of libqsg.so (declarations mirror include/qsg.h).
+
+The library is built in-tree by :mod:`quicksilver_gb300.build`.  Loading it
+needs no GPU; every tracking entry point fails with QSG_ERR_NO_DEVICE when no
+CUDA device is visible -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libqsg.so"
+
+QSG_OK = 0
+QSG_ERR_INVALID = 1
+QSG_ERR_CUDA = 2
+QSG_ERR_CAPACITY = 3
+QSG_ERR_DEVICE = 4
+QSG_ERR_UNSUPPORTED = 5
+QSG_ERR_IO = 6
+QSG_ERR_NO_DEVICE = 7
+
+BALANCE_FIELDS = ("absorb", "census", "escape", "collision", "end", "fission", "produce",
+                  "scatter", "start", "source", "rr", "split", "num_segments")
+BAL = {name: i for i, name in enumerate(BALANCE_FIELDS)}
+
+# MC_Base_Particle field order (MC_Base_Particle.hh:75-92), 136 bytes.
+PARTICLE_DTYPE = np.dtype([
+    ("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("vx", "<f8"), ("vy", "<f8"), ("vz", "<f8"),
+    ("kinetic_energy", "<f8"), ("weight", "<f8"), ("time_to_census", "<f8"), ("age", "<f8"),
+    ("num_mean_free_paths", "<f8"), ("num_segments", "<f8"),
+    ("random_number_seed", "<u8"), ("identifier", "<u8"),
+    ("last_event", "<i4"), ("num_collisions", "<i4"), ("breed", "<i4"), ("species", "<i4"),
+    ("domain", "<i4"), ("cell", "<i4"),
+])
+assert PARTICLE_DTYPE.itemsize == 136
+SOA_FIELDS = PARTICLE_DTYPE.names
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_up = C.POINTER(C.c_uint64)
+
+
+class QsgProblem(C.Structure):
+    _fields_ = [
+        ("num_groups", C.c_int32), ("energies", _dp),
+        ("num_isotopes", C.c_int32), ("isotope_reaction_offset", _ip), ("reaction_type", _ip),
+        ("reaction_nubar", _dp), ("reaction_xs", _dp),
+        ("num_materials", C.c_int32), ("material_isotope_offset", _ip), ("material_isotope_gid", _ip),
+        ("material_atom_fraction", _dp), ("material_mass", _dp),
+        ("num_cells", C.c_int32), ("num_nodes", C.c_int32), ("nodes", _dp), ("cell_points", _ip),
+        ("facet_local_points", _ip), ("facet_planes", _dp), ("facet_event", _ip),
+        ("facet_adjacent_cell", _ip), ("facet_adjacent_facet", _ip), ("cell_material", _ip),
+        ("cell_number_density", _dp), ("cell_volume", _dp), ("cell_id", _up),
+        ("time_step", C.c_double),
+    ]
+
+
+class QsgParticleSoA(C.Structure):
+    _fields_ = [(name, _dp) for name in SOA_FIELDS[:12]] + \
+               [(name, _up) for name in SOA_FIELDS[12:14]] + \
+               [(name, _ip) for name in SOA_FIELDS[14:]]
+
+
+class QsgOptions(C.Structure):
+    _fields_ = [("device", C.c_int32), ("block_size", C.c_int32), ("flux_replicas", C.c_int32),
+                ("balance_replicas", C.c_int32), ("particle_capacity", C.c_uint64),
+                ("max_segments", C.c_uint64)]
+
+
+class QsgSimulation(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("dt", "lx", "ly", "lz", "e_min", "e_max", "low_weight_cutoff")] + \
+               [(n, C.c_uint64) for n in ("n_particles", "batch_size", "n_batches")] + \
+               [(n, C.c_int32) for n in ("n_steps", "nx", "ny", "nz", "seed", "x_dom", "y_dom", "z_dom",
+                                         "n_groups", "load_balance", "balance_replications",
+                                         "flux_replications", "cell_replications", "coral_benchmark",
+                                         "boundary_condition")]
+
+
+class QsgError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"qsg error {code}: {message}")
+        self.code = code
+
+
+_lib = None
+_VP = C.c_void_p
+
+_SIGNATURES = {
+    "qsg_abi_version": ([], C.c_int),
+    "qsg_last_error": ([C.c_char_p, C.c_size_t], C.c_int),
+    "qsg_device_count": ([C.POINTER(C.c_int)], C.c_int),
+    "qsg_create": ([C.POINTER(QsgProblem), C.POINTER(QsgOptions), C.POINTER(_VP)], C.c_int),
+    "qsg_destroy": ([_VP], C.c_int),
+    "qsg_set_particles": ([_VP, C.POINTER(QsgParticleSoA), C.c_uint64], C.c_int),
+    "qsg_begin_cycle_from_census": ([_VP, C.POINTER(C.c_uint64)], C.c_int),
+    "qsg_sizes": ([_VP, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], C.c_int),
+    "qsg_get_census": ([_VP, C.POINTER(QsgParticleSoA), C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
+    "qsg_track_cycle": ([_VP, _VP], C.c_int),
+    "qsg_track_cycle_sync": ([_VP], C.c_int),
+    "qsg_read_tallies": ([_VP, _up, _dp], C.c_int),
+    "qsg_reset_tallies": ([_VP], C.c_int),
+    "qsg_device_status": ([_VP, C.POINTER(C.c_uint32), C.c_int], C.c_int),
+    "qsg_processing_view": ([_VP, C.POINTER(QsgParticleSoA), C.POINTER(C.c_uint64)], C.c_int),
+    "qsg_processed_view": ([_VP, C.POINTER(QsgParticleSoA), C.POINTER(C.c_uint64)], C.c_int),
+    "qsg_deck_parse_file": ([C.c_char_p, C.POINTER(_VP)], C.c_int),
+    "qsg_deck_parse_string": ([C.c_char_p, C.POINTER(_VP)], C.c_int),
+    "qsg_deck_set": ([_VP, C.c_char_p, C.c_char_p], C.c_int),
+    "qsg_deck_free": ([_VP], C.c_int),
+    "qsg_deck_simulation": ([_VP, C.POINTER(QsgSimulation)], C.c_int),
+    "qsg_deck_build": ([_VP, C.POINTER(_VP)], C.c_int),
+    "qsg_host_problem_view": ([_VP, C.POINTER(QsgProblem)], C.c_int),
+    "qsg_host_problem_source_rates": ([_VP, _dp, C.c_int32], C.c_int),
+    "qsg_host_problem_scale_xs": ([_VP, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double], C.c_int),
+    "qsg_host_problem_free": ([_VP], C.c_int),
+}
+
+
+def lib() -> C.CDLL:
+    """Load libqsg.so (building it first if it is missing)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            from . import build as _build
+            _build.build()
+        handle = C.CDLL(str(LIB_PATH))
+        for name, (args, res) in _SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = handle
+    return _lib
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(2048)
+    lib().qsg_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(code: int) -> None:
+    if code != QSG_OK:
+        raise QsgError(code, last_error())
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    check(lib().qsg_device_count(C.byref(n)))
+    return n.value
+
+
+def soa_from_columns(cols: dict) -> QsgParticleSoA:
+    """Build a QsgParticleSoA view over contiguous numpy columns (kept alive by the caller)."""
+    soa = QsgParticleSoA()
+    for name in SOA_FIELDS:
+        arr = cols[name]
+        assert arr.flags["C_CONTIGUOUS"]
+        ctype = dict(QsgParticleSoA._fields_)[name]
+        setattr(soa, name, arr.ctypes.data_as(ctype))
+    return soa
+
+
+def soa_from_pointers(ptrs: dict) -> QsgParticleSoA:
+    """Build a QsgParticleSoA from raw addresses (e.g. device pointers)."""
+    soa = QsgParticleSoA()
+    for name in SOA_FIELDS:
+        ctype = dict(QsgParticleSoA._fields_)[name]
+        setattr(soa, name, C.cast(C.c_void_p(ptrs[name]), ctype))
+    return soa
+
+
+def columns_of(records: np.ndarray) -> dict:
+    """Split a PARTICLE_DTYPE record array into contiguous columns."""
+    return {name: np.ascontiguousarray(records[name]) for name in SOA_FIELDS}
+
+
+def records_from_columns(cols: dict, n: int) -> np.ndarray:
+    out = np.empty(n, dtype=PARTICLE_DTYPE)
+    for name in SOA_FIELDS:
+        out[name] = cols[name][:n]
+    return out
+
+
+def empty_columns(n: int) -> dict:
+    return {name: np.empty(max(n, 1), dtype=PARTICLE_DTYPE[name]) for name in SOA_FIELDS}

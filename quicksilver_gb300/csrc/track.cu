@@ -1,0 +1,1128 @@
+// Cycle-tracking kernel (one thread per history) and the C-ABI handle.
+//
+// Replaces CycleTrackingKernel / CycleTrackingGuts (main.cc:126-134,
+// CycleTracking.cc:14-120) for one spatial domain.  Design:
+//   * particles live in HBM as structure-of-arrays (coalesced 8-byte loads
+//     and stores per field), read once at history start, written once at
+//     census / fission;
+//   * cross sections are pre-reduced per (cross-section class, group): the
+//     reference's per-cell cached total (MacroscopicCrossSection.cc:58-81) is
+//     identical for every cell of one (material, number density) class, so one
+//     table row serves all of them with the same bits;
+//   * mesh tables per cell: 24 planes, the 14 nodes, adjacency packed to
+//     5 bytes per facet -- L2-resident for the benchmark meshes;
+//   * balance counters are accumulated per thread, reduced per block and
+//     added with one 64-bit atomic per counter per block; scalar flux uses
+//     FP64 atomics into `flux_replicas` privatised copies;
+//   * census and fission products are appended with warp-aggregated atomics.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "qsg.h"
+#include "status.h"
+#include "track_device.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace qsg {
+
+enum LocalCounter { LC_SEG = 0, LC_COLL, LC_SCAT, LC_ABS, LC_FIS, LC_PROD, LC_ESC, LC_CEN, LC_N };
+
+__device__ __forceinline__ void raise_flag(const DevTally& tally, unsigned int bit)
+{
+    atomicOr(tally.error_flags, bit);
+}
+
+// Reserve one slot of `s` for each calling lane with one atomic per warp.
+__device__ __forceinline__ uint64_t append_slot(const DevStore& s)
+{
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(s.count, (unsigned long long)g.size());
+    base = g.shfl(base, 0);
+    return base + g.thread_rank();
+}
+
+// MCT_Nearest_Facet_3D_G_Distance_To_Segment, MCT.cc:280-395.
+__device__ __forceinline__ double distance_to_segment(double plane_tolerance, double dot, double A, double B, double C,
+                                                      double D, const double* p0, const double* p1,
+                                                      const double* p2, const Particle& p)
+{
+    const double bb_tol = 1e-9;
+    double numerator = -1.0 * (A * p.x + B * p.y + C * p.z + D);
+    if (numerator < 0.0 && numerator * numerator > plane_tolerance) return kHugeDouble;
+    double distance = numerator / dot;
+    double ip[3];
+    ip[0] = p.x + distance * p.alpha;
+    ip[1] = p.y + distance * p.beta;
+    ip[2] = p.z + distance * p.gamma;
+    int u, v;
+    if (C < -0.5 || C > 0.5) { u = 0; v = 1; }
+    else if (B < -0.5 || B > 0.5) { u = 2; v = 0; }
+    else if (A < -0.5 || A > 0.5) { u = 1; v = 2; }
+    else return kHugeDouble;  // no dominant normal component: crosses stay 0 and the test fails
+    // bounding-box rejects on the two projected axes (first axis u, then v)
+    {
+        double hi = ip[u] + bb_tol, lo = ip[u] - bb_tol;
+        if (p0[u] > hi && p1[u] > hi && p2[u] > hi) return kHugeDouble;
+        if (p0[u] < lo && p1[u] < lo && p2[u] < lo) return kHugeDouble;
+    }
+    {
+        double hi = ip[v] + bb_tol, lo = ip[v] - bb_tol;
+        if (p0[v] > hi && p1[v] > hi && p2[v] > hi) return kHugeDouble;
+        if (p0[v] < lo && p1[v] < lo && p2[v] < lo) return kHugeDouble;
+    }
+    double cross1 = (p1[u] - p0[u]) * (ip[v] - p0[v]) - (p1[v] - p0[v]) * (ip[u] - p0[u]);
+    double cross2 = (p2[u] - p1[u]) * (ip[v] - p1[v]) - (p2[v] - p1[v]) * (ip[u] - p1[u]);
+    double cross0 = (p0[u] - p2[u]) * (ip[v] - p2[v]) - (p0[v] - p2[v]) * (ip[u] - p2[u]);
+    double s = cross0 + cross1 + cross2;
+    double cross_tol = 1e-9 * (s < 0 ? -s : s);
+    if ((cross0 > -cross_tol && cross1 > -cross_tol && cross2 > -cross_tol) ||
+        (cross0 < cross_tol && cross1 < cross_tol && cross2 < cross_tol))
+        return distance;
+    return kHugeDouble;
+}
+
+// MCT_Nearest_Facet (MCT.cc:86-137) with MCT_Nearest_Facet_3D_G
+// (MCT.cc:549-621) and both Find_Nearest overloads (MCT.cc:436-536).
+// Moves the particle toward the cell centre on a retry, as the reference
+// does through its coordinate reference (MCT.cc:510, 656-666).
+__device__ double nearest_facet(const DevTables& t, const DevTally& tally, Particle& p, int& facet_out)
+{
+    const int cell = p.cell;
+    const double* planes = t.planes + (int64_t)cell * (kFacets * 4);
+    const double* nodes = t.cell_nodes + (int64_t)cell * (kCellPoints * 3);
+    int iteration = 0;
+    double move_factor = 0.5 * kSmallDouble;
+    for (;;) {
+        double plane_tolerance = 1e-16 * (p.x * p.x + p.y * p.y + p.z * p.z);
+        double best = 1e80;
+        int best_f = 0;
+        double neg = -kHugeDouble;
+        int neg_f = 0;
+        for (int f = 0; f < kFacets; f++) {
+            const double2 ab = __ldg(reinterpret_cast<const double2*>(planes + 4 * f));
+            const double2 cd = __ldg(reinterpret_cast<const double2*>(planes + 4 * f + 2));
+            double d = kHugeDouble;
+            double dot = ab.x * p.alpha + ab.y * p.beta + cd.x * p.gamma;
+            if (dot > 0.0) {
+                double q0[3], q1[3], q2[3];
+                const double* n0 = nodes + 3 * t.facet_local[f][0];
+                const double* n1 = nodes + 3 * t.facet_local[f][1];
+                const double* n2 = nodes + 3 * t.facet_local[f][2];
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    q0[a] = __ldg(n0 + a);
+                    q1[a] = __ldg(n1 + a);
+                    q2[a] = __ldg(n2 + a);
+                }
+                d = distance_to_segment(plane_tolerance, dot, ab.x, ab.y, cd.x, cd.y, q0, q1, q2, p);
+            }
+            // Find_Nearest: positive distances with `<=` (later facet wins a
+            // tie), otherwise the largest non-positive one.
+            if (d > 0.0) {
+                if (d <= best) { best = d; best_f = f; }
+            } else if (d > neg) {
+                neg = d; neg_f = f;
+            }
+        }
+        if (best == kHugeDouble && neg != -kHugeDouble) { best = neg; best_f = neg_f; }
+        bool retry = false;
+        if ((best == kHugeDouble && move_factor > 0) || (p.num_segments > 10000000 && best <= 0.0)) {
+            const double* c = t.cell_center + 3 * (int64_t)cell;
+            p.x += move_factor * (__ldg(c + 0) - p.x);
+            p.y += move_factor * (__ldg(c + 1) - p.y);
+            p.z += move_factor * (__ldg(c + 2) - p.z);
+            iteration++;
+            move_factor *= 2.0;
+            if (move_factor > 1.0e-2) move_factor = 1.0e-2;
+            if (iteration == 10000) raise_flag(tally, QSG_DEV_TRACKING_LIMIT);
+            else retry = true;
+        }
+        if (!retry) {
+            if (best < 0) best = 0;
+            if (best >= kHugeDouble) raise_flag(tally, QSG_DEV_BAD_FACET);
+            facet_out = best_f;
+            return best;
+        }
+    }
+}
+
+enum { OUT_COLLISION = 0, OUT_FACET = 1, OUT_CENSUS = 2 };
+
+// MC_Segment_Outcome, MC_Segment_Outcome.cc:30-226.
+__device__ __forceinline__ int segment_outcome(const DevTables& t, const DevTally& tally, Particle& p,
+                                               int cls, double* flux_row)
+{
+    double d_coll, d_facet, d_census;
+    double speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
+    bool force_collision = false;
+    if (p.num_mean_free_paths < 0.0) {
+        force_collision = true;
+        p.num_mean_free_paths = kSmallDouble;
+    }
+    double sigma = __ldg(t.sigma_total + (int64_t)cls * t.num_groups + p.group);
+    p.total_xs = sigma;
+    p.mean_free_path = (sigma == 0.0) ? kHugeDouble : 1.0 / sigma;
+    if (p.num_mean_free_paths == 0.0) {
+        double r = rng_sample(p.seed);
+        p.num_mean_free_paths = -1.0 * log(r);
+    }
+    d_coll = force_collision ? kSmallDouble : p.num_mean_free_paths * p.mean_free_path;
+    d_census = speed * p.time_to_census;
+    int facet = 0;
+    d_facet = nearest_facet(t, tally, p, facet);
+    if (p.last_event == QSG_EVENT_FACET_TRACKING_ERROR) return OUT_FACET;
+    if (force_collision) {
+        d_facet = kHugeDouble;
+        d_census = kHugeDouble;
+        d_coll = kTinyDouble;
+    }
+    // MC_Find_Min (MC_Segment_Outcome.cc:232-248): strict <, ties keep the lower index
+    int outcome = OUT_COLLISION;
+    double seg = d_coll;
+    if (d_facet < seg) { seg = d_facet; outcome = OUT_FACET; }
+    if (d_census < seg) { seg = d_census; outcome = OUT_CENSUS; }
+    if (seg < 0) raise_flag(tally, QSG_DEV_NEGATIVE_DISTANCE);
+    p.num_mean_free_paths -= seg / p.mean_free_path;
+    if (outcome == OUT_COLLISION) {
+        p.last_event = QSG_EVENT_COLLISION;
+        p.num_mean_free_paths = 0.0;
+    } else if (outcome == OUT_FACET) {
+        p.last_event = QSG_EVENT_FACET_TRANSIT_EXIT;
+        p.facet = facet;
+    } else {
+        p.last_event = QSG_EVENT_CENSUS;
+        p.time_to_census = (p.time_to_census < 0.0) ? p.time_to_census : 0.0;
+    }
+    if (force_collision) p.num_mean_free_paths = 0.0;
+    if (seg == 0.0) return outcome;
+    p.x += (p.alpha * seg);
+    p.y += (p.beta * seg);
+    p.z += (p.gamma * seg);
+    double seg_time = (seg / speed);
+    p.time_to_census -= seg_time;
+    p.age += seg_time;
+    if (p.time_to_census < 0.0) p.time_to_census = 0.0;
+    atomicAdd(flux_row + (int64_t)p.cell * t.num_groups + p.group, seg * p.weight);
+    return outcome;
+}
+
+// updateTrajectory (CollisionEvent.cc:24-46) with DirectionCosine::
+// Rotate3DVector (DirectionCosine.hh:122-147).
+__device__ __forceinline__ void update_trajectory(double energy, double angle, Particle& p)
+{
+    p.kinetic_energy = energy;
+    double cosTheta = angle;
+    double r = rng_sample(p.seed);
+    double phi = 2 * 3.14159265 * r;
+    double sinPhi, cosPhi;
+    sincos(phi, &sinPhi, &cosPhi);
+    double sinTheta = sqrt((1.0 - (cosTheta * cosTheta)));
+    double cos_theta = p.gamma;
+    double sin_theta = sqrt((1.0 - (cos_theta * cos_theta)));
+    double cos_phi, sin_phi;
+    if (sin_theta < 1e-6) {
+        cos_phi = 1.0;
+        sin_phi = 0.0;
+    } else {
+        cos_phi = p.alpha / sin_theta;
+        sin_phi = p.beta / sin_theta;
+    }
+    double a = cos_theta * cos_phi * (sinTheta * cosPhi) - sin_phi * (sinTheta * sinPhi) + sin_theta * cos_phi * cosTheta;
+    double b = cos_theta * sin_phi * (sinTheta * cosPhi) + cos_phi * (sinTheta * sinPhi) + sin_theta * sin_phi * cosTheta;
+    double g = -sin_theta * (sinTheta * cosPhi) + cos_theta * cosTheta;
+    p.alpha = a;
+    p.beta = b;
+    p.gamma = g;
+    const double m = kNeutronRestMassEnergy;
+    double speed = (kSpeedOfLight * sqrt((1.0 - ((m * m) / ((energy + m) * (energy + m))))));
+    p.vx = speed * p.alpha;
+    p.vy = speed * p.beta;
+    p.vz = speed * p.gamma;
+    r = rng_sample(p.seed);
+    p.num_mean_free_paths = -1.0 * log(r);
+}
+
+// CollisionEvent, CollisionEvent.cc:48-148, with NuclearDataReaction::
+// sampleCollision (NuclearData.cc:52-88).  Returns true to keep tracking.
+__device__ __forceinline__ bool collision_event(const DevTables& t, const DevTally& tally, Particle& p, int cls,
+                                                const DevStore& extra, uint32_t* cnt)
+{
+    const int G = t.num_groups;
+    const int K = t.max_reactions;
+    const int nk = __ldg(t.class_num_reactions + cls);
+    const double* row = t.macro_xs + ((int64_t)cls * G + p.group) * K;
+    double current = p.total_xs * rng_sample(p.seed);
+    int sel = -1;
+    for (int k = 0; k < nk; k++) {
+        current -= __ldg(row + k);
+        if (current < 0) { sel = k; break; }
+    }
+    if (sel < 0) {
+        // the reference asserts and carries on with an invalid index
+        // (CollisionEvent.cc:84); flag it and take the class's last reaction
+        raise_flag(tally, QSG_DEV_NO_REACTION);
+        sel = nk - 1;
+    }
+    const int type = t.class_reaction_type[cls * K + sel];
+    const double mass = __ldg(t.material_mass + __ldg(t.class_material + cls));
+    double e_out[4], a_out[4];
+    int n_out = 0;
+    if (type == QSG_REACT_SCATTER) {
+        n_out = 1;
+        double rn = rng_sample(p.seed);
+        e_out[0] = p.kinetic_energy * (1.0 - (rn * (1.0 / mass)));
+        rn = rng_sample(p.seed) * 2.0 - 1.0;
+        a_out[0] = rn;
+    } else if (type == QSG_REACT_FISSION) {
+        int num = (int)(__ldg(t.class_reaction_nubar + cls * K + sel) + rng_sample(p.seed));
+        if (num > 4) num = 4;  // nuBar < 4 is checked at qsg_create
+        n_out = num;
+        for (int o = 0; o < num; o++) {
+            double rn = rng_sample(p.seed) / 2.0 + 0.5;
+            e_out[o] = (20 * rn * rn);
+            rn = rng_sample(p.seed) * 2.0 - 1.0;
+            a_out[o] = rn;
+        }
+    }
+    cnt[LC_COLL]++;
+    if (type == QSG_REACT_SCATTER) cnt[LC_SCAT]++;
+    else if (type == QSG_REACT_ABSORPTION) cnt[LC_ABS]++;
+    else if (type == QSG_REACT_FISSION) {
+        cnt[LC_FIS]++;
+        cnt[LC_PROD] += (uint32_t)n_out;
+    }
+    if (n_out == 0) return false;
+    for (int s = 1; s < n_out; s++) {
+        Particle sec = p;
+        sec.seed = rng_spawn(p.seed);
+        sec.identifier = sec.seed;
+        update_trajectory(e_out[s], a_out[s], sec);
+        uint64_t slot = append_slot(extra);
+        if (slot < extra.capacity) store_particle(extra, slot, sec);
+        else raise_flag(tally, QSG_DEV_STORE_OVERFLOW);
+    }
+    update_trajectory(e_out[0], a_out[0], p);
+    if (n_out > 1) {
+        uint64_t slot = append_slot(extra);
+        if (slot < extra.capacity) store_particle(extra, slot, p);
+        else raise_flag(tally, QSG_DEV_STORE_OVERFLOW);
+    }
+    p.group = energy_group(t, p.kinetic_energy);
+    return n_out == 1;
+}
+
+// MCT_Reflect_Particle, MCT.cc:400-430.
+__device__ __forceinline__ void reflect_particle(const DevTables& t, Particle& p)
+{
+    const double* pl = t.planes + ((int64_t)p.cell * kFacets + p.facet) * 4;
+    double nx = __ldg(pl + 0), ny = __ldg(pl + 1), nz = __ldg(pl + 2);
+    double dot = 2.0 * (p.alpha * nx + p.beta * ny + p.gamma * nz);
+    if (dot > 0) {
+        p.alpha -= dot * nx;
+        p.beta -= dot * ny;
+        p.gamma -= dot * nz;
+    }
+    double speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
+    p.vx = speed * p.alpha;
+    p.vy = speed * p.beta;
+    p.vz = speed * p.gamma;
+}
+
+__device__ __forceinline__ int balance_slot(int local)
+{
+    switch (local) {
+    case LC_SEG: return QSG_BAL_NUM_SEGMENTS;
+    case LC_COLL: return QSG_BAL_COLLISION;
+    case LC_SCAT: return QSG_BAL_SCATTER;
+    case LC_ABS: return QSG_BAL_ABSORB;
+    case LC_FIS: return QSG_BAL_FISSION;
+    case LC_PROD: return QSG_BAL_PRODUCE;
+    case LC_ESC: return QSG_BAL_ESCAPE;
+    default: return QSG_BAL_CENSUS;
+    }
+}
+
+template <int BLOCK>
+__device__ __forceinline__ void flush_counters(const DevTally& tally, uint32_t* cnt, int replica)
+{
+    __shared__ unsigned long long red[BLOCK / 32][LC_N];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < LC_N; k++) {
+        unsigned long long v = cnt[k];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) red[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < LC_N) {
+        unsigned long long sum = 0;
+        for (int w = 0; w < BLOCK / 32; w++) sum += red[w][threadIdx.x];
+        if (sum) atomicAdd(tally.balance + (int64_t)replica * QSG_BAL_COUNT + balance_slot(threadIdx.x), sum);
+    }
+}
+
+// One thread per particle of `in`: CycleTrackingGuts + CycleTrackingFunction
+// (CycleTracking.cc:14-120).
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) track_kernel(DevTables t, DevTally tally, DevStore in, uint64_t n,
+                                                      DevStore census, DevStore extra)
+{
+    uint32_t cnt[LC_N];
+#pragma unroll
+    for (int k = 0; k < LC_N; k++) cnt[k] = 0;
+    const uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
+    if (i < n) {
+        Particle p;
+        load_particle(t, in, i, p);
+        if (!(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz > 0.0)) raise_flag(tally, QSG_DEV_BAD_FACET);
+        // CycleTracking.cc:37-39 replica selection by particle index
+        double* flux_row = tally.flux + (int64_t)(i % (uint64_t)tally.flux_replicas) * t.num_cells * t.num_groups;
+        uint64_t segs_this_launch = 0;
+        bool keep;
+        do {
+            const int cls = __ldg(t.cell_class + p.cell);
+            int outcome = segment_outcome(t, tally, p, cls, flux_row);
+            cnt[LC_SEG]++;
+            p.num_segments += 1.;
+            if (outcome == OUT_COLLISION) {
+                keep = collision_event(t, tally, p, cls, extra, cnt);
+            } else if (outcome == OUT_FACET) {
+                // MC_Facet_Crossing_Event, MC_Facet_Crossing_Event.cc:23-70
+                const int64_t fi = (int64_t)p.cell * kFacets + p.facet;
+                const uint8_t fe = __ldg(t.adj_facet_event + fi);
+                const int ev = fe >> 5;
+                if (ev == QSG_ADJ_TRANSIT_ON_PROCESSOR) {
+                    p.cell = __ldg(t.adj_cell + fi);
+                    p.facet = fe & 31;
+                    p.last_event = QSG_EVENT_FACET_TRANSIT_EXIT;
+                    keep = true;
+                } else if (ev == QSG_ADJ_BOUNDARY_ESCAPE) {
+                    cnt[LC_ESC]++;
+                    p.last_event = QSG_EVENT_FACET_ESCAPE;
+                    p.species = -1;
+                    keep = false;
+                } else if (ev == QSG_ADJ_BOUNDARY_REFLECTION) {
+                    p.last_event = QSG_EVENT_FACET_REFLECTION;
+                    reflect_particle(t, p);
+                    keep = true;
+                } else {
+                    raise_flag(tally, QSG_DEV_OFF_PROCESSOR);
+                    keep = false;
+                }
+            } else {
+                // census: ParticleVault::pushParticle (ParticleVault.hh:86-93)
+                uint64_t slot = append_slot(census);
+                if (slot < census.capacity) store_particle(census, slot, p);
+                else raise_flag(tally, QSG_DEV_STORE_OVERFLOW);
+                cnt[LC_CEN]++;
+                keep = false;
+            }
+            if (keep && ++segs_this_launch >= tally.max_segments) {
+                raise_flag(tally, QSG_DEV_SEGMENT_LIMIT);
+                keep = false;
+            }
+        } while (keep);
+    }
+    flush_counters<BLOCK>(tally, cnt, (int)(blockIdx.x % (unsigned)tally.balance_replicas));
+}
+
+constexpr int kTrackBlock = 128;
+
+// ------------------------------------------------------------------------
+// Host side.
+
+#define QSG_CUDA(call)                                                                      \
+    do {                                                                                    \
+        cudaError_t err__ = (call);                                                         \
+        if (err__ != cudaSuccess)                                                           \
+            return ::qsg::fail(QSG_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(err__)); \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T* ptr = nullptr;
+    size_t n = 0;
+    int alloc(size_t count)
+    {
+        free();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc(&ptr, count * sizeof(T));
+        if (e != cudaSuccess) {
+            ptr = nullptr;
+            return fail(QSG_ERR_CUDA, "cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(e));
+        }
+        n = count;
+        return QSG_OK;
+    }
+    int upload(const std::vector<T>& v)
+    {
+        int st = alloc(v.size());
+        if (st) return st;
+        if (!v.empty()) QSG_CUDA(cudaMemcpy(ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+        return QSG_OK;
+    }
+    void free()
+    {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        n = 0;
+    }
+};
+
+// One particle store: 20 field arrays carved out of one allocation.
+struct Store {
+    void* base = nullptr;
+    unsigned long long* count = nullptr;  // device counter
+    uint64_t capacity = 0;
+    DevStore view{};
+
+    int reserve(uint64_t cap)
+    {
+        if (cap <= capacity && base) return QSG_OK;
+        uint64_t nc = capacity ? capacity : 1024;
+        while (nc < cap) nc *= 2;
+        size_t bytes = nc * 136 + 256 * 21;
+        void* nb = nullptr;
+        cudaError_t e = cudaMalloc(&nb, bytes);
+        if (e != cudaSuccess) return fail(QSG_ERR_CUDA, "cudaMalloc store (%zu bytes): %s", bytes, cudaGetErrorString(e));
+        DevStore nv = carve(nb, nc);
+        if (base) {
+            unsigned long long n_old = 0;
+            e = cudaMemcpy(&n_old, count, sizeof(n_old), cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess && n_old) e = copy_fields(nv, view, 0, 0, std::min<uint64_t>(n_old, capacity));
+            if (e == cudaSuccess) e = cudaMemcpy(nv.count, &n_old, sizeof(n_old), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) {
+                cudaFree(nb);
+                return fail(QSG_ERR_CUDA, "store grow: %s", cudaGetErrorString(e));
+            }
+            cudaFree(base);
+        } else {
+            e = cudaMemset(nv.count, 0, sizeof(unsigned long long));
+            if (e != cudaSuccess) {
+                cudaFree(nb);
+                return fail(QSG_ERR_CUDA, "store init: %s", cudaGetErrorString(e));
+            }
+        }
+        base = nb;
+        view = nv;
+        count = nv.count;
+        capacity = nc;
+        return QSG_OK;
+    }
+
+    static DevStore carve(void* b, uint64_t cap)
+    {
+        DevStore v{};
+        char* p = static_cast<char*>(b);
+        auto take = [&](size_t esz) {
+            char* r = p;
+            p += (cap * esz + 255) & ~size_t(255);
+            return r;
+        };
+        v.count = reinterpret_cast<unsigned long long*>(p);
+        p += 256;
+        double** dfields[12] = {&v.x, &v.y, &v.z, &v.vx, &v.vy, &v.vz, &v.kinetic_energy, &v.weight,
+                                &v.time_to_census, &v.age, &v.num_mean_free_paths, &v.num_segments};
+        for (double** f : dfields) *f = reinterpret_cast<double*>(take(8));
+        v.seed = reinterpret_cast<uint64_t*>(take(8));
+        v.identifier = reinterpret_cast<uint64_t*>(take(8));
+        int32_t** ifields[6] = {&v.last_event, &v.num_collisions, &v.breed, &v.species, &v.domain, &v.cell};
+        for (int32_t** f : ifields) *f = reinterpret_cast<int32_t*>(take(4));
+        v.capacity = cap;
+        return v;
+    }
+
+    static cudaError_t copy_fields(const DevStore& dst, const DevStore& src, uint64_t dst_off, uint64_t src_off,
+                                   uint64_t n, cudaStream_t s = 0)
+    {
+        if (n == 0) return cudaSuccess;
+        double* dd[12] = {dst.x, dst.y, dst.z, dst.vx, dst.vy, dst.vz, dst.kinetic_energy, dst.weight,
+                          dst.time_to_census, dst.age, dst.num_mean_free_paths, dst.num_segments};
+        double* sd[12] = {src.x, src.y, src.z, src.vx, src.vy, src.vz, src.kinetic_energy, src.weight,
+                          src.time_to_census, src.age, src.num_mean_free_paths, src.num_segments};
+        for (int k = 0; k < 12; k++) {
+            cudaError_t e = cudaMemcpyAsync(dd[k] + dst_off, sd[k] + src_off, n * 8, cudaMemcpyDeviceToDevice, s);
+            if (e != cudaSuccess) return e;
+        }
+        uint64_t* du[2] = {dst.seed, dst.identifier};
+        uint64_t* su[2] = {src.seed, src.identifier};
+        for (int k = 0; k < 2; k++) {
+            cudaError_t e = cudaMemcpyAsync(du[k] + dst_off, su[k] + src_off, n * 8, cudaMemcpyDeviceToDevice, s);
+            if (e != cudaSuccess) return e;
+        }
+        int32_t* di[6] = {dst.last_event, dst.num_collisions, dst.breed, dst.species, dst.domain, dst.cell};
+        int32_t* si[6] = {src.last_event, src.num_collisions, src.breed, src.species, src.domain, src.cell};
+        for (int k = 0; k < 6; k++) {
+            cudaError_t e = cudaMemcpyAsync(di[k] + dst_off, si[k] + src_off, n * 4, cudaMemcpyDeviceToDevice, s);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+
+    void release()
+    {
+        if (base) cudaFree(base);
+        base = nullptr;
+        count = nullptr;
+        capacity = 0;
+        view = DevStore{};
+    }
+};
+
+}  // namespace qsg
+
+struct QsgHandle {
+    int device = 0;
+    int block_size = qsg::kTrackBlock;
+    int32_t flux_replicas = 1, balance_replicas = 1;
+    uint64_t max_segments = (uint64_t)1 << 40;
+    int32_t num_cells = 0, num_groups = 0;
+    // tables
+    qsg::DevBuf<double> energies, sigma_total, macro_xs, class_nubar, material_mass, cell_nodes, cell_center, planes;
+    qsg::DevBuf<int32_t> class_num_reactions, class_material, cell_class, adj_cell;
+    qsg::DevBuf<int8_t> class_type;
+    qsg::DevBuf<uint8_t> adj_facet_event;
+    qsg::DevTables tables{};
+    // tallies
+    qsg::DevBuf<double> flux;
+    qsg::DevBuf<unsigned long long> balance;
+    qsg::DevBuf<unsigned int> flags;
+    // particle stores: processing, processed (census), extra (fission products)
+    qsg::Store processing, processed, extra;
+    uint64_t n_processing = 0;   // host mirror of processing count
+};
+
+namespace qsg {
+namespace {
+
+int set_device(const QsgHandle* h) {
+    QSG_CUDA(cudaSetDevice(h->device));
+    return QSG_OK;
+}
+
+DevTally tally_view(QsgHandle* h)
+{
+    DevTally t{};
+    t.flux = h->flux.ptr;
+    t.balance = h->balance.ptr;
+    t.error_flags = h->flags.ptr;
+    t.flux_replicas = h->flux_replicas;
+    t.balance_replicas = h->balance_replicas;
+    t.max_segments = h->max_segments;
+    return t;
+}
+
+int validate_problem(const QsgProblem* p)
+{
+    if (p->num_groups < 1 || !p->energies) return fail(QSG_ERR_INVALID, "problem: num_groups/energies missing");
+    if (p->num_isotopes < 1 || !p->isotope_reaction_offset || !p->reaction_type || !p->reaction_nubar ||
+        !p->reaction_xs)
+        return fail(QSG_ERR_INVALID, "problem: nuclear data missing");
+    if (p->num_materials < 1 || !p->material_isotope_offset || !p->material_isotope_gid ||
+        !p->material_atom_fraction || !p->material_mass)
+        return fail(QSG_ERR_INVALID, "problem: materials missing");
+    if (p->num_cells < 1 || !p->nodes || !p->cell_points || !p->facet_local_points || !p->facet_planes ||
+        !p->facet_event || !p->facet_adjacent_cell || !p->facet_adjacent_facet || !p->cell_material ||
+        !p->cell_number_density)
+        return fail(QSG_ERR_INVALID, "problem: mesh tables missing");
+    for (int k = 0; k < 72; k++)
+        if (p->facet_local_points[k] < 0 || p->facet_local_points[k] >= kCellPoints)
+            return fail(QSG_ERR_INVALID, "problem: facet_local_points must index a cell's 14 points");
+    for (int i = 0; i < p->num_isotopes; i++)
+        if (p->isotope_reaction_offset[i + 1] < p->isotope_reaction_offset[i])
+            return fail(QSG_ERR_INVALID, "problem: isotope_reaction_offset not monotone");
+    const int R = p->isotope_reaction_offset[p->num_isotopes];
+    for (int r = 0; r < R; r++) {
+        if (p->reaction_type[r] < QSG_REACT_SCATTER || p->reaction_type[r] > QSG_REACT_FISSION)
+            return fail(QSG_ERR_INVALID, "problem: reaction %d has undefined type", r);
+        if (p->reaction_type[r] == QSG_REACT_FISSION && !(p->reaction_nubar[r] < 4.0))
+            return fail(QSG_ERR_INVALID, "problem: fission nuBar %.17g can exceed the 4 products per collision "
+                        "(CollisionEvent.cc:15)", p->reaction_nubar[r]);
+    }
+    for (int m = 0; m < p->num_materials; m++) {
+        int k0 = p->material_isotope_offset[m], k1 = p->material_isotope_offset[m + 1];
+        if (k1 <= k0) return fail(QSG_ERR_INVALID, "problem: material %d has no isotopes", m);
+        for (int k = k0; k < k1; k++)
+            if (p->material_isotope_gid[k] < 0 || p->material_isotope_gid[k] >= p->num_isotopes)
+                return fail(QSG_ERR_INVALID, "problem: material %d names isotope out of range", m);
+    }
+    const int64_t C = p->num_cells;
+    for (int64_t c = 0; c < C; c++) {
+        if (p->cell_material[c] < 0 || p->cell_material[c] >= p->num_materials)
+            return fail(QSG_ERR_INVALID, "problem: cell %lld material out of range", (long long)c);
+        for (int k = 0; k < kCellPoints; k++)
+            if (p->cell_points[c * kCellPoints + k] < 0 || p->cell_points[c * kCellPoints + k] >= p->num_nodes)
+                return fail(QSG_ERR_INVALID, "problem: cell %lld point out of range", (long long)c);
+        for (int f = 0; f < kFacets; f++) {
+            int ev = p->facet_event[c * kFacets + f];
+            int ac = p->facet_adjacent_cell[c * kFacets + f];
+            int af = p->facet_adjacent_facet[c * kFacets + f];
+            if (ev < QSG_ADJ_UNDEFINED || ev > QSG_ADJ_TRANSIT_OFF_PROCESSOR)
+                return fail(QSG_ERR_INVALID, "problem: facet event out of range");
+            if (ev == QSG_ADJ_TRANSIT_OFF_PROCESSOR)
+                return fail(QSG_ERR_UNSUPPORTED, "problem: off-processor facets need the multi-domain exchange, "
+                            "which this single-domain library does not implement");
+            if (ac < 0 || ac >= C || af < 0 || af >= kFacets)
+                return fail(QSG_ERR_INVALID, "problem: facet adjacency out of range");
+        }
+    }
+    return QSG_OK;
+}
+
+// Fold the per-cell tables into cross-section classes and upload.
+int upload_tables(QsgHandle* h, const QsgProblem* p)
+{
+    const int G = p->num_groups;
+    const int64_t C = p->num_cells;
+    // class = (material, number density) pair
+    std::map<std::pair<int, uint64_t>, int> class_of;
+    std::vector<int32_t> cell_class(C);
+    std::vector<std::pair<int, double>> classes;
+    for (int64_t c = 0; c < C; c++) {
+        double nd = p->cell_number_density[c];
+        uint64_t bits;
+        memcpy(&bits, &nd, 8);
+        auto key = std::make_pair((int)p->cell_material[c], bits);
+        auto it = class_of.find(key);
+        if (it == class_of.end()) {
+            int id = (int)classes.size();
+            class_of.emplace(key, id);
+            classes.emplace_back(p->cell_material[c], nd);
+            cell_class[c] = id;
+        } else {
+            cell_class[c] = it->second;
+        }
+    }
+    int K = 1;
+    for (auto& cl : classes) {
+        int m = cl.first, nk = 0;
+        for (int k = p->material_isotope_offset[m]; k < p->material_isotope_offset[m + 1]; k++) {
+            int iso = p->material_isotope_gid[k];
+            nk += p->isotope_reaction_offset[iso + 1] - p->isotope_reaction_offset[iso];
+        }
+        K = std::max(K, nk);
+    }
+    const int NCL = (int)classes.size();
+    std::vector<double> sigma_total((size_t)NCL * G), macro((size_t)NCL * G * K, 0.0), nubar((size_t)NCL * K, 0.0);
+    std::vector<int32_t> nreact(NCL), cmat(NCL);
+    std::vector<int8_t> ctype((size_t)NCL * K, 0);
+    for (int ci = 0; ci < NCL; ci++) {
+        int m = classes[ci].first;
+        double nd = classes[ci].second;
+        cmat[ci] = m;
+        int kk = 0;
+        for (int k = p->material_isotope_offset[m]; k < p->material_isotope_offset[m + 1]; k++) {
+            int iso = p->material_isotope_gid[k];
+            for (int r = p->isotope_reaction_offset[iso]; r < p->isotope_reaction_offset[iso + 1]; r++) {
+                ctype[(size_t)ci * K + kk] = (int8_t)p->reaction_type[r];
+                nubar[(size_t)ci * K + kk] = p->reaction_nubar[r];
+                kk++;
+            }
+        }
+        nreact[ci] = kk;
+        for (int g = 0; g < G; g++) {
+            // weightedMacroscopicCrossSection (MacroscopicCrossSection.cc:58-81)
+            double sum = 0.0;
+            kk = 0;
+            for (int k = p->material_isotope_offset[m]; k < p->material_isotope_offset[m + 1]; k++) {
+                int iso = p->material_isotope_gid[k];
+                double af = p->material_atom_fraction[k];
+                double micro_total = 0.0;
+                for (int r = p->isotope_reaction_offset[iso]; r < p->isotope_reaction_offset[iso + 1]; r++)
+                    micro_total += p->reaction_xs[(int64_t)r * G + g];
+                bool zero = (af == 0.0 || nd == 0.0);
+                sum += zero ? 1e-20 : af * nd * micro_total;
+                for (int r = p->isotope_reaction_offset[iso]; r < p->isotope_reaction_offset[iso + 1]; r++) {
+                    macro[((size_t)ci * G + g) * K + kk] = zero ? 1e-20 : af * nd * p->reaction_xs[(int64_t)r * G + g];
+                    kk++;
+                }
+            }
+            sigma_total[(size_t)ci * G + g] = sum;
+        }
+    }
+    // mesh
+    std::vector<double> nodes((size_t)C * kCellPoints * 3), center((size_t)C * 3), planes((size_t)C * kFacets * 4);
+    std::vector<int32_t> adj_cell((size_t)C * kFacets);
+    std::vector<uint8_t> adj_fe((size_t)C * kFacets);
+    for (int64_t c = 0; c < C; c++) {
+        double sx = 0, sy = 0, sz = 0;
+        for (int k = 0; k < kCellPoints; k++) {
+            const double* nd = p->nodes + 3 * (int64_t)p->cell_points[c * kCellPoints + k];
+            nodes[(c * kCellPoints + k) * 3 + 0] = nd[0];
+            nodes[(c * kCellPoints + k) * 3 + 1] = nd[1];
+            nodes[(c * kCellPoints + k) * 3 + 2] = nd[2];
+            sx += nd[0];
+            sy += nd[1];
+            sz += nd[2];
+        }
+        // MCT_Cell_Position_3D_G (MCT.cc:231-253)
+        double one_over = 1.0 / ((double)kCellPoints);
+        center[c * 3 + 0] = sx * one_over;
+        center[c * 3 + 1] = sy * one_over;
+        center[c * 3 + 2] = sz * one_over;
+        for (int f = 0; f < kFacets; f++) {
+            for (int a = 0; a < 4; a++) planes[(c * kFacets + f) * 4 + a] = p->facet_planes[(c * kFacets + f) * 4 + a];
+            adj_cell[c * kFacets + f] = p->facet_adjacent_cell[c * kFacets + f];
+            adj_fe[c * kFacets + f] =
+                (uint8_t)(p->facet_adjacent_facet[c * kFacets + f] | (p->facet_event[c * kFacets + f] << 5));
+        }
+    }
+    std::vector<double> energies(p->energies, p->energies + G + 1);
+    std::vector<double> mass(p->material_mass, p->material_mass + p->num_materials);
+    int st;
+    if ((st = h->energies.upload(energies)) || (st = h->sigma_total.upload(sigma_total)) ||
+        (st = h->macro_xs.upload(macro)) || (st = h->class_nubar.upload(nubar)) ||
+        (st = h->material_mass.upload(mass)) || (st = h->cell_nodes.upload(nodes)) ||
+        (st = h->cell_center.upload(center)) || (st = h->planes.upload(planes)) ||
+        (st = h->class_num_reactions.upload(nreact)) || (st = h->class_material.upload(cmat)) ||
+        (st = h->cell_class.upload(cell_class)) || (st = h->adj_cell.upload(adj_cell)) ||
+        (st = h->class_type.upload(ctype)) || (st = h->adj_facet_event.upload(adj_fe)))
+        return st;
+    DevTables& t = h->tables;
+    t.num_groups = G;
+    t.num_cells = (int32_t)C;
+    t.max_reactions = K;
+    t.energies = h->energies.ptr;
+    t.sigma_total = h->sigma_total.ptr;
+    t.macro_xs = h->macro_xs.ptr;
+    t.class_num_reactions = h->class_num_reactions.ptr;
+    t.class_material = h->class_material.ptr;
+    t.class_reaction_type = h->class_type.ptr;
+    t.class_reaction_nubar = h->class_nubar.ptr;
+    t.material_mass = h->material_mass.ptr;
+    t.cell_class = h->cell_class.ptr;
+    t.cell_nodes = h->cell_nodes.ptr;
+    t.cell_center = h->cell_center.ptr;
+    t.planes = h->planes.ptr;
+    t.adj_cell = h->adj_cell.ptr;
+    t.adj_facet_event = h->adj_facet_event.ptr;
+    for (int f = 0; f < kFacets; f++)
+        for (int k = 0; k < 3; k++) t.facet_local[f][k] = (int8_t)p->facet_local_points[f * 3 + k];
+    t.time_step = p->time_step;
+    return QSG_OK;
+}
+
+int check_soa(const QsgParticleSoA* s)
+{
+    if (!s || !s->x || !s->y || !s->z || !s->vx || !s->vy || !s->vz || !s->kinetic_energy || !s->weight ||
+        !s->time_to_census || !s->age || !s->num_mean_free_paths || !s->num_segments || !s->random_number_seed ||
+        !s->identifier || !s->last_event || !s->num_collisions || !s->breed || !s->species || !s->domain || !s->cell)
+        return fail(QSG_ERR_INVALID, "particle SoA has a null field");
+    return QSG_OK;
+}
+
+int copy_soa(const DevStore& d, const QsgParticleSoA* h, uint64_t n, bool to_device)
+{
+    if (n == 0) return QSG_OK;
+    cudaMemcpyKind kind = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+    double* dd[12] = {d.x, d.y, d.z, d.vx, d.vy, d.vz, d.kinetic_energy, d.weight,
+                      d.time_to_census, d.age, d.num_mean_free_paths, d.num_segments};
+    double* hd[12] = {h->x, h->y, h->z, h->vx, h->vy, h->vz, h->kinetic_energy, h->weight,
+                      h->time_to_census, h->age, h->num_mean_free_paths, h->num_segments};
+    for (int k = 0; k < 12; k++)
+        QSG_CUDA(to_device ? cudaMemcpy(dd[k], hd[k], n * 8, kind) : cudaMemcpy(hd[k], dd[k], n * 8, kind));
+    uint64_t* du[2] = {d.seed, d.identifier};
+    uint64_t* hu[2] = {h->random_number_seed, h->identifier};
+    for (int k = 0; k < 2; k++)
+        QSG_CUDA(to_device ? cudaMemcpy(du[k], hu[k], n * 8, kind) : cudaMemcpy(hu[k], du[k], n * 8, kind));
+    int32_t* di[6] = {d.last_event, d.num_collisions, d.breed, d.species, d.domain, d.cell};
+    int32_t* hi[6] = {h->last_event, h->num_collisions, h->breed, h->species, h->domain, h->cell};
+    for (int k = 0; k < 6; k++)
+        QSG_CUDA(to_device ? cudaMemcpy(di[k], hi[k], n * 4, kind) : cudaMemcpy(hi[k], di[k], n * 4, kind));
+    return QSG_OK;
+}
+
+int launch_track(QsgHandle* h, Store& in, uint64_t n, cudaStream_t s)
+{
+    if (n == 0) return QSG_OK;
+    const int B = kTrackBlock;
+    uint64_t blocks = (n + B - 1) / B;
+    if (blocks > 0x7fffffffULL) return fail(QSG_ERR_CAPACITY, "too many particles for one launch");
+    track_kernel<kTrackBlock><<<(unsigned)blocks, B, 0, s>>>(h->tables, tally_view(h), in.view, n,
+                                                               h->processed.view, h->extra.view);
+    QSG_CUDA(cudaGetLastError());
+    return QSG_OK;
+}
+
+// The tracking passes of one cycle: processing store, then fission products
+// until none are left.  Synchronises on `s` between passes to size the next.
+int track_cycle_impl(QsgHandle* h, cudaStream_t s)
+{
+    int st;
+    uint64_t n = h->n_processing;
+    unsigned long long census_n = 0;
+    QSG_CUDA(cudaMemcpyAsync(&census_n, h->processed.count, sizeof(census_n), cudaMemcpyDeviceToHost, s));
+    QSG_CUDA(cudaStreamSynchronize(s));
+    Store* cur = &h->processing;
+    int pass = 0;
+    while (n > 0) {
+        if ((st = h->processed.reserve(census_n + n))) return st;
+        if ((st = h->extra.reserve(4 * n))) return st;
+        QSG_CUDA(cudaMemsetAsync(h->extra.count, 0, sizeof(unsigned long long), s));
+        if ((st = launch_track(h, *cur, n, s))) return st;
+        unsigned long long counts[2];
+        QSG_CUDA(cudaMemcpyAsync(&counts[0], h->extra.count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        QSG_CUDA(cudaMemcpyAsync(&counts[1], h->processed.count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        QSG_CUDA(cudaStreamSynchronize(s));
+        census_n = counts[1];
+        n = counts[0];
+        // the extra store becomes the next pass's input; the old input is free
+        std::swap(h->processing, h->extra);
+        cur = &h->processing;
+        pass++;
+    }
+    h->n_processing = 0;
+    QSG_CUDA(cudaMemsetAsync(h->processing.count, 0, sizeof(unsigned long long), s));
+    return QSG_OK;
+}
+
+}  // namespace
+}  // namespace qsg
+
+using namespace qsg;
+
+extern "C" int qsg_device_count(int* count)
+{
+    if (!count) return fail(QSG_ERR_INVALID, "qsg_device_count: null argument");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    *count = n;
+    return QSG_OK;
+}
+
+extern "C" int qsg_create(const QsgProblem* problem, const QsgOptions* options, QsgHandle** out)
+{
+    QSG_API_BEGIN
+    if (!problem || !out) return fail(QSG_ERR_INVALID, "qsg_create: null argument");
+    *out = nullptr;
+    int st = validate_problem(problem);
+    if (st) return st;
+    int ndev = 0;
+    qsg_device_count(&ndev);
+    if (ndev == 0) return fail(QSG_ERR_NO_DEVICE, "qsg_create: no CUDA device visible");
+    QsgHandle* h = new QsgHandle();
+    if (options) {
+        h->device = options->device;
+        if (options->flux_replicas > 0) h->flux_replicas = options->flux_replicas;
+        if (options->balance_replicas > 0) h->balance_replicas = options->balance_replicas;
+        if (options->max_segments > 0) h->max_segments = options->max_segments;
+    }
+    h->num_cells = problem->num_cells;
+    h->num_groups = problem->num_groups;
+    auto cleanup = [&](int code) {
+        qsg_destroy(h);
+        return code;
+    };
+    if ((st = set_device(h))) return cleanup(st);
+    if ((st = upload_tables(h, problem))) return cleanup(st);
+    if ((st = h->flux.alloc((size_t)h->flux_replicas * h->num_cells * h->num_groups))) return cleanup(st);
+    if ((st = h->balance.alloc((size_t)h->balance_replicas * QSG_BAL_COUNT))) return cleanup(st);
+    if ((st = h->flags.alloc(1))) return cleanup(st);
+    if (cudaMemset(h->flux.ptr, 0, h->flux.n * sizeof(double)) != cudaSuccess ||
+        cudaMemset(h->balance.ptr, 0, h->balance.n * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(h->flags.ptr, 0, sizeof(unsigned int)) != cudaSuccess)
+        return cleanup(fail(QSG_ERR_CUDA, "qsg_create: memset failed"));
+    uint64_t cap = options && options->particle_capacity ? options->particle_capacity : 1024;
+    if ((st = h->processing.reserve(cap)) || (st = h->processed.reserve(cap)) || (st = h->extra.reserve(cap)))
+        return cleanup(st);
+    *out = h;
+    return QSG_OK;
+    QSG_API_END
+}
+
+extern "C" int qsg_destroy(QsgHandle* h)
+{
+    if (!h) return QSG_OK;
+    cudaSetDevice(h->device);
+    h->energies.free(); h->sigma_total.free(); h->macro_xs.free(); h->class_nubar.free();
+    h->material_mass.free(); h->cell_nodes.free(); h->cell_center.free(); h->planes.free();
+    h->class_num_reactions.free(); h->class_material.free(); h->cell_class.free(); h->adj_cell.free();
+    h->class_type.free(); h->adj_facet_event.free();
+    h->flux.free(); h->balance.free(); h->flags.free();
+    h->processing.release(); h->processed.release(); h->extra.release();
+    delete h;
+    return QSG_OK;
+}
+
+extern "C" int qsg_set_particles(QsgHandle* h, const QsgParticleSoA* host, uint64_t n)
+{
+    QSG_API_BEGIN
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_set_particles: null handle");
+    int st = check_soa(host);
+    if (st && n) return st;
+    if ((st = set_device(h))) return st;
+    if ((st = h->processing.reserve(n))) return st;
+    if ((st = copy_soa(h->processing.view, host, n, true))) return st;
+    unsigned long long nn = n;
+    QSG_CUDA(cudaMemcpy(h->processing.count, &nn, sizeof(nn), cudaMemcpyHostToDevice));
+    QSG_CUDA(cudaMemset(h->processed.count, 0, sizeof(unsigned long long)));
+    h->n_processing = n;
+    return QSG_OK;
+    QSG_API_END
+}
+
+extern "C" int qsg_begin_cycle_from_census(QsgHandle* h, uint64_t* n)
+{
+    QSG_API_BEGIN
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_begin_cycle_from_census: null handle");
+    int st = set_device(h);
+    if (st) return st;
+    unsigned long long c = 0;
+    QSG_CUDA(cudaMemcpy(&c, h->processed.count, sizeof(c), cudaMemcpyDeviceToHost));
+    std::swap(h->processing, h->processed);
+    QSG_CUDA(cudaMemset(h->processed.count, 0, sizeof(unsigned long long)));
+    h->n_processing = c;
+    if (n) *n = c;
+    return QSG_OK;
+    QSG_API_END
+}
+
+extern "C" int qsg_sizes(QsgHandle* h, uint64_t* processing, uint64_t* processed)
+{
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_sizes: null handle");
+    int st = set_device(h);
+    if (st) return st;
+    unsigned long long c = 0;
+    QSG_CUDA(cudaMemcpy(&c, h->processed.count, sizeof(c), cudaMemcpyDeviceToHost));
+    if (processing) *processing = h->n_processing;
+    if (processed) *processed = c;
+    return QSG_OK;
+}
+
+extern "C" int qsg_get_census(QsgHandle* h, QsgParticleSoA* host, uint64_t cap, uint64_t* n_out)
+{
+    QSG_API_BEGIN
+    if (!h || !n_out) return fail(QSG_ERR_INVALID, "qsg_get_census: null argument");
+    int st = set_device(h);
+    if (st) return st;
+    unsigned long long c = 0;
+    QSG_CUDA(cudaMemcpy(&c, h->processed.count, sizeof(c), cudaMemcpyDeviceToHost));
+    *n_out = c;
+    if (c > cap) return fail(QSG_ERR_CAPACITY, "qsg_get_census: %llu particles, capacity %llu", c,
+                             (unsigned long long)cap);
+    if (c == 0) return QSG_OK;
+    if ((st = check_soa(host))) return st;
+    return copy_soa(h->processed.view, host, c, false);
+    QSG_API_END
+}
+
+extern "C" int qsg_track_cycle(QsgHandle* h, void* stream)
+{
+    QSG_API_BEGIN
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_track_cycle: null handle");
+    int st = set_device(h);
+    if (st) return st;
+    return track_cycle_impl(h, static_cast<cudaStream_t>(stream));
+    QSG_API_END
+}
+
+extern "C" int qsg_track_cycle_sync(QsgHandle* h)
+{
+    QSG_API_BEGIN
+    int st = qsg_track_cycle(h, nullptr);
+    if (st) return st;
+    QSG_CUDA(cudaDeviceSynchronize());
+    unsigned int flags = 0;
+    QSG_CUDA(cudaMemcpy(&flags, h->flags.ptr, sizeof(flags), cudaMemcpyDeviceToHost));
+    if (flags) return fail(QSG_ERR_DEVICE, "tracking kernel raised device flags 0x%x", flags);
+    return QSG_OK;
+    QSG_API_END
+}
+
+extern "C" int qsg_read_tallies(QsgHandle* h, uint64_t* balance, double* flux)
+{
+    QSG_API_BEGIN
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_read_tallies: null handle");
+    int st = set_device(h);
+    if (st) return st;
+    QSG_CUDA(cudaDeviceSynchronize());
+    if (balance) {
+        std::vector<unsigned long long> b(h->balance.n);
+        QSG_CUDA(cudaMemcpy(b.data(), h->balance.ptr, b.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        for (int k = 0; k < QSG_BAL_COUNT; k++) {
+            uint64_t s = 0;
+            for (int r = 0; r < h->balance_replicas; r++) s += b[(size_t)r * QSG_BAL_COUNT + k];
+            balance[k] = s;
+        }
+    }
+    if (flux) {
+        const size_t cg_n = (size_t)h->num_cells * h->num_groups;
+        QSG_CUDA(cudaMemcpy(flux, h->flux.ptr, cg_n * sizeof(double), cudaMemcpyDeviceToHost));
+        if (h->flux_replicas > 1) {
+            std::vector<double> tmp(cg_n);
+            for (int r = 1; r < h->flux_replicas; r++) {
+                QSG_CUDA(cudaMemcpy(tmp.data(), h->flux.ptr + r * cg_n, cg_n * sizeof(double), cudaMemcpyDeviceToHost));
+                for (size_t i = 0; i < cg_n; i++) flux[i] += tmp[i];
+            }
+        }
+    }
+    return QSG_OK;
+    QSG_API_END
+}
+
+extern "C" int qsg_reset_tallies(QsgHandle* h)
+{
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_reset_tallies: null handle");
+    int st = set_device(h);
+    if (st) return st;
+    QSG_CUDA(cudaMemset(h->flux.ptr, 0, h->flux.n * sizeof(double)));
+    QSG_CUDA(cudaMemset(h->balance.ptr, 0, h->balance.n * sizeof(unsigned long long)));
+    return QSG_OK;
+}
+
+extern "C" int qsg_device_status(QsgHandle* h, uint32_t* flags, int clear)
+{
+    if (!h || !flags) return fail(QSG_ERR_INVALID, "qsg_device_status: null argument");
+    int st = set_device(h);
+    if (st) return st;
+    unsigned int f = 0;
+    QSG_CUDA(cudaMemcpy(&f, h->flags.ptr, sizeof(f), cudaMemcpyDeviceToHost));
+    *flags = f;
+    if (clear) QSG_CUDA(cudaMemset(h->flags.ptr, 0, sizeof(unsigned int)));
+    return QSG_OK;
+}
+
+static void fill_view(const DevStore& d, QsgParticleSoA* v)
+{
+    v->x = d.x; v->y = d.y; v->z = d.z; v->vx = d.vx; v->vy = d.vy; v->vz = d.vz;
+    v->kinetic_energy = d.kinetic_energy; v->weight = d.weight; v->time_to_census = d.time_to_census;
+    v->age = d.age; v->num_mean_free_paths = d.num_mean_free_paths; v->num_segments = d.num_segments;
+    v->random_number_seed = d.seed; v->identifier = d.identifier; v->last_event = d.last_event;
+    v->num_collisions = d.num_collisions; v->breed = d.breed; v->species = d.species; v->domain = d.domain;
+    v->cell = d.cell;
+}
+
+extern "C" int qsg_processing_view(QsgHandle* h, QsgParticleSoA* v, uint64_t* n)
+{
+    if (!h || !v || !n) return fail(QSG_ERR_INVALID, "qsg_processing_view: null argument");
+    fill_view(h->processing.view, v);
+    *n = h->n_processing;
+    return QSG_OK;
+}
+
+extern "C" int qsg_processed_view(QsgHandle* h, QsgParticleSoA* v, uint64_t* n)
+{
+    if (!h || !v || !n) return fail(QSG_ERR_INVALID, "qsg_processed_view: null argument");
+    int st = set_device(h);
+    if (st) return st;
+    unsigned long long c = 0;
+    QSG_CUDA(cudaMemcpy(&c, h->processed.count, sizeof(c), cudaMemcpyDeviceToHost));
+    fill_view(h->processed.view, v);
+    *n = c;
+    return QSG_OK;
+}

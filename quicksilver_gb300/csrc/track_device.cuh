@@ -1,0 +1,179 @@
+// Device-side history tracking for one spatial domain.
+//
+// Every routine reproduces the reference's floating-point expression order
+// (the library is compiled with --fmad=false, so each * and + rounds on its
+// own exactly as the reference's CPU build does).  Comments name the
+// reference lines each step follows.
+#pragma once
+
+#include <cstdint>
+
+#include "qsg.h"
+
+namespace qsg {
+
+// PhysicalConstants.hh:9-16
+constexpr double kNeutronRestMassEnergy = 9.395656981095e+2;
+constexpr double kPi = 3.1415926535897932;
+constexpr double kSpeedOfLight = 2.99792458e+10;
+constexpr double kTinyDouble = 1.0e-13;
+constexpr double kSmallDouble = 1.0e-10;
+constexpr double kHugeDouble = 1.0e+75;
+
+constexpr int kFacets = 24;
+constexpr int kCellPoints = 14;
+
+// Structure-of-arrays particle store in device memory (136 B per particle,
+// the MC_Base_Particle fields).  `count` lives in device memory so kernels
+// can append with atomics.
+struct DevStore {
+    double *x, *y, *z, *vx, *vy, *vz;
+    double *kinetic_energy, *weight, *time_to_census, *age, *num_mean_free_paths, *num_segments;
+    uint64_t *seed, *identifier;
+    int32_t *last_event, *num_collisions, *breed, *species, *domain, *cell;
+    unsigned long long* count;
+    uint64_t capacity;
+};
+
+// Read-only problem tables in device memory.
+struct DevTables {
+    int32_t num_groups;            // G
+    int32_t num_cells;
+    int32_t max_reactions;         // K: reactions per cross-section class row
+    const double* energies;        // [G+1]
+    const double* sigma_total;     // [classes][G]  weightedMacroscopicCrossSection values
+    const double* macro_xs;        // [classes][G][K] macroscopicCrossSection per (iso, reaction)
+    const int32_t* class_num_reactions;  // [classes]
+    const int32_t* class_material;       // [classes]
+    const int8_t* class_reaction_type;   // [classes][K]
+    const double* class_reaction_nubar;  // [classes][K]
+    const double* material_mass;         // [materials]
+    const int32_t* cell_class;     // [C]
+    const double* cell_nodes;      // [C][14][3]
+    const double* cell_center;     // [C][3] MCT_Cell_Position_3D_G
+    const double* planes;          // [C][24][4]
+    const int32_t* adj_cell;       // [C][24]
+    const uint8_t* adj_facet_event;// [C][24] facet | (event << 5)
+    int8_t facet_local[kFacets][3];
+    double time_step;
+};
+
+struct DevTally {
+    double* flux;                  // [replicas][C][G]
+    unsigned long long* balance;   // [replicas][QSG_BAL_COUNT]
+    unsigned int* error_flags;
+    int32_t flux_replicas;
+    int32_t balance_replicas;
+    uint64_t max_segments;
+};
+
+// MC_RNG_State.hh:22-33
+__device__ __forceinline__ double rng_sample(uint64_t& seed)
+{
+    seed = 2862933555777941757ULL * seed + 3037000493ULL;
+    return 5.4210108624275222e-20 * __ull2double_rn(seed);
+}
+
+// Numerical Recipes psdes (2 rounds) as MC_RNG_State.cc:29-52, used by
+// rngSpawn_Random_Number_Seed (MC_RNG_State.cc:106-113).
+__device__ __forceinline__ uint64_t rng_spawn(uint64_t& parent)
+{
+    const uint32_t c1[2] = {0xbaa96887u, 0x1e17d32cu};
+    const uint32_t c2[2] = {0x4b0f3b58u, 0xe874f0c3u};
+    uint32_t lword = (uint32_t)(parent >> 32);
+    uint32_t irword = (uint32_t)(parent & 0xffffffffu);
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        uint32_t iswap = irword;
+        uint32_t ia = iswap ^ c1[i];
+        uint32_t lo = ia & 0xffffu;
+        uint32_t hi = ia >> 16;
+        uint32_t ib = lo * lo + ~(hi * hi);
+        ia = (ib >> 16) | ((ib & 0xffffu) << 16);
+        irword = lword ^ ((ia ^ c2[i]) + lo * hi);
+        lword = iswap;
+    }
+    uint64_t spawned = ((uint64_t)lword << 32) | (uint64_t)irword;
+    rng_sample(parent);
+    return spawned;
+}
+
+// NuclearData::getEnergyGroup, NuclearData.cc:207-228
+__device__ __forceinline__ int energy_group(const DevTables& t, double e)
+{
+    const int n = t.num_groups + 1;
+    const double* en = t.energies;
+    if (e <= __ldg(en)) return 0;
+    if (e > __ldg(en + n - 1)) return n - 1;
+    int high = n - 1, low = 0;
+    while (high != low + 1) {
+        int mid = (high + low) / 2;
+        if (e < __ldg(en + mid)) high = mid;
+        else low = mid;
+    }
+    return low;
+}
+
+struct Particle {
+    double x, y, z, vx, vy, vz;
+    double alpha, beta, gamma;
+    double kinetic_energy, weight, time_to_census, age;
+    double num_mean_free_paths, num_segments, total_xs, mean_free_path;
+    uint64_t seed, identifier;
+    int32_t last_event, num_collisions, breed, species, domain, cell, facet, group;
+};
+
+__device__ __forceinline__ void load_particle(const DevTables& t, const DevStore& s, uint64_t i, Particle& p)
+{
+    p.x = s.x[i]; p.y = s.y[i]; p.z = s.z[i];
+    p.vx = s.vx[i]; p.vy = s.vy[i]; p.vz = s.vz[i];
+    p.kinetic_energy = s.kinetic_energy[i];
+    p.weight = s.weight[i];
+    p.time_to_census = s.time_to_census[i];
+    p.age = s.age[i];
+    p.num_mean_free_paths = s.num_mean_free_paths[i];
+    p.num_segments = s.num_segments[i];
+    p.seed = s.seed[i];
+    p.identifier = s.identifier[i];
+    p.last_event = s.last_event[i];
+    p.num_collisions = s.num_collisions[i];
+    p.breed = s.breed[i];
+    p.species = s.species[i];
+    p.domain = s.domain[i];
+    p.cell = s.cell[i];
+    p.facet = 0;
+    p.total_xs = 0.0;
+    p.mean_free_path = 0.0;
+    // direction from velocity (MC_Base_Particle.hh:317-325)
+    double speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
+    double factor = 1.0 / speed;
+    p.alpha = factor * p.vx;
+    p.beta = factor * p.vy;
+    p.gamma = factor * p.vz;
+    // MC_Load_Particle.cc:18-26
+    if (p.time_to_census <= 0.0) p.time_to_census += t.time_step;
+    if (p.age < 0.0) p.age = 0.0;
+    p.group = energy_group(t, p.kinetic_energy);
+}
+
+__device__ __forceinline__ void store_particle(const DevStore& s, uint64_t i, const Particle& p)
+{
+    s.x[i] = p.x; s.y[i] = p.y; s.z[i] = p.z;
+    s.vx[i] = p.vx; s.vy[i] = p.vy; s.vz[i] = p.vz;
+    s.kinetic_energy[i] = p.kinetic_energy;
+    s.weight[i] = p.weight;
+    s.time_to_census[i] = p.time_to_census;
+    s.age[i] = p.age;
+    s.num_mean_free_paths[i] = p.num_mean_free_paths;
+    s.num_segments[i] = p.num_segments;
+    s.seed[i] = p.seed;
+    s.identifier[i] = p.identifier;
+    s.last_event[i] = p.last_event;
+    s.num_collisions[i] = p.num_collisions;
+    s.breed[i] = p.breed;
+    s.species[i] = p.species;
+    s.domain[i] = p.domain;
+    s.cell[i] = p.cell;
+}
+
+}  // namespace qsg
