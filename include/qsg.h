@@ -52,7 +52,8 @@ enum {
     QSG_DEV_OFF_PROCESSOR = 1u << 3,    /* Transit_Off_Processor facet hit    */
     QSG_DEV_STORE_OVERFLOW = 1u << 4,   /* census / extra store overflow      */
     QSG_DEV_BAD_FACET = 1u << 5,        /* no facet bounds the particle       */
-    QSG_DEV_NEGATIVE_DISTANCE = 1u << 6 /* MC_Segment_Outcome.cc:265-276      */
+    QSG_DEV_NEGATIVE_DISTANCE = 1u << 6,/* MC_Segment_Outcome.cc:265-276      */
+    QSG_DEV_PASS_LIMIT = 1u << 7        /* fission products left after max_passes */
 };
 
 /* ---- enums shared with the reference ------------------------------------ */
@@ -146,6 +147,8 @@ typedef struct QsgOptions {
     int32_t balance_replicas;    /* privatised counter copies (0 = 1)          */
     uint64_t particle_capacity;  /* per store (0 = grow on demand)             */
     uint64_t max_segments;       /* per history per launch guard (0 = 2^40)    */
+    int32_t max_passes;          /* fission passes per asynchronous cycle (0 = 8) */
+    int32_t reserved;
 } QsgOptions;
 
 typedef struct QsgHandle QsgHandle;
@@ -181,11 +184,18 @@ int qsg_get_census(QsgHandle* h, QsgParticleSoA* host, uint64_t cap, uint64_t* n
  * or fission; fission products (ParticleVaultContainer::addExtraParticle) are
  * tracked in follow-up passes inside the same call, as cycleTracking's
  * while(!done) loop does (main.cc:155-299).  Census particles are appended to
- * the processed store.  Asynchronous on `stream` (a cudaStream_t or NULL). */
+ * the processed store.  Work is enqueued on `stream` (a cudaStream_t or NULL);
+ * the call waits on that stream once per pass to read the remaining count and
+ * grow the stores, so it returns when the last pass has been enqueued. */
 int qsg_track_cycle(QsgHandle* h, void* stream);
 /* Like qsg_track_cycle, but synchronous and reporting the device error flag
  * as QSG_ERR_DEVICE. */
 int qsg_track_cycle_sync(QsgHandle* h);
+/* Exactly QsgOptions::max_passes passes with no host synchronisation (CUDA
+ * graph capturable); the stores must already be large enough
+ * (qsg_configure_cycle sizes them).  Fission products still left afterwards
+ * raise QSG_DEV_PASS_LIMIT, overflow raises QSG_DEV_STORE_OVERFLOW. */
+int qsg_track_cycle_async(QsgHandle* h, void* stream);
 
 /* Balance counters summed over replicas (13 x u64, QSG_BAL_* order) and the
  * scalar flux [num_cells*G] summed over replicas (Tallies.cc:16-23,75-96). */
@@ -194,6 +204,36 @@ int qsg_read_tallies(QsgHandle* h, uint64_t* balance, double* flux);
 int qsg_reset_tallies(QsgHandle* h);
 /* Device error flag bits (QSG_DEV_*) raised since the last reset, and clear. */
 int qsg_device_status(QsgHandle* h, uint32_t* flags, int clear);
+
+/* ---- whole cycle on the device ------------------------------------------ */
+/* Constants of the cycle set-up (SimulationParameters / MaterialParameters,
+ * Parameters.hh:45-167). */
+typedef struct QsgCycleConfig {
+    const double* source_rate;   /* [num_materials] MaterialParameters::sourceRate     */
+    uint64_t n_particles;        /* population target, SimulationParameters::nParticles */
+    double e_min, e_max;         /* source energy range (MeV)                           */
+    double low_weight_cutoff;    /* SimulationParameters::lowWeightCutoff               */
+    int32_t load_balance;        /* SimulationParameters::loadBalance                   */
+    int32_t reserved;
+    uint64_t store_capacity;     /* particles per store (0 = 4 x (n_particles + source)) */
+} QsgCycleConfig;
+/* Precompute the source (MC_SourceNow.cc:35-64: particle weight and per-cell
+ * counts are constant over the run) and size the particle stores.  Needs the
+ * problem's cell_volume and cell_id. */
+int qsg_configure_cycle(QsgHandle* h, const QsgCycleConfig* config);
+/* cycleInit (main.cc:96-121) on the device, asynchronous on `stream`: the
+ * previous census becomes the processing store, then MC_SourceNow,
+ * PopulationControl and RouletteLowWeightParticles. */
+int qsg_cycle_init(QsgHandle* h, void* stream);
+/* cycleFinalize (main.cc:310-324), asynchronous: the cycle's 13 counters
+ * (END = census count) and scalar-flux total are appended to a device-resident
+ * history, then counters and flux are zeroed (Tallies.cc:25-98). */
+int qsg_cycle_finalize(QsgHandle* h, void* stream);
+/* Copy history rows [first, first+n): balance [n*13] and flux totals [n]
+ * (either may be NULL).  Synchronous. */
+int qsg_cycle_history(QsgHandle* h, uint64_t first, uint64_t n, uint64_t* balance, double* flux_total);
+/* Copy the processing store (e.g. after qsg_cycle_init) to host arrays. */
+int qsg_get_processing(QsgHandle* h, QsgParticleSoA* host, uint64_t cap, uint64_t* n_out);
 
 /* Device pointers of the stores, for zero-copy callers (e.g. torch). */
 int qsg_processing_view(QsgHandle* h, QsgParticleSoA* device_view, uint64_t* n);

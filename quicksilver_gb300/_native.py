@@ -67,7 +67,7 @@ class QsgParticleSoA(C.Structure):
 class QsgOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("block_size", C.c_int32), ("flux_replicas", C.c_int32),
                 ("balance_replicas", C.c_int32), ("particle_capacity", C.c_uint64),
-                ("max_segments", C.c_uint64)]
+                ("max_segments", C.c_uint64), ("max_passes", C.c_int32), ("reserved", C.c_int32)]
 
 
 class QsgSimulation(C.Structure):
@@ -77,6 +77,12 @@ class QsgSimulation(C.Structure):
                                          "n_groups", "load_balance", "balance_replications",
                                          "flux_replications", "cell_replications", "coral_benchmark",
                                          "boundary_condition")]
+
+
+class QsgCycleConfig(C.Structure):
+    _fields_ = [("source_rate", _dp), ("n_particles", C.c_uint64), ("e_min", C.c_double), ("e_max", C.c_double),
+                ("low_weight_cutoff", C.c_double), ("load_balance", C.c_int32), ("reserved", C.c_int32),
+                ("store_capacity", C.c_uint64)]
 
 
 class QsgError(RuntimeError):
@@ -100,9 +106,15 @@ _SIGNATURES = {
     "qsg_get_census": ([_VP, C.POINTER(QsgParticleSoA), C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
     "qsg_track_cycle": ([_VP, _VP], C.c_int),
     "qsg_track_cycle_sync": ([_VP], C.c_int),
+    "qsg_track_cycle_async": ([_VP, _VP], C.c_int),
     "qsg_read_tallies": ([_VP, _up, _dp], C.c_int),
     "qsg_reset_tallies": ([_VP], C.c_int),
     "qsg_device_status": ([_VP, C.POINTER(C.c_uint32), C.c_int], C.c_int),
+    "qsg_configure_cycle": ([_VP, C.POINTER(QsgCycleConfig)], C.c_int),
+    "qsg_cycle_init": ([_VP, _VP], C.c_int),
+    "qsg_cycle_finalize": ([_VP, _VP], C.c_int),
+    "qsg_cycle_history": ([_VP, C.c_uint64, C.c_uint64, _up, _dp], C.c_int),
+    "qsg_get_processing": ([_VP, C.POINTER(QsgParticleSoA), C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
     "qsg_processing_view": ([_VP, C.POINTER(QsgParticleSoA), C.POINTER(C.c_uint64)], C.c_int),
     "qsg_processed_view": ([_VP, C.POINTER(QsgParticleSoA), C.POINTER(C.c_uint64)], C.c_int),
     "qsg_deck_parse_file": ([C.c_char_p, C.POINTER(_VP)], C.c_int),

@@ -37,21 +37,6 @@ namespace qsg {
 
 enum LocalCounter { LC_SEG = 0, LC_COLL, LC_SCAT, LC_ABS, LC_FIS, LC_PROD, LC_ESC, LC_CEN, LC_N };
 
-__device__ __forceinline__ void raise_flag(const DevTally& tally, unsigned int bit)
-{
-    atomicOr(tally.error_flags, bit);
-}
-
-// Reserve one slot of `s` for each calling lane with one atomic per warp.
-__device__ __forceinline__ uint64_t append_slot(const DevStore& s)
-{
-    cg::coalesced_group g = cg::coalesced_threads();
-    unsigned long long base = 0;
-    if (g.thread_rank() == 0) base = atomicAdd(s.count, (unsigned long long)g.size());
-    base = g.shfl(base, 0);
-    return base + g.thread_rank();
-}
-
 // MCT_Nearest_Facet_3D_G_Distance_To_Segment, MCT.cc:280-395.
 __device__ __forceinline__ double distance_to_segment(double plane_tolerance, double dot, double A, double B, double C,
                                                       double D, const double* p0, const double* p1,
@@ -372,25 +357,45 @@ __device__ __forceinline__ void flush_counters(const DevTally& tally, uint32_t* 
     }
 }
 
-// One thread per particle of `in`: CycleTrackingGuts + CycleTrackingFunction
-// (CycleTracking.cc:14-120).
+// Persistent tracking pass over the store `in` (its count is read on the
+// device): CycleTrackingGuts + CycleTrackingFunction (CycleTracking.cc:14-120)
+// one segment per loop trip.  A lane whose history ends pulls the next
+// particle index from the work cursor at once (warp-aggregated atomic), so
+// long histories do not hold idle lanes; the warp leaves when every lane has
+// finished and the queue is empty.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) track_kernel(DevTables t, DevTally tally, DevStore in, uint64_t n,
-                                                      DevStore census, DevStore extra)
+__global__ void __launch_bounds__(BLOCK) track_kernel(DevTables t, DevTally tally, DevStore in, DevStore census,
+                                                      DevStore extra, unsigned long long* cursor)
 {
     uint32_t cnt[LC_N];
 #pragma unroll
     for (int k = 0; k < LC_N; k++) cnt[k] = 0;
-    const uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
-    if (i < n) {
-        Particle p;
-        load_particle(t, in, i, p);
-        if (!(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz > 0.0)) raise_flag(tally, QSG_DEV_BAD_FACET);
-        // CycleTracking.cc:37-39 replica selection by particle index
-        double* flux_row = tally.flux + (int64_t)(i % (uint64_t)tally.flux_replicas) * t.num_cells * t.num_groups;
-        uint64_t segs_this_launch = 0;
-        bool keep;
-        do {
+    const uint64_t n = *in.count;
+    Particle p;
+    bool active = false, exhausted = false;
+    double* flux_row = tally.flux;
+    uint64_t segs_this_history = 0;
+    for (;;) {
+        if (!active && !exhausted) {
+            cg::coalesced_group g = cg::coalesced_threads();
+            unsigned long long base = 0;
+            if (g.thread_rank() == 0) base = atomicAdd(cursor, (unsigned long long)g.size());
+            base = g.shfl(base, 0);
+            const uint64_t i = base + g.thread_rank();
+            if (i < n) {
+                load_particle(t, in, i, p);
+                if (!(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz > 0.0)) raise_flag(tally, QSG_DEV_BAD_FACET);
+                // CycleTracking.cc:37-39 replica selection by particle index
+                flux_row = tally.flux + (int64_t)(i % (uint64_t)tally.flux_replicas) * t.num_cells * t.num_groups;
+                segs_this_history = 0;
+                active = true;
+            } else {
+                exhausted = true;
+            }
+        }
+        if (__all_sync(0xffffffffu, !active)) break;
+        if (active) {
+            bool keep;
             const int cls = __ldg(t.cell_class + p.cell);
             int outcome = segment_outcome(t, tally, p, cls, flux_row);
             cnt[LC_SEG]++;
@@ -428,183 +433,24 @@ __global__ void __launch_bounds__(BLOCK) track_kernel(DevTables t, DevTally tall
                 cnt[LC_CEN]++;
                 keep = false;
             }
-            if (keep && ++segs_this_launch >= tally.max_segments) {
+            if (keep && ++segs_this_history >= tally.max_segments) {
                 raise_flag(tally, QSG_DEV_SEGMENT_LIMIT);
                 keep = false;
             }
-        } while (keep);
+            active = keep;
+        }
     }
     flush_counters<BLOCK>(tally, cnt, (int)(blockIdx.x % (unsigned)tally.balance_replicas));
 }
 
-constexpr int kTrackBlock = 128;
-
 // ------------------------------------------------------------------------
 // Host side.
 
-#define QSG_CUDA(call)                                                                      \
-    do {                                                                                    \
-        cudaError_t err__ = (call);                                                         \
-        if (err__ != cudaSuccess)                                                           \
-            return ::qsg::fail(QSG_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(err__)); \
-    } while (0)
-
-template <typename T>
-struct DevBuf {
-    T* ptr = nullptr;
-    size_t n = 0;
-    int alloc(size_t count)
-    {
-        free();
-        if (count == 0) count = 1;
-        cudaError_t e = cudaMalloc(&ptr, count * sizeof(T));
-        if (e != cudaSuccess) {
-            ptr = nullptr;
-            return fail(QSG_ERR_CUDA, "cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(e));
-        }
-        n = count;
-        return QSG_OK;
-    }
-    int upload(const std::vector<T>& v)
-    {
-        int st = alloc(v.size());
-        if (st) return st;
-        if (!v.empty()) QSG_CUDA(cudaMemcpy(ptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
-        return QSG_OK;
-    }
-    void free()
-    {
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        n = 0;
-    }
-};
-
-// One particle store: 20 field arrays carved out of one allocation.
-struct Store {
-    void* base = nullptr;
-    unsigned long long* count = nullptr;  // device counter
-    uint64_t capacity = 0;
-    DevStore view{};
-
-    int reserve(uint64_t cap)
-    {
-        if (cap <= capacity && base) return QSG_OK;
-        uint64_t nc = capacity ? capacity : 1024;
-        while (nc < cap) nc *= 2;
-        size_t bytes = nc * 136 + 256 * 21;
-        void* nb = nullptr;
-        cudaError_t e = cudaMalloc(&nb, bytes);
-        if (e != cudaSuccess) return fail(QSG_ERR_CUDA, "cudaMalloc store (%zu bytes): %s", bytes, cudaGetErrorString(e));
-        DevStore nv = carve(nb, nc);
-        if (base) {
-            unsigned long long n_old = 0;
-            e = cudaMemcpy(&n_old, count, sizeof(n_old), cudaMemcpyDeviceToHost);
-            if (e == cudaSuccess && n_old) e = copy_fields(nv, view, 0, 0, std::min<uint64_t>(n_old, capacity));
-            if (e == cudaSuccess) e = cudaMemcpy(nv.count, &n_old, sizeof(n_old), cudaMemcpyHostToDevice);
-            if (e != cudaSuccess) {
-                cudaFree(nb);
-                return fail(QSG_ERR_CUDA, "store grow: %s", cudaGetErrorString(e));
-            }
-            cudaFree(base);
-        } else {
-            e = cudaMemset(nv.count, 0, sizeof(unsigned long long));
-            if (e != cudaSuccess) {
-                cudaFree(nb);
-                return fail(QSG_ERR_CUDA, "store init: %s", cudaGetErrorString(e));
-            }
-        }
-        base = nb;
-        view = nv;
-        count = nv.count;
-        capacity = nc;
-        return QSG_OK;
-    }
-
-    static DevStore carve(void* b, uint64_t cap)
-    {
-        DevStore v{};
-        char* p = static_cast<char*>(b);
-        auto take = [&](size_t esz) {
-            char* r = p;
-            p += (cap * esz + 255) & ~size_t(255);
-            return r;
-        };
-        v.count = reinterpret_cast<unsigned long long*>(p);
-        p += 256;
-        double** dfields[12] = {&v.x, &v.y, &v.z, &v.vx, &v.vy, &v.vz, &v.kinetic_energy, &v.weight,
-                                &v.time_to_census, &v.age, &v.num_mean_free_paths, &v.num_segments};
-        for (double** f : dfields) *f = reinterpret_cast<double*>(take(8));
-        v.seed = reinterpret_cast<uint64_t*>(take(8));
-        v.identifier = reinterpret_cast<uint64_t*>(take(8));
-        int32_t** ifields[6] = {&v.last_event, &v.num_collisions, &v.breed, &v.species, &v.domain, &v.cell};
-        for (int32_t** f : ifields) *f = reinterpret_cast<int32_t*>(take(4));
-        v.capacity = cap;
-        return v;
-    }
-
-    static cudaError_t copy_fields(const DevStore& dst, const DevStore& src, uint64_t dst_off, uint64_t src_off,
-                                   uint64_t n, cudaStream_t s = 0)
-    {
-        if (n == 0) return cudaSuccess;
-        double* dd[12] = {dst.x, dst.y, dst.z, dst.vx, dst.vy, dst.vz, dst.kinetic_energy, dst.weight,
-                          dst.time_to_census, dst.age, dst.num_mean_free_paths, dst.num_segments};
-        double* sd[12] = {src.x, src.y, src.z, src.vx, src.vy, src.vz, src.kinetic_energy, src.weight,
-                          src.time_to_census, src.age, src.num_mean_free_paths, src.num_segments};
-        for (int k = 0; k < 12; k++) {
-            cudaError_t e = cudaMemcpyAsync(dd[k] + dst_off, sd[k] + src_off, n * 8, cudaMemcpyDeviceToDevice, s);
-            if (e != cudaSuccess) return e;
-        }
-        uint64_t* du[2] = {dst.seed, dst.identifier};
-        uint64_t* su[2] = {src.seed, src.identifier};
-        for (int k = 0; k < 2; k++) {
-            cudaError_t e = cudaMemcpyAsync(du[k] + dst_off, su[k] + src_off, n * 8, cudaMemcpyDeviceToDevice, s);
-            if (e != cudaSuccess) return e;
-        }
-        int32_t* di[6] = {dst.last_event, dst.num_collisions, dst.breed, dst.species, dst.domain, dst.cell};
-        int32_t* si[6] = {src.last_event, src.num_collisions, src.breed, src.species, src.domain, src.cell};
-        for (int k = 0; k < 6; k++) {
-            cudaError_t e = cudaMemcpyAsync(di[k] + dst_off, si[k] + src_off, n * 4, cudaMemcpyDeviceToDevice, s);
-            if (e != cudaSuccess) return e;
-        }
-        return cudaSuccess;
-    }
-
-    void release()
-    {
-        if (base) cudaFree(base);
-        base = nullptr;
-        count = nullptr;
-        capacity = 0;
-        view = DevStore{};
-    }
-};
-
 }  // namespace qsg
 
-struct QsgHandle {
-    int device = 0;
-    int block_size = qsg::kTrackBlock;
-    int32_t flux_replicas = 1, balance_replicas = 1;
-    uint64_t max_segments = (uint64_t)1 << 40;
-    int32_t num_cells = 0, num_groups = 0;
-    // tables
-    qsg::DevBuf<double> energies, sigma_total, macro_xs, class_nubar, material_mass, cell_nodes, cell_center, planes;
-    qsg::DevBuf<int32_t> class_num_reactions, class_material, cell_class, adj_cell;
-    qsg::DevBuf<int8_t> class_type;
-    qsg::DevBuf<uint8_t> adj_facet_event;
-    qsg::DevTables tables{};
-    // tallies
-    qsg::DevBuf<double> flux;
-    qsg::DevBuf<unsigned long long> balance;
-    qsg::DevBuf<unsigned int> flags;
-    // particle stores: processing, processed (census), extra (fission products)
-    qsg::Store processing, processed, extra;
-    uint64_t n_processing = 0;   // host mirror of processing count
-};
+#include "handle.cuh"
 
 namespace qsg {
-namespace {
 
 int set_device(const QsgHandle* h) {
     QSG_CUDA(cudaSetDevice(h->device));
@@ -622,6 +468,8 @@ DevTally tally_view(QsgHandle* h)
     t.max_segments = h->max_segments;
     return t;
 }
+
+namespace {
 
 int validate_problem(const QsgProblem* p)
 {
@@ -813,6 +661,8 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
     return QSG_OK;
 }
 
+}  // namespace
+
 int check_soa(const QsgParticleSoA* s)
 {
     if (!s || !s->x || !s->y || !s->z || !s->vx || !s->vy || !s->vz || !s->kinetic_energy || !s->weight ||
@@ -843,51 +693,66 @@ int copy_soa(const DevStore& d, const QsgParticleSoA* h, uint64_t n, bool to_dev
     return QSG_OK;
 }
 
-int launch_track(QsgHandle* h, Store& in, uint64_t n, cudaStream_t s)
+namespace {
+
+// One tracking pass: processing store -> census + fission products (extra).
+// The pass's particle count is read by the kernel from the store's device
+// counter, so nothing here waits for the device.
+int launch_pass(QsgHandle* h, cudaStream_t s)
 {
-    if (n == 0) return QSG_OK;
-    const int B = kTrackBlock;
-    uint64_t blocks = (n + B - 1) / B;
-    if (blocks > 0x7fffffffULL) return fail(QSG_ERR_CAPACITY, "too many particles for one launch");
-    track_kernel<kTrackBlock><<<(unsigned)blocks, B, 0, s>>>(h->tables, tally_view(h), in.view, n,
-                                                               h->processed.view, h->extra.view);
+    unsigned long long* cursor = &h->scalars.ptr->cursor;
+    QSG_CUDA(cudaMemsetAsync(h->extra.count, 0, sizeof(unsigned long long), s));
+    QSG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s));
+    track_kernel<kTrackBlock><<<h->track_blocks, kTrackBlock, 0, s>>>(h->tables, tally_view(h), h->processing.view,
+                                                                       h->processed.view, h->extra.view, cursor);
     QSG_CUDA(cudaGetLastError());
+    // the extra store becomes the next pass's input; the old input is free
+    std::swap(h->processing, h->extra);
     return QSG_OK;
 }
 
-// The tracking passes of one cycle: processing store, then fission products
-// until none are left.  Synchronises on `s` between passes to size the next.
-int track_cycle_impl(QsgHandle* h, cudaStream_t s)
+__global__ void leftover_check_kernel(const unsigned long long* count, unsigned int* flags)
 {
-    int st;
-    uint64_t n = h->n_processing;
-    unsigned long long census_n = 0;
-    QSG_CUDA(cudaMemcpyAsync(&census_n, h->processed.count, sizeof(census_n), cudaMemcpyDeviceToHost, s));
-    QSG_CUDA(cudaStreamSynchronize(s));
-    Store* cur = &h->processing;
-    int pass = 0;
-    while (n > 0) {
-        if ((st = h->processed.reserve(census_n + n))) return st;
-        if ((st = h->extra.reserve(4 * n))) return st;
-        QSG_CUDA(cudaMemsetAsync(h->extra.count, 0, sizeof(unsigned long long), s));
-        if ((st = launch_track(h, *cur, n, s))) return st;
-        unsigned long long counts[2];
-        QSG_CUDA(cudaMemcpyAsync(&counts[0], h->extra.count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-        QSG_CUDA(cudaMemcpyAsync(&counts[1], h->processed.count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-        QSG_CUDA(cudaStreamSynchronize(s));
-        census_n = counts[1];
-        n = counts[0];
-        // the extra store becomes the next pass's input; the old input is free
-        std::swap(h->processing, h->extra);
-        cur = &h->processing;
-        pass++;
-    }
-    h->n_processing = 0;
-    QSG_CUDA(cudaMemsetAsync(h->processing.count, 0, sizeof(unsigned long long), s));
-    return QSG_OK;
+    if (*count != 0) atomicOr(flags, QSG_DEV_PASS_LIMIT);
 }
 
 }  // namespace
+
+// Asynchronous cycle: a fixed number of passes, no host synchronisation.
+// Stores must already hold enough capacity (qsg_configure_cycle sizes them);
+// overflow and leftover fission products raise device flags.
+int track_passes_async(QsgHandle* h, cudaStream_t s)
+{
+    int st;
+    for (int pass = 0; pass < h->max_passes; pass++)
+        if ((st = launch_pass(h, s))) return st;
+    leftover_check_kernel<<<1, 1, 0, s>>>(h->processing.count, h->flags.ptr);
+    QSG_CUDA(cudaGetLastError());
+    h->n_processing = 0;
+    return QSG_OK;
+}
+
+// Synchronous cycle: passes until no fission products are left, growing the
+// stores between passes from the counts read back after each pass.
+int track_passes_sync(QsgHandle* h, cudaStream_t s)
+{
+    int st;
+    unsigned long long counts[2];
+    for (;;) {
+        QSG_CUDA(cudaMemcpyAsync(&counts[0], h->processing.count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        QSG_CUDA(cudaMemcpyAsync(&counts[1], h->processed.count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        QSG_CUDA(cudaStreamSynchronize(s));
+        const uint64_t n = counts[0];
+        if (n == 0) break;
+        if ((st = h->processed.reserve(counts[1] + n))) return st;
+        if ((st = h->extra.reserve(4 * n))) return st;
+        if ((st = launch_pass(h, s))) return st;
+    }
+    h->n_processing = 0;
+    h->known_census = counts[1];
+    return QSG_OK;
+}
+
 }  // namespace qsg
 
 using namespace qsg;
@@ -921,6 +786,7 @@ extern "C" int qsg_create(const QsgProblem* problem, const QsgOptions* options, 
         if (options->flux_replicas > 0) h->flux_replicas = options->flux_replicas;
         if (options->balance_replicas > 0) h->balance_replicas = options->balance_replicas;
         if (options->max_segments > 0) h->max_segments = options->max_segments;
+        if (options->max_passes > 0) h->max_passes = options->max_passes;
     }
     h->num_cells = problem->num_cells;
     h->num_groups = problem->num_groups;
@@ -930,6 +796,21 @@ extern "C" int qsg_create(const QsgProblem* problem, const QsgOptions* options, 
     };
     if ((st = set_device(h))) return cleanup(st);
     if ((st = upload_tables(h, problem))) return cleanup(st);
+    {
+        cudaDeviceProp prop;
+        QSG_CUDA(cudaGetDeviceProperties(&prop, h->device));
+        h->num_sms = prop.multiProcessorCount;
+        int per_sm = 0;
+        QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel<kTrackBlock>, kTrackBlock, 0));
+        h->track_blocks = h->num_sms * (per_sm > 0 ? per_sm : 1);
+    }
+    h->num_materials = problem->num_materials;
+    if (problem->cell_volume) h->h_cell_volume.assign(problem->cell_volume, problem->cell_volume + problem->num_cells);
+    if (problem->cell_id) h->h_cell_id.assign(problem->cell_id, problem->cell_id + problem->num_cells);
+    h->h_cell_material.assign(problem->cell_material, problem->cell_material + problem->num_cells);
+    if ((st = h->scalars.alloc(1))) return cleanup(st);
+    if (cudaMemset(h->scalars.ptr, 0, sizeof(CycleScalars)) != cudaSuccess)
+        return cleanup(fail(QSG_ERR_CUDA, "qsg_create: memset failed"));
     if ((st = h->flux.alloc((size_t)h->flux_replicas * h->num_cells * h->num_groups))) return cleanup(st);
     if ((st = h->balance.alloc((size_t)h->balance_replicas * QSG_BAL_COUNT))) return cleanup(st);
     if ((st = h->flags.alloc(1))) return cleanup(st);
@@ -953,7 +834,9 @@ extern "C" int qsg_destroy(QsgHandle* h)
     h->material_mass.free(); h->cell_nodes.free(); h->cell_center.free(); h->planes.free();
     h->class_num_reactions.free(); h->class_material.free(); h->cell_class.free(); h->adj_cell.free();
     h->class_type.free(); h->adj_facet_event.free();
-    h->flux.free(); h->balance.free(); h->flags.free();
+    h->flux.free(); h->balance.free(); h->flags.free(); h->flux_partial.free();
+    h->cell_volume.free(); h->cell_id.free(); h->src_cell.free(); h->src_cell_count.free();
+    h->src_cell_offset.free(); h->scalars.free(); h->history.free();
     h->processing.release(); h->processed.release(); h->extra.release();
     delete h;
     return QSG_OK;
@@ -997,9 +880,11 @@ extern "C" int qsg_sizes(QsgHandle* h, uint64_t* processing, uint64_t* processed
     if (!h) return fail(QSG_ERR_INVALID, "qsg_sizes: null handle");
     int st = set_device(h);
     if (st) return st;
-    unsigned long long c = 0;
+    QSG_CUDA(cudaDeviceSynchronize());
+    unsigned long long c = 0, p = 0;
     QSG_CUDA(cudaMemcpy(&c, h->processed.count, sizeof(c), cudaMemcpyDeviceToHost));
-    if (processing) *processing = h->n_processing;
+    QSG_CUDA(cudaMemcpy(&p, h->processing.count, sizeof(p), cudaMemcpyDeviceToHost));
+    if (processing) *processing = p;
     if (processed) *processed = c;
     return QSG_OK;
 }
@@ -1027,15 +912,27 @@ extern "C" int qsg_track_cycle(QsgHandle* h, void* stream)
     if (!h) return fail(QSG_ERR_INVALID, "qsg_track_cycle: null handle");
     int st = set_device(h);
     if (st) return st;
-    return track_cycle_impl(h, static_cast<cudaStream_t>(stream));
+    return track_passes_sync(h, static_cast<cudaStream_t>(stream));
+    QSG_API_END
+}
+
+extern "C" int qsg_track_cycle_async(QsgHandle* h, void* stream)
+{
+    QSG_API_BEGIN
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_track_cycle_async: null handle");
+    int st = set_device(h);
+    if (st) return st;
+    return track_passes_async(h, static_cast<cudaStream_t>(stream));
     QSG_API_END
 }
 
 extern "C" int qsg_track_cycle_sync(QsgHandle* h)
 {
     QSG_API_BEGIN
-    int st = qsg_track_cycle(h, nullptr);
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_track_cycle_sync: null handle");
+    int st = set_device(h);
     if (st) return st;
+    if ((st = track_passes_sync(h, nullptr))) return st;
     QSG_CUDA(cudaDeviceSynchronize());
     unsigned int flags = 0;
     QSG_CUDA(cudaMemcpy(&flags, h->flags.ptr, sizeof(flags), cudaMemcpyDeviceToHost));

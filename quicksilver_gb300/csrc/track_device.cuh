@@ -6,6 +6,8 @@
 // reference lines each step follows.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include <cstdint>
 
 #include "qsg.h"
@@ -21,6 +23,7 @@ constexpr double kSmallDouble = 1.0e-10;
 constexpr double kHugeDouble = 1.0e+75;
 
 constexpr int kFacets = 24;
+constexpr int kTrackBlock = 128;      // threads per block of the tracking kernel
 constexpr int kCellPoints = 14;
 
 // Structure-of-arrays particle store in device memory (136 B per particle,
@@ -66,6 +69,22 @@ struct DevTally {
     int32_t balance_replicas;
     uint64_t max_segments;
 };
+
+__device__ __forceinline__ void raise_flag(const DevTally& tally, unsigned int bit)
+{
+    atomicOr(tally.error_flags, bit);
+}
+
+// Reserve one slot of `s` for each calling lane with one atomic per warp.
+__device__ __forceinline__ uint64_t append_slot(const DevStore& s)
+{
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(s.count, (unsigned long long)g.size());
+    base = g.shfl(base, 0);
+    return base + g.thread_rank();
+}
 
 // MC_RNG_State.hh:22-33
 __device__ __forceinline__ double rng_sample(uint64_t& seed)

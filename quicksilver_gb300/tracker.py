@@ -1,0 +1,79 @@
+"""Python face of the C-ABI tracking handle (libqsg.so, include/qsg.h).
+
+``Tracker`` is the drop-in for the per-vault tracking launch of the
+reference's ``cycleTracking`` (main.cc:155-236): upload the processing
+particles, track them on the GPU, read back census particles and tallies.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .problem import HostProblem
+
+
+class Tracker:
+    def __init__(self, problem: HostProblem, flux_replicas: int = 1, balance_replicas: int = 1,
+                 particle_capacity: int = 0, max_segments: int = 0, device: int = 0, max_passes: int = 0):
+        self.problem = problem
+        opts = N.QsgOptions(device=device, block_size=0, flux_replicas=flux_replicas,
+                            balance_replicas=balance_replicas, particle_capacity=particle_capacity,
+                            max_segments=max_segments, max_passes=max_passes, reserved=0)
+        self._h = C.c_void_p()
+        N.check(N.lib().qsg_create(C.byref(problem.view), C.byref(opts), C.byref(self._h)))
+        self.num_cells = problem.num_cells
+        self.num_groups = problem.num_groups
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def close(self):
+        if self._h:
+            N.lib().qsg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_particles(self, records: np.ndarray) -> None:
+        recs = np.ascontiguousarray(records, dtype=N.PARTICLE_DTYPE)
+        cols = N.columns_of(recs)
+        soa = N.soa_from_columns(cols)
+        N.check(N.lib().qsg_set_particles(self._h, C.byref(soa), len(recs)))
+
+    def track(self) -> None:
+        N.check(N.lib().qsg_track_cycle_sync(self._h))
+
+    def sizes(self):
+        a, b = C.c_uint64(), C.c_uint64()
+        N.check(N.lib().qsg_sizes(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def census(self) -> np.ndarray:
+        _, n = self.sizes()
+        cols = N.empty_columns(n)
+        soa = N.soa_from_columns(cols)
+        got = C.c_uint64()
+        N.check(N.lib().qsg_get_census(self._h, C.byref(soa), n, C.byref(got)))
+        return N.records_from_columns(cols, got.value)
+
+    def tallies(self):
+        bal = np.zeros(13, dtype=np.uint64)
+        flux = np.zeros(self.num_cells * self.num_groups, dtype=np.float64)
+        N.check(N.lib().qsg_read_tallies(self._h, bal.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                         flux.ctypes.data_as(C.POINTER(C.c_double))))
+        return bal, flux.reshape(self.num_cells, self.num_groups)
+
+    def reset_tallies(self) -> None:
+        N.check(N.lib().qsg_reset_tallies(self._h))
+
+    def device_status(self, clear: bool = True) -> int:
+        f = C.c_uint32()
+        N.check(N.lib().qsg_device_status(self._h, C.byref(f), int(clear)))
+        return f.value

@@ -1,0 +1,164 @@
+"""Generate golden fixtures from the UNMODIFIED reference (test infrastructure).
+
+Needs the reference sources (default /root/reference/src) and builds
+``oracle/_ref/qs_ref_harness`` with ``make -C oracle ref``.  For every deck in
+quicksilver_gb300/decks it runs the reference harness and stores in
+``tests/golden/<deck>.npz``:
+
+* ``balance``        [cycles, 13] uint64, Tallies.cc:400-414 order
+* ``flux``           [cycles, cells, groups] float64 (small decks only)
+* ``flux_cell``      [cycles, cells]  per-cell sums, gid order
+* ``flux_group``     [cycles, groups] per-group sums
+* ``flux_proj``      [cycles, 4] projections on fixed pseudo-random weights
+* ``init_sha``/``census_sha``  sha256 of the sorted 136-byte particle records
+  after cycleInit and after cycleTracking, plus their counts
+* ``init_head``      first 32 sorted records after cycle 0's cycleInit
+* ``table_sha``      sha256 of every problem table in global-cell order
+* ``rng_*``          known-answer vectors of rngSample / rngSpawn
+* ``track_seconds``  reference cycleTracking wall time per cycle (8 threads here)
+
+Usage: python tests/golden/make_golden.py [deck ...]
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import struct
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+DECKS = ROOT / "quicksilver_gb300" / "decks"
+HARNESS = ROOT / "oracle" / "_ref" / "qs_ref_harness"
+REF_SRC = os.environ.get("QS_REF_SRC", "/root/reference/src")
+FULL_FLUX_LIMIT = 20000   # store the whole flux array when cells*groups is at most this
+
+PARTICLE_DTYPE = np.dtype([
+    ("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("vx", "<f8"), ("vy", "<f8"), ("vz", "<f8"),
+    ("kinetic_energy", "<f8"), ("weight", "<f8"), ("time_to_census", "<f8"), ("age", "<f8"),
+    ("num_mean_free_paths", "<f8"), ("num_segments", "<f8"),
+    ("random_number_seed", "<u8"), ("identifier", "<u8"),
+    ("last_event", "<i4"), ("num_collisions", "<i4"), ("breed", "<i4"), ("species", "<i4"),
+    ("domain", "<i4"), ("cell", "<i4"),
+])
+
+TABLES = ["energies", "iso_react_off", "reaction_type", "reaction_nubar", "reaction_xs", "mat_iso_off",
+          "mat_iso_gid", "mat_iso_af", "mat_mass", "cell_volume", "cell_density", "cell_material",
+          "cell_nodes", "cell_planes", "facet_point_coords", "facet_event", "facet_adj_facet", "facet_adj_gid",
+          "time_step"]
+
+
+def read_dump(path: Path) -> dict:
+    out = {}
+    data = path.read_bytes()
+    off = 0
+    while off < len(data):
+        (nlen,) = struct.unpack_from("<I", data, off)
+        off += 4
+        name = data[off:off + nlen].decode()
+        off += nlen
+        dtype = chr(data[off])
+        off += 1
+        (count,) = struct.unpack_from("<Q", data, off)
+        off += 8
+        np_dtype = {"d": "<f8", "q": "<u8", "i": "<i4"}[dtype]
+        nbytes = count * np.dtype(np_dtype).itemsize
+        out[name] = np.frombuffer(data, dtype=np_dtype, count=count, offset=off).copy()
+        off += nbytes
+    return out
+
+
+def particles(d: dict, name: str) -> np.ndarray:
+    f = d[name + "_f64"].reshape(-1, 12)
+    q = d[name + "_u64"].reshape(-1, 2)
+    i = d[name + "_i32"].reshape(-1, 6)
+    recs = np.empty(len(f), dtype=PARTICLE_DTYPE)
+    for k, n in enumerate(PARTICLE_DTYPE.names[:12]):
+        recs[n] = f[:, k]
+    recs["random_number_seed"] = q[:, 0]
+    recs["identifier"] = q[:, 1]
+    for k, n in enumerate(PARTICLE_DTYPE.names[14:]):
+        recs[n] = i[:, k]
+    return recs
+
+
+def sort_records(recs: np.ndarray) -> np.ndarray:
+    return recs[np.lexsort((recs["random_number_seed"], recs["identifier"]))]
+
+
+def sha(arr: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(arr).tobytes()).hexdigest()
+
+
+def projection_weights(cells: int, groups: int) -> np.ndarray:
+    return np.random.default_rng(20240601).uniform(0.5, 1.5, size=(4, cells * groups))
+
+
+def ensure_harness() -> None:
+    res = subprocess.run(["make", "-C", str(ROOT / "oracle"), "ref", f"REF_SRC={REF_SRC}", "-j8"],
+                         capture_output=True, text=True)
+    if res.returncode != 0:
+        raise SystemExit(f"reference build failed:\n{res.stderr[-4000:]}")
+
+
+def run_deck(deck: Path, workdir: Path) -> dict:
+    dump = workdir / (deck.stem + ".dump")
+    env = dict(os.environ, QS_DUMP=str(dump), QS_DUMP_TABLES="1", QS_DUMP_PARTICLES="1", OMP_NUM_THREADS="8")
+    res = subprocess.run([str(HARNESS), "-i", str(deck)], env=env, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise SystemExit(f"reference run failed on {deck}:\n{res.stderr[-4000:]}")
+    return read_dump(dump)
+
+
+def make(deck: Path, workdir: Path) -> None:
+    d = run_deck(deck, workdir)
+    cycles = sum(1 for k in d if k.startswith("balance_c"))
+    G = len(d["energies"]) - 1
+    C = len(d["cell_volume"])
+    out = {"balance": np.stack([d[f"balance_c{c}"] for c in range(cycles)])}
+    flux = np.stack([d[f"flux_c{c}"] for c in range(cycles)])
+    if C * G <= FULL_FLUX_LIMIT:
+        out["flux"] = flux.reshape(cycles, C, G)
+    out["flux_cell"] = flux.reshape(cycles, C, G).sum(axis=2)
+    out["flux_group"] = flux.reshape(cycles, C, G).sum(axis=1)
+    out["flux_proj"] = flux @ projection_weights(C, G).T
+    out["flux_total"] = flux.sum(axis=1)
+    init_sha, census_sha, init_n, census_n = [], [], [], []
+    for c in range(cycles):
+        ini = sort_records(particles(d, f"init_c{c}"))
+        cen = sort_records(particles(d, f"census_c{c}"))
+        init_sha.append(sha(ini))
+        census_sha.append(sha(cen))
+        init_n.append(len(ini))
+        census_n.append(len(cen))
+        if c == 0:
+            out["init_head"] = ini[:32]
+            out["census_head"] = cen[:32]
+    out["init_sha"] = np.array(init_sha)
+    out["census_sha"] = np.array(census_sha)
+    out["init_n"] = np.array(init_n, dtype=np.int64)
+    out["census_n"] = np.array(census_n, dtype=np.int64)
+    out["table_names"] = np.array(TABLES)
+    out["table_sha"] = np.array([sha(d[t]) for t in TABLES])
+    out["mat_names"] = np.array(bytes(d["mat_names"].astype(np.uint8)).decode().split("\n")[:-1])
+    for k in ("rng_seeds", "rng_samples", "rng_states", "rng_spawned", "rng_parent_after", "track_seconds"):
+        out[k] = d[k]
+    np.savez_compressed(HERE / (deck.stem + ".npz"), **out)
+    print(f"{deck.name}: cycles={cycles} cells={C} groups={G} segments={int(out['balance'][:, 12].sum())}")
+
+
+def main(argv: list[str]) -> None:
+    import tempfile
+    ensure_harness()
+    names = argv or sorted(p.stem for p in DECKS.glob("*.inp") if p.stem.startswith("t_") or p.stem == "config1")
+    with tempfile.TemporaryDirectory() as tmp:
+        for name in names:
+            make(DECKS / f"{name}.inp", Path(tmp))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

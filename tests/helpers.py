@@ -1,0 +1,52 @@
+"""Shared helpers for the parity tests (test infrastructure)."""
+from __future__ import annotations
+
+import numpy as np
+
+from quicksilver_gb300 import Deck
+from quicksilver_gb300 import _native as N
+
+DECKS = __import__("pathlib").Path(__file__).resolve().parent.parent / "quicksilver_gb300" / "decks"
+
+
+def load_problem(deck_name: str, overrides: dict | None = None):
+    deck = Deck.from_file(DECKS / deck_name, overrides)
+    return deck, deck.simulation, deck.build()
+
+
+def oracle_run(hp, sim):
+    import oracle_py as O
+    return O.OracleRun(hp.ptr, hp.num_cells, hp.num_groups, hp.source_rates(), sim.n_particles,
+                       sim.e_min, sim.e_max, sim.low_weight_cutoff, sim.load_balance, keepalive=hp)
+
+
+def sort_particles(recs: np.ndarray) -> np.ndarray:
+    return recs[np.lexsort((recs["random_number_seed"], recs["identifier"]))]
+
+
+def assert_flux_close(got: np.ndarray, want: np.ndarray, rel: float = 1e-12, scale_floor: float = 0.0):
+    """Per (cell, group) agreement: |got - want| <= rel*|want| + scale_floor*mean(|want| over nonzero).
+
+    With scale_floor = 0 this is a pure per-entry relative bound (used between
+    two CPU runs with the same libm, where only summation order differs).  The
+    GPU tests pass scale_floor = 1e-12: libdevice's log/sincos round
+    differently from glibc in the last bit, which moves a trajectory by ~1e-15
+    cm; on an entry fed only by a segment that clips a cell corner that is a
+    large *relative* change of a negligible value.  Entries that are zero in
+    `want` must be zero in `got`.
+    """
+    got = np.asarray(got, dtype=np.float64)
+    want = np.asarray(want, dtype=np.float64)
+    assert got.shape == want.shape
+    denom = np.abs(want)
+    bad_zero = (denom == 0) & (got != 0)
+    assert not bad_zero.any(), f"{bad_zero.sum()} entries nonzero where reference is zero"
+    nz = denom > 0
+    if not nz.any():
+        return 0.0
+    floor = scale_floor * float(denom[nz].mean())
+    err = np.abs(got[nz] - want[nz]) / (rel * denom[nz] + floor)
+    worst = float(err.max())
+    assert worst <= 1.0, (f"flux error {worst:.3e} x tolerance (max relative "
+                          f"{float((np.abs(got[nz] - want[nz]) / denom[nz]).max()):.3e})")
+    return worst

@@ -1,0 +1,84 @@
+"""GPU tracking (through the C ABI) against the C oracle, cycle by cycle.
+
+Each cycle the oracle performs cycleInit; its processing particles are given
+to both the oracle and libqsg (qsg_set_particles / qsg_track_cycle_sync /
+qsg_get_census / qsg_read_tallies).  Tracking balance counters must match bit
+for bit; scalar flux per (cell, group) within 1e-12 relative; census
+particles match one to one by identifier (integer fields exactly, floating
+fields to 1e-7 relative -- libdevice's log/sin/cos may differ from libm in the
+last bit, and long histories with many rotations carry that forward; 1e-9
+was observed after ~200 collisions on the fission deck).
+"""
+import numpy as np
+import pytest
+
+from helpers import DECKS, assert_flux_close, load_problem, oracle_run, sort_particles
+from quicksilver_gb300.tracker import Tracker
+
+pytestmark = pytest.mark.gpu
+
+TRACK_SLOTS = [0, 1, 2, 3, 5, 6, 7, 12]   # absorb census escape collision fission produce scatter num_segments
+FP_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "kinetic_energy", "weight", "time_to_census", "age",
+             "num_mean_free_paths", "num_segments"]
+INT_FIELDS = ["random_number_seed", "identifier", "last_event", "num_collisions", "breed", "species",
+              "domain", "cell"]
+SMALL = ["t_homog", "t_absorb", "t_escape", "t_nocoll", "t_scatter_octant", "t_fission", "t_nonflat",
+         "t_default"]
+
+
+def compare_census(got, want):
+    assert len(got) == len(want)
+    g, w = sort_particles(got), sort_particles(want)
+    for f in INT_FIELDS:
+        np.testing.assert_array_equal(g[f], w[f], err_msg=f)
+    for f in FP_FIELDS:
+        np.testing.assert_allclose(g[f], w[f], rtol=1e-7, atol=1e-12, err_msg=f)
+
+
+def run_parity(name, cycles=None, flux_replicas=1):
+    _, sim, hp = load_problem(f"{name}.inp")
+    run = oracle_run(hp, sim)
+    trk = Tracker(hp, flux_replicas=flux_replicas)
+    n_cycles = sim.n_steps if cycles is None else cycles
+    for c in range(n_cycles):
+        run.cycle_init()
+        particles = run.processing()
+        trk.reset_tallies()
+        trk.set_particles(particles)
+        trk.track()
+        bal, flux = trk.tallies()
+        census = trk.census()
+        run.cycle_tracking(0)
+        want_bal = run.balance()
+        np.testing.assert_array_equal(bal[TRACK_SLOTS], want_bal[TRACK_SLOTS], err_msg=f"{name} cycle {c}")
+        want_flux = run.flux()
+        assert_flux_close(flux, want_flux, rel=1e-12, scale_floor=1e-12)
+        assert_flux_close(flux.sum(axis=1), want_flux.sum(axis=1), rel=1e-12)   # per cell
+        assert_flux_close(flux.sum(axis=0), want_flux.sum(axis=0), rel=1e-12)   # per group
+        assert abs(flux.sum() - want_flux.sum()) <= 1e-12 * abs(want_flux.sum())
+        compare_census(census, run.processed())
+        assert trk.device_status() == 0
+        run.cycle_finalize()
+    trk.close()
+
+
+@pytest.mark.parametrize("name", SMALL)
+def test_gpu_tracking_matches_oracle(gpu, name):
+    run_parity(name)
+
+
+def test_gpu_tracking_config1(gpu):
+    run_parity("config1")
+
+
+def test_gpu_flux_replicas(gpu):
+    run_parity("t_homog", cycles=2, flux_replicas=4)
+
+
+def test_gpu_empty_vault(gpu):
+    _, sim, hp = load_problem("t_homog.inp")
+    trk = Tracker(hp)
+    trk.set_particles(np.empty(0, dtype=__import__("quicksilver_gb300").PARTICLE_DTYPE))
+    trk.track()
+    bal, flux = trk.tallies()
+    assert bal.sum() == 0 and flux.sum() == 0 and len(trk.census()) == 0
