@@ -1,0 +1,347 @@
+#!/usr/bin/env python3
+"""Benchmark: segments/s of Quicksilver's cycleTracking phase on one GB300.
+
+Workload (N=1): the non-flat multi-material problem -- 40^3 cells over a
+40 cm cube, 3 materials in concentric spherical shells (radii 8 and 16 cm),
+2 isotopes x 3 reactions per material with polynomial cross sections,
+230 groups, 1e6 particles (quicksilver_gb300/decks/config2.inp, seeded
+synthetic deck).  One step = one cycle's tracking (the reference's
+cycleTracking phase, its FOM denominator MC_Fast_Timer.cc:97-104) over the
+particles the device-side cycle set-up produced; set-up and finalisation run
+between steps, untimed.  Segments are the reference's _numSegments counter.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  `value` = segments / device time of the tracking
+calls with particles already in HBM (L2 flushed before every step);
+`e2e` = the same through the C ABI from pinned host buffers (H2D of the
+cycle's particles, tracking, D2H of census particles, counters and flux
+inside the timed region).  `--impl reference` times the CPU port of the
+reference algorithm (oracle/qs_oracle.c, all host threads) on the same deck:
+the reference's own C++ cannot be built on the benchmark host (its sources
+are not there), so the port -- bit-exact with the reference on the golden
+decks -- stands in for it.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+DECK = ROOT / "quicksilver_gb300" / "decks" / "config2.inp"
+WORKLOAD = ("config2: 40^3-cell 40 cm cube, 3 materials in spherical shells (r=8, 16 cm), 2 isotopes x "
+            "3 reactions each, polynomial cross sections, 230 groups, 1e6 particles, FP64")
+METRIC = "segments/s per cycle (cycleTracking phase)"
+B_ALG_PER_SEGMENT = 288          # algorithmic HBM bytes per segment (136-B record read+write + 16-B flux RMW)
+PROFILE_SUMMARY = ROOT / "profiles" / "track_kernel_config2.md"
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.device_index = device_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device_index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def profile_traffic_per_segment():
+    """DRAM bytes per segment of the tracking kernel from the committed ncu summary."""
+    if not PROFILE_SUMMARY.exists():
+        return None
+    for line in PROFILE_SUMMARY.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_segment:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_port_rate(deck_path: Path, cycles: int, threads: int):
+    """The CPU port (oracle) timed on the host cores: (segments/s, segments, seconds)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_py
+    from quicksilver_gb300 import Deck
+    deck = Deck.from_file(deck_path)
+    sim = deck.simulation
+    hp = deck.build()
+    run = oracle_py.OracleRun(hp.ptr, hp.num_cells, hp.num_groups, hp.source_rates(), sim.n_particles,
+                              sim.e_min, sim.e_max, sim.low_weight_cutoff, sim.load_balance, keepalive=hp)
+    seg = 0
+    secs = 0.0
+    for _ in range(cycles):
+        run.cycle_init()
+        t0 = time.perf_counter()
+        run.cycle_tracking(threads)
+        secs += time.perf_counter() - t0
+        seg += int(run.balance()[12])
+        run.cycle_finalize()
+    run.close()
+    return seg / secs, seg, secs
+
+
+def run_reference_arm(args, world, rank):
+    """--impl reference: the CPU port of the reference algorithm on the host cores."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_py
+    from quicksilver_gb300 import Deck
+    deck = Deck.from_file(DECK)
+    sim = deck.simulation
+    hp = deck.build()
+    run = oracle_py.OracleRun(hp.ptr, hp.num_cells, hp.num_groups, hp.source_rates(), sim.n_particles,
+                              sim.e_min, sim.e_max, sim.low_weight_cutoff, sim.load_balance, keepalive=hp)
+    for _ in range(args.warmup):
+        run.cycle_init()
+        run.cycle_tracking(threads)
+        run.cycle_finalize()
+    seg, secs = 0, 0.0
+    for _ in range(args.steps):
+        run.cycle_init()
+        t0 = time.perf_counter()
+        run.cycle_tracking(threads)
+        secs += time.perf_counter() - t0
+        seg += int(run.balance()[12])
+        run.cycle_finalize()
+    value = seg / secs
+    sample = f"{args.steps} whole config2 cycles ({seg} segments) after {args.warmup} warm-up cycles"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded deck config2.inp)",
+            "config": {"workload": WORKLOAD, "impl": "CPU port of the reference algorithm (oracle/qs_oracle.c), "
+                       "OpenMP over particles; the reference C++ sources are not present on this host"},
+            "cpu_baseline": {"value": value, "unit": "segments/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "segments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--flux-replicas", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_env()
+
+    if args.impl == "reference":
+        run_reference_arm(args, world, rank)
+        return
+
+    import torch
+    from quicksilver_gb300 import Deck
+    from quicksilver_gb300 import _native as N
+    from quicksilver_gb300.monte_carlo import MonteCarlo
+
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    deck = Deck.from_file(DECK)
+    mc = MonteCarlo(deck, flux_replicas=args.flux_replicas, device=local)
+    h = mc.tracker.handle
+    lib = N.lib()
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # 256 MiB > 129 MB L2
+
+    def flush_l2():
+        flush.add_(1.0)
+
+    # warm-up cycles (whole cycles on the device)
+    for _ in range(args.warmup):
+        mc.cycle_init(stream)
+        mc.cycle_tracking(stream)
+        mc.cycle_finalize(stream)
+    barrier()
+
+    # ---- device-resident timed steps: tracking phase only ----
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    first_cycle = mc.cycles
+    with ClockSampler(local) as clocks:
+        barrier()
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            mc.cycle_init(stream)
+            flush_l2()
+            events[k][0].record(stream)
+            N.check(lib.qsg_track_cycle(h, sp))
+            events[k][1].record(stream)
+            mc.cycle_finalize(stream)
+        barrier()
+        wall = time.perf_counter() - wall0
+    ms = [a.elapsed_time(b) for a, b in events]
+    hist = mc.history(first_cycle, args.steps)
+    segments = int(hist.balance[:, N.BAL["num_segments"]].sum())
+    track_s = sum(ms) / 1e3
+    flags = mc.device_status()
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    n_cap = int(2 * deck.simulation.n_particles)
+    pinned = {name: torch.empty(n_cap, dtype={"<f8": torch.float64, "<u8": torch.int64, "<i4": torch.int32}[
+        N.PARTICLE_DTYPE[name].str], pin_memory=True) for name in N.SOA_FIELDS}
+    census_pinned = {name: torch.empty_like(t, pin_memory=True) for name, t in pinned.items()}
+    soa_in = N.soa_from_pointers({k: v.data_ptr() for k, v in pinned.items()})
+    soa_out = N.soa_from_pointers({k: v.data_ptr() for k, v in census_pinned.items()})
+    ncell_g = mc.problem.num_cells * mc.problem.num_groups
+    flux_host = torch.empty(ncell_g, dtype=torch.float64, pin_memory=True)
+    bal_host = torch.empty(13, dtype=torch.int64, pin_memory=True)
+    e2e_s, e2e_seg, h2d, d2h = 0.0, 0, 0, 0
+    e2e_steps = args.steps
+    for k in range(e2e_steps):
+        mc.cycle_init(stream)
+        n = C.c_uint64()
+        N.check(lib.qsg_get_processing(h, C.byref(soa_in), n_cap, C.byref(n)))   # the host's vault, untimed
+        barrier()
+        t0 = time.perf_counter()
+        N.check(lib.qsg_reset_tallies(h))
+        N.check(lib.qsg_set_particles(h, C.byref(soa_in), n.value))
+        N.check(lib.qsg_track_cycle(h, sp))
+        nc = C.c_uint64()
+        N.check(lib.qsg_get_census(h, C.byref(soa_out), n_cap, C.byref(nc)))
+        N.check(lib.qsg_read_tallies(h, C.cast(C.c_void_p(bal_host.data_ptr()), C.POINTER(C.c_uint64)),
+                                     C.cast(C.c_void_p(flux_host.data_ptr()), C.POINTER(C.c_double))))
+        torch.cuda.synchronize()
+        e2e_s += time.perf_counter() - t0
+        e2e_seg += int(bal_host[12])
+        h2d += 136 * n.value
+        d2h += 136 * nc.value + 13 * 8 + 8 * ncell_g
+        mc.cycle_finalize(stream)
+    flags |= mc.device_status()
+
+    # max over ranks
+    if pg is not None:
+        t = torch.tensor([track_s, e2e_s, wall], dtype=torch.float64, device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        track_s, e2e_s, wall = t.tolist()
+        s = torch.tensor([segments, e2e_seg], dtype=torch.float64, device="cuda")
+        pg.all_reduce(s)
+        segments, e2e_seg = int(s[0]), int(s[1])
+    if rank != 0:
+        return
+
+    value = segments / track_s
+    peak, peak_kind = measured_peak_hbm()
+    seg_per_launch = segments / world / args.steps
+    achieved = B_ALG_PER_SEGMENT * seg_per_launch / (track_s / args.steps) / 1e9
+    tps = profile_traffic_per_segment()
+    line = {
+        "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * track_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded deck config2.inp)",
+        "config": {"workload": WORKLOAD, "step": "one cycle's tracking (cycleTracking phase)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "flushed (256 MiB write) before every timed step", "particles_in_hbm": True,
+                   "flux_replicas": args.flux_replicas, "wall_s_timed_region": wall},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "traffic": (tps * seg_per_launch) if tps else None,
+                     "algorithmic_bytes_per_segment": B_ALG_PER_SEGMENT,
+                     "note": "FP64-issue bound on GB300, see profiles/"},
+        "e2e": {"value": e2e_seg / e2e_s, "unit": "segments/s", "h2d_bytes_per_step": h2d // e2e_steps,
+                "d2h_bytes_per_step": d2h // e2e_steps},
+        # event-timed region: one tracking-kernel launch per step (config2 has no fission, so one pass)
+        "gpu_launches": args.steps,
+        "device_flags": flags,
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        rate, seg, secs = cpu_port_rate(DECK, 2, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": rate, "unit": "segments/s", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"config2 cycles 0-1 ({seg} segments, {secs:.1f} s tracking) with "
+                                          f"{os.cpu_count()} OpenMP threads"}
+    print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
