@@ -1,0 +1,60 @@
+"""CPU-side checks of the C ABI: the library loads without a GPU, exports
+every function include/qsg.h declares, and its host-only entry points (deck
+reader, table builder, error reporting) behave like the reference's."""
+import ctypes
+import re
+
+import numpy as np
+import pytest
+
+from helpers import DECKS
+from quicksilver_gb300 import Deck
+from quicksilver_gb300 import _native as N
+
+HEADER = DECKS.parent.parent / "include" / "qsg.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^int\s+(qsg_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    names = declared_functions()
+    assert len(names) >= 30
+    for name in names:
+        assert hasattr(native_lib, name), f"{name} declared in qsg.h but not exported"
+
+
+def test_abi_version(native_lib):
+    assert native_lib.qsg_abi_version() == 1
+
+
+def test_bad_deck_reports_error():
+    with pytest.raises(N.QsgError) as ei:
+        Deck.from_string("Geometry:\n   material: x\n   shape: cone\n")
+    assert ei.value.code == N.QSG_ERR_INVALID and "brick or sphere" in str(ei.value)
+    with pytest.raises(N.QsgError) as ei:
+        Deck.from_file("/nonexistent/deck.inp")
+    assert ei.value.code == N.QSG_ERR_IO
+
+
+def test_default_problem_and_overrides():
+    # no Geometry block: supplyDefaults (Parameters.cc:350-379)
+    d = Deck.from_string("Simulation:\n   nx: 2\n   ny: 2\n   nz: 2\n   nGroups: 4\n", {"lx": 4, "ly": 4, "lz": 4})
+    s = d.simulation
+    assert (s.nx, s.n_groups, s.lx) == (2, 4, 4.0)
+    hp = d.build()
+    assert hp.num_materials == 1 and hp.num_cells == 8
+    assert np.all(hp.array("cell_volume") > 0)
+    with pytest.raises(N.QsgError):
+        d.set("noSuchKey", 1)
+
+
+def test_create_without_gpu_fails_loudly(has_gpu):
+    if has_gpu:
+        pytest.skip("a GPU is visible")
+    _, _, hp = None, None, Deck.from_file(DECKS / "t_homog.inp").build()
+    h = ctypes.c_void_p()
+    rc = N.lib().qsg_create(ctypes.byref(hp.view), None, ctypes.byref(h))
+    assert rc == N.QSG_ERR_NO_DEVICE and "no CUDA device" in N.last_error()
