@@ -53,7 +53,9 @@ enum {
     QSG_DEV_STORE_OVERFLOW = 1u << 4,   /* census / extra store overflow      */
     QSG_DEV_BAD_FACET = 1u << 5,        /* no facet bounds the particle       */
     QSG_DEV_NEGATIVE_DISTANCE = 1u << 6,/* MC_Segment_Outcome.cc:265-276      */
-    QSG_DEV_PASS_LIMIT = 1u << 7        /* fission products left after max_passes */
+    QSG_DEV_PASS_LIMIT = 1u << 7,       /* fission products left after max_passes */
+    QSG_DEV_SCREEN_MISS = 1u << 8       /* verification build only: the FP32 facet
+                                           screen skipped a facet FP64 accepts */
 };
 
 /* ---- enums shared with the reference ------------------------------------ */

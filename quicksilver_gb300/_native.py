@@ -11,7 +11,11 @@ from pathlib import Path
 
 import numpy as np
 
-LIB_PATH = Path(__file__).resolve().parent / "lib" / "libqsg.so"
+import os
+
+# QSG_LIB=verify selects the screen-verification build (libqsg_verify.so)
+LIB_PATH = Path(__file__).resolve().parent / "lib" / (
+    "libqsg_verify.so" if os.environ.get("QSG_LIB") == "verify" else "libqsg.so")
 
 QSG_OK = 0
 QSG_ERR_INVALID = 1
@@ -136,7 +140,7 @@ def lib() -> C.CDLL:
     if _lib is None:
         if not LIB_PATH.exists():
             from . import build as _build
-            _build.build()
+            _build.build(verify_screen=LIB_PATH.name == "libqsg_verify.so")
         handle = C.CDLL(str(LIB_PATH))
         for name, (args, res) in _SIGNATURES.items():
             fn = getattr(handle, name)

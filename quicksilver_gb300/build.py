@@ -64,43 +64,52 @@ def _run(cmd: list[str]) -> None:
         sys.stderr.write(res.stderr)
 
 
-def build(verbose: bool = False, ptxas_verbose: bool = False) -> Path:
-    """Compile every translation unit and link ``libqsg.so``; returns its path."""
-    OBJ.mkdir(parents=True, exist_ok=True)
+def build(verbose: bool = False, ptxas_verbose: bool = False, verify_screen: bool = False) -> Path:
+    """Compile every translation unit and link ``libqsg.so``; returns its path.
+
+    ``verify_screen`` builds ``libqsg_verify.so`` instead: the facet search also
+    evaluates every facet the FP32 screen skipped and raises QSG_DEV_SCREEN_MISS
+    if FP64 would have accepted one (a test build; slower).
+    """
+    obj_dir = OBJ / ("verify" if verify_screen else "")
+    lib = OUT / ("libqsg_verify.so" if verify_screen else "libqsg.so")
+    obj_dir.mkdir(parents=True, exist_ok=True)
     nvcc = _nvcc()
     jobs = []
     objs = []
     for rel in HOST_SOURCES:
         src = CSRC / rel
-        obj = OBJ / (Path(rel).stem + ".o")
+        obj = obj_dir / (Path(rel).stem + ".o")
         objs.append(obj)
         if _stale(obj, src):
             jobs.append(["g++", *CXX_FLAGS, f"-I{INCLUDE}", f"-I{CSRC / 'host'}", "-c", str(src), "-o", str(obj)])
     for rel in CUDA_SOURCES:
         src = CSRC / rel
-        obj = OBJ / (Path(rel).stem + ".cu.o")
+        obj = obj_dir / (Path(rel).stem + ".cu.o")
         objs.append(obj)
         if _stale(obj, src):
             flags = list(NVCC_FLAGS)
             if ptxas_verbose:
                 flags += ["-Xptxas", "-v"]
+            if verify_screen:
+                flags += ["-DQSG_VERIFY_SCREEN"]
             jobs.append([nvcc, *NVCC_ARCH, *flags, f"-I{INCLUDE}", f"-I{CSRC}", f"-I{CSRC / 'host'}",
                          "-c", str(src), "-o", str(obj)])
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             for fut in [ex.submit(_run, j) for j in jobs]:
                 fut.result()
-    if jobs or not LIB.exists():
+    if jobs or not lib.exists():
         cuda_lib = _cuda_home() / "lib64"
         if not cuda_lib.exists():
             cuda_lib = _cuda_home() / "lib"
-        link = ["g++", "-shared", "-o", str(LIB), *map(str, objs), f"-L{cuda_lib}",
+        link = ["g++", "-shared", "-o", str(lib), *map(str, objs), f"-L{cuda_lib}",
                 f"-Wl,-rpath,{cuda_lib}", "-lcudart", "-lpthread"]
         _run(link)
     if verbose:
-        print(f"built {LIB}")
-    return LIB
+        print(f"built {lib}")
+    return lib
 
 
 if __name__ == "__main__":
-    build(verbose=True, ptxas_verbose="-v" in sys.argv)
+    build(verbose=True, ptxas_verbose="-v" in sys.argv, verify_screen="--verify-screen" in sys.argv)

@@ -101,9 +101,9 @@ __global__ void __launch_bounds__(kInitBlock) source_kernel(SourceArgs a)
     while (current < which_volume) {
         facet++;
         if (facet == kFacets) break;
-        p0 = nodes + 3 * tb.facet_local[facet][0];
-        p1 = nodes + 3 * tb.facet_local[facet][1];
-        p2 = nodes + 3 * tb.facet_local[facet][2];
+        p0 = nodes + 3 * kFacetLocal[facet][0];
+        p1 = nodes + 3 * kFacetLocal[facet][1];
+        p2 = nodes + 3 * kFacetLocal[facet][2];
         current += tet_det(p0, p1, p2, c);
     }
     double r1 = rng_sample(p.seed);

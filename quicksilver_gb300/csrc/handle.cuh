@@ -184,7 +184,9 @@ struct QsgHandle {
     qsg::DevBuf<double> energies, sigma_total, macro_xs, class_nubar, material_mass, cell_nodes, cell_center, planes;
     qsg::DevBuf<int32_t> class_num_reactions, class_material, cell_class, adj_cell;
     qsg::DevBuf<int8_t> class_type;
-    qsg::DevBuf<uint8_t> adj_facet_event;
+    qsg::DevBuf<uint8_t> adj_facet_event, proj;
+    qsg::DevBuf<float4> plane32;
+    qsg::DevBuf<float> node32;
     qsg::DevTables tables{};
     // host copies needed by the cycle set-up
     std::vector<double> h_cell_volume;

@@ -77,8 +77,81 @@ __device__ __forceinline__ double distance_to_segment(double plane_tolerance, do
     return kHugeDouble;
 }
 
+// FP32 screen of one facet.  Returns true when the reference's FP64
+// computation for this facet (MCT.cc:580-606 and :280-395) is *proven* to end
+// in _hugeDouble, so the facet can be skipped: either its outward normal does
+// not face the direction (dot <= 0), or the FP64 inside test must see crosses
+// of clearly mixed sign.  Every quantity is computed in float in cell-local
+// coordinates with an explicit bound on its distance from the FP64 value the
+// reference computes (u = 2^-24 is the float unit roundoff; the factors are
+// several times the rounding-error counts); any doubt -- a tiny dot, NaN, a
+// bound that does not separate -- answers false and the facet is evaluated
+// exactly in FP64.
+__device__ __forceinline__ bool facet_screened_out(const float4 pl, uint8_t proj, const float* n32, const int8_t* loc,
+                                                   float x, float y, float z, float a, float b, float g,
+                                                   float pos_max, float slack)
+{
+    constexpr float u = 5.9604645e-8f;
+    if (proj == 0xff) return true;   // no dominant normal component: the FP64 test always fails
+    const float s_dot = fabsf(pl.x * a) + fabsf(pl.y * b) + fabsf(pl.z * g);
+    const float d = pl.x * a + pl.y * b + pl.z * g;
+    const float e_d = 16.0f * u * s_dot + 1e-12f;
+    if (d < -e_d) return true;                   // FP64 dot <= 0: not a candidate
+    if (!(d > 2.0f * e_d)) return false;         // sign uncertain (or NaN): evaluate exactly
+    const float t_n = fabsf(pl.x * x) + fabsf(pl.y * y) + fabsf(pl.z * z) + fabsf(pl.w);
+    const float n = -(pl.x * x + pl.y * y + pl.z * z + pl.w);
+    const float e_n = 16.0f * u * t_n + slack;
+    const float tt = n * __frcp_rn(d);
+    const float att = fabsf(tt);
+    const float e_t = (e_n + att * e_d * 1.01f) / (d - e_d) + 4.0f * u * att;
+    const int iu = proj & 3, iv = proj >> 2;
+    const float pu = (iu == 0) ? x : ((iu == 1) ? y : z);
+    const float pv = (iv == 0) ? x : ((iv == 1) ? y : z);
+    const float du = (iu == 0) ? a : ((iu == 1) ? b : g);
+    const float dv = (iv == 0) ? a : ((iv == 1) ? b : g);
+    const float ipu = pu + tt * du;
+    const float ipv = pv + tt * dv;
+    const float ip_max = fmaxf(fabsf(ipu), fabsf(ipv));
+    const float e_ip = e_t + 3.0f * u * (pos_max + att + ip_max) + slack;
+    float cmin = 3.4e38f, cmax = -3.4e38f, csum = 0.0f, ecmax = 0.0f, amax = 0.0f;
+    float vu[3], vv[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        vu[k] = __ldg(n32 + 3 * loc[k] + iu);
+        vv[k] = __ldg(n32 + 3 * loc[k] + iv);
+        amax = fmaxf(amax, fmaxf(fabsf(vu[k]), fabsf(vv[k])));
+    }
+    const float e_v = 3.0f * u * amax + slack;   // vertex: float rounding of (node - centre)
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        // the reference's crosses are cross1 (0->1), cross2 (1->2), cross0 (2->0)
+        const int k1 = (k + 1) % 3;
+        const float eu = vu[k1] - vu[k], ev = vv[k1] - vv[k];
+        const float ru = ipu - vu[k], rv = ipv - vv[k];
+        const float c = eu * rv - ev * ru;
+        // edge error (two vertices) times the lever arm, lever-arm error
+        // (intersection point and vertex) times the edge, and float rounding
+        const float ec = (fabsf(ru) + fabsf(rv)) * (2.0f * e_v) + (fabsf(eu) + fabsf(ev)) * (e_ip + e_v) +
+                         8.0f * u * (fabsf(eu * rv) + fabsf(ev * ru));
+        cmin = fminf(cmin, c);
+        cmax = fmaxf(cmax, c);
+        csum += c;
+        ecmax = fmaxf(ecmax, ec);
+    }
+    const float cabs = fmaxf(fabsf(cmin), fabsf(cmax));
+    const float tol = 1.01e-9f * (fabsf(csum) + 3.0f * ecmax + 12.0f * u * cabs) + 1e-30f;
+    const float thr = tol + ecmax;
+    return (cmin <= -thr) && (cmax >= thr);
+}
+
 // MCT_Nearest_Facet (MCT.cc:86-137) with MCT_Nearest_Facet_3D_G
 // (MCT.cc:549-621) and both Find_Nearest overloads (MCT.cc:436-536).
+// Facets the FP32 screen proves to be _hugeDouble are not evaluated; the rest
+// go through the reference's FP64 computation.  Find_Nearest is then applied
+// to the 24 values: the smallest positive distance with `<=` (a later facet
+// wins a tie); if none, the largest non-positive one; _hugeDouble entries
+// count as positive, so when no finite positive distance exists the result is
+// _hugeDouble at the highest-numbered facet holding it.
 // Moves the particle toward the cell centre on a retry, as the reference
 // does through its coordinate reference (MCT.cc:510, 656-666).
 __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Particle& p, int& facet_out)
@@ -86,39 +159,90 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
     const int cell = p.cell;
     const double* planes = t.planes + (int64_t)cell * (kFacets * 4);
     const double* nodes = t.cell_nodes + (int64_t)cell * (kCellPoints * 3);
+    const float4* pl32 = t.plane32 + (int64_t)cell * kFacets;
+    const float* n32 = t.node32 + (int64_t)cell * (kCellPoints * 3);
+    const uint8_t* proj = t.proj + (int64_t)cell * kFacets;
+    const double* ctr = t.cell_center + 3 * (int64_t)cell;
+    const double cx = __ldg(ctr + 0), cy = __ldg(ctr + 1), cz = __ldg(ctr + 2);
+    const float a32 = (float)p.alpha, b32 = (float)p.beta, g32 = (float)p.gamma;
+    const float slack = (float)t.abs_slack;
     int iteration = 0;
     double move_factor = 0.5 * kSmallDouble;
     for (;;) {
-        double plane_tolerance = 1e-16 * (p.x * p.x + p.y * p.y + p.z * p.z);
+        const float x32 = (float)(p.x - cx), y32 = (float)(p.y - cy), z32 = (float)(p.z - cz);
+        const float pos_max = fmaxf(fabsf(x32), fmaxf(fabsf(y32), fabsf(z32)));
+        uint32_t exact = 0;
+#pragma unroll 4
+        for (int f = 0; f < kFacets; f++) {
+            if (!facet_screened_out(__ldg(pl32 + f), __ldg(proj + f), n32, kFacetLocal[f], x32, y32, z32, a32, b32,
+                                    g32, pos_max, slack))
+                exact |= 1u << f;
+        }
         double best = 1e80;
         int best_f = 0;
         double neg = -kHugeDouble;
         int neg_f = 0;
-        for (int f = 0; f < kFacets; f++) {
-            const double2 ab = __ldg(reinterpret_cast<const double2*>(planes + 4 * f));
-            const double2 cd = __ldg(reinterpret_cast<const double2*>(planes + 4 * f + 2));
-            double d = kHugeDouble;
-            double dot = ab.x * p.alpha + ab.y * p.beta + cd.x * p.gamma;
-            if (dot > 0.0) {
+        int huge_f = -1;   // highest facet whose value is _hugeDouble
+        const uint32_t screened = ~exact & 0xffffffu;
+        if (screened) huge_f = 31 - __clz(screened);
+#ifdef QSG_VERIFY_SCREEN
+        {
+            // verification build: every screened facet must be _hugeDouble in FP64
+            const double plane_tolerance = 1e-16 * (p.x * p.x + p.y * p.y + p.z * p.z);
+            for (int f = 0; f < kFacets; f++) {
+                if (!((screened >> f) & 1u)) continue;
+                const double* pl = planes + 4 * f;
+                const double dot = pl[0] * p.alpha + pl[1] * p.beta + pl[2] * p.gamma;
+                if (!(dot > 0.0)) continue;
                 double q0[3], q1[3], q2[3];
-                const double* n0 = nodes + 3 * t.facet_local[f][0];
-                const double* n1 = nodes + 3 * t.facet_local[f][1];
-                const double* n2 = nodes + 3 * t.facet_local[f][2];
-#pragma unroll
-                for (int a = 0; a < 3; a++) {
-                    q0[a] = __ldg(n0 + a);
-                    q1[a] = __ldg(n1 + a);
-                    q2[a] = __ldg(n2 + a);
+                for (int k = 0; k < 3; k++) {
+                    q0[k] = nodes[3 * kFacetLocal[f][0] + k];
+                    q1[k] = nodes[3 * kFacetLocal[f][1] + k];
+                    q2[k] = nodes[3 * kFacetLocal[f][2] + k];
                 }
-                d = distance_to_segment(plane_tolerance, dot, ab.x, ab.y, cd.x, cd.y, q0, q1, q2, p);
+                if (distance_to_segment(plane_tolerance, dot, pl[0], pl[1], pl[2], pl[3], q0, q1, q2, p) != kHugeDouble)
+                    raise_flag(tally, QSG_DEV_SCREEN_MISS);
             }
-            // Find_Nearest: positive distances with `<=` (later facet wins a
-            // tie), otherwise the largest non-positive one.
-            if (d > 0.0) {
-                if (d <= best) { best = d; best_f = f; }
-            } else if (d > neg) {
-                neg = d; neg_f = f;
+        }
+#endif
+        if (exact) {
+            const double plane_tolerance = 1e-16 * (p.x * p.x + p.y * p.y + p.z * p.z);
+            uint32_t m = exact;
+            while (m) {
+                const int f = __ffs(m) - 1;
+                m &= m - 1;
+                const double2 ab = __ldg(reinterpret_cast<const double2*>(planes + 4 * f));
+                const double2 cd = __ldg(reinterpret_cast<const double2*>(planes + 4 * f + 2));
+                double d = kHugeDouble;
+                const double dot = ab.x * p.alpha + ab.y * p.beta + cd.x * p.gamma;
+                if (dot > 0.0) {
+                    double q0[3], q1[3], q2[3];
+                    const double* n0 = nodes + 3 * kFacetLocal[f][0];
+                    const double* n1 = nodes + 3 * kFacetLocal[f][1];
+                    const double* n2 = nodes + 3 * kFacetLocal[f][2];
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        q0[k] = __ldg(n0 + k);
+                        q1[k] = __ldg(n1 + k);
+                        q2[k] = __ldg(n2 + k);
+                    }
+                    d = distance_to_segment(plane_tolerance, dot, ab.x, ab.y, cd.x, cd.y, q0, q1, q2, p);
+                }
+                if (d == kHugeDouble) {
+                    if (f > huge_f) huge_f = f;
+                } else if (d > 0.0) {
+                    if (d <= best) { best = d; best_f = f; }
+                } else if (d > neg) {
+                    neg = d;
+                    neg_f = f;
+                }
             }
+        }
+        // _hugeDouble is positive and larger than any finite distance, so it
+        // only wins when no finite positive distance exists
+        if (best == 1e80 && huge_f >= 0) {
+            best = kHugeDouble;
+            best_f = huge_f;
         }
         if (best == kHugeDouble && neg != -kHugeDouble) { best = neg; best_f = neg_f; }
         bool retry = false;
@@ -149,15 +273,20 @@ __device__ __forceinline__ int segment_outcome(const DevTables& t, const DevTall
                                                int cls, double* flux_row)
 {
     double d_coll, d_facet, d_census;
-    double speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
+    if (p.speed < 0.0) p.speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
+    const double speed = p.speed;
     bool force_collision = false;
     if (p.num_mean_free_paths < 0.0) {
         force_collision = true;
         p.num_mean_free_paths = kSmallDouble;
     }
-    double sigma = __ldg(t.sigma_total + (int64_t)cls * t.num_groups + p.group);
-    p.total_xs = sigma;
-    p.mean_free_path = (sigma == 0.0) ? kHugeDouble : 1.0 / sigma;
+    const int key = cls * t.num_groups + p.group;
+    if (key != p.xs_key) {
+        const double sigma = __ldg(t.sigma_total + key);
+        p.total_xs = sigma;
+        p.mean_free_path = (sigma == 0.0) ? kHugeDouble : 1.0 / sigma;
+        p.xs_key = key;
+    }
     if (p.num_mean_free_paths == 0.0) {
         double r = rng_sample(p.seed);
         p.num_mean_free_paths = -1.0 * log(r);
@@ -234,6 +363,7 @@ __device__ __forceinline__ void update_trajectory(double energy, double angle, P
     p.vx = speed * p.alpha;
     p.vy = speed * p.beta;
     p.vz = speed * p.gamma;
+    p.speed = -1.0;   // |velocity| of the new velocity is recomputed when next needed
     r = rng_sample(p.seed);
     p.num_mean_free_paths = -1.0 * log(r);
 }
@@ -318,10 +448,12 @@ __device__ __forceinline__ void reflect_particle(const DevTables& t, Particle& p
         p.beta -= dot * ny;
         p.gamma -= dot * nz;
     }
-    double speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
+    // |velocity| of the unchanged velocity: the cached value has the same bits
+    const double speed = (p.speed < 0.0) ? sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz) : p.speed;
     p.vx = speed * p.alpha;
     p.vy = speed * p.beta;
     p.vz = speed * p.gamma;
+    p.speed = -1.0;   // the next segment recomputes |velocity| of the new velocity
 }
 
 __device__ __forceinline__ int balance_slot(int local)
@@ -485,8 +617,9 @@ int validate_problem(const QsgProblem* p)
         !p->cell_number_density)
         return fail(QSG_ERR_INVALID, "problem: mesh tables missing");
     for (int k = 0; k < 72; k++)
-        if (p->facet_local_points[k] < 0 || p->facet_local_points[k] >= kCellPoints)
-            return fail(QSG_ERR_INVALID, "problem: facet_local_points must index a cell's 14 points");
+        if (p->facet_local_points[k] != kFacetLocalHost[k / 3][k % 3])
+            return fail(QSG_ERR_UNSUPPORTED, "problem: facet_local_points differ from Quicksilver's 24-facet "
+                        "hex-cell convention (MC_Domain.cc:41-46)");
     for (int i = 0; i < p->num_isotopes; i++)
         if (p->isotope_reaction_offset[i + 1] < p->isotope_reaction_offset[i])
             return fail(QSG_ERR_INVALID, "problem: isotope_reaction_offset not monotone");
@@ -655,9 +788,46 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
     t.planes = h->planes.ptr;
     t.adj_cell = h->adj_cell.ptr;
     t.adj_facet_event = h->adj_facet_event.ptr;
-    for (int f = 0; f < kFacets; f++)
-        for (int k = 0; k < 3; k++) t.facet_local[f][k] = (int8_t)p->facet_local_points[f * 3 + k];
     t.time_step = p->time_step;
+
+    // FP32 screening tables in cell-local coordinates (origin: the cell's
+    // MCT_Cell_Position_3D_G centre), and the projection of each facet's FP64
+    // inside test (MCT.cc:331-385: C, then B, then A dominant).
+    std::vector<float4> plane32((size_t)C * kFacets);
+    std::vector<float> node32((size_t)C * kCellPoints * 3);
+    std::vector<uint8_t> proj((size_t)C * kFacets);
+    double lmax = 0.0, dmax = 0.0;
+    for (int64_t c = 0; c < C; c++) {
+        const double cx = center[c * 3 + 0], cy = center[c * 3 + 1], cz = center[c * 3 + 2];
+        for (int k = 0; k < kCellPoints; k++) {
+            const double* nd = &nodes[(c * kCellPoints + k) * 3];
+            node32[(c * kCellPoints + k) * 3 + 0] = (float)(nd[0] - cx);
+            node32[(c * kCellPoints + k) * 3 + 1] = (float)(nd[1] - cy);
+            node32[(c * kCellPoints + k) * 3 + 2] = (float)(nd[2] - cz);
+            lmax = std::max(lmax, fabs(nd[0]) + fabs(nd[1]) + fabs(nd[2]));
+        }
+        for (int f = 0; f < kFacets; f++) {
+            const double* pl = &planes[(c * kFacets + f) * 4];
+            const double A = pl[0], B = pl[1], Cc = pl[2], D = pl[3];
+            const double dl = D + A * cx + B * cy + Cc * cz;
+            plane32[c * kFacets + f] = make_float4((float)A, (float)B, (float)Cc, (float)dl);
+            dmax = std::max(dmax, fabs(D));
+            uint8_t pr;
+            if (Cc < -0.5 || Cc > 0.5) pr = 0 | (1 << 2);
+            else if (B < -0.5 || B > 0.5) pr = 2 | (0 << 2);
+            else if (A < -0.5 || A > 0.5) pr = 1 | (2 << 2);
+            else pr = 0xff;
+            proj[c * kFacets + f] = pr;
+        }
+    }
+    if ((st = h->plane32.upload(plane32)) || (st = h->node32.upload(node32)) || (st = h->proj.upload(proj))) return st;
+    t.plane32 = h->plane32.ptr;
+    t.node32 = h->node32.ptr;
+    t.proj = h->proj.ptr;
+    // FP64 rounding of quantities formed from global coordinates (numerator,
+    // intersection point, the shifted plane offset) stays below a few units of
+    // 2^-53 times these magnitudes; 16x that is the screen's absolute slack
+    t.abs_slack = 16.0 * 1.1102230246251565e-16 * (4.0 * lmax + 2.0 * dmax) + 1e-30;
     return QSG_OK;
 }
 
@@ -834,6 +1004,7 @@ extern "C" int qsg_destroy(QsgHandle* h)
     h->material_mass.free(); h->cell_nodes.free(); h->cell_center.free(); h->planes.free();
     h->class_num_reactions.free(); h->class_material.free(); h->cell_class.free(); h->adj_cell.free();
     h->class_type.free(); h->adj_facet_event.free();
+    h->plane32.free(); h->node32.free(); h->proj.free();
     h->flux.free(); h->balance.free(); h->flags.free(); h->flux_partial.free();
     h->cell_volume.free(); h->cell_id.free(); h->src_cell.free(); h->src_cell_count.free();
     h->src_cell_offset.free(); h->scalars.free(); h->history.free();

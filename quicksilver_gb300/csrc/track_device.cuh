@@ -26,6 +26,19 @@ constexpr int kFacets = 24;
 constexpr int kTrackBlock = 128;      // threads per block of the tracking kernel
 constexpr int kCellPoints = 14;
 
+// Corners of the 24 triangular facets as indices into a cell's 14 points:
+// the mesh convention of the reference (MC_Domain.cc:41-46), which fixes facet
+// numbering and therefore tie-breaks.  qsg_create checks the problem's table
+// against it.
+static __constant__ int8_t kFacetLocal[kFacets][3] = {
+    {1, 3, 8}, {3, 7, 8}, {7, 5, 8}, {5, 1, 8},  {0, 4, 9},  {4, 6, 9},  {6, 2, 9},  {2, 0, 9},
+    {3, 2, 10}, {2, 6, 10}, {6, 7, 10}, {7, 3, 10}, {0, 1, 11}, {1, 5, 11}, {5, 4, 11}, {4, 0, 11},
+    {4, 5, 12}, {5, 7, 12}, {7, 6, 12}, {6, 4, 12}, {0, 2, 13}, {2, 3, 13}, {3, 1, 13}, {1, 0, 13}};
+static const int8_t kFacetLocalHost[kFacets][3] = {
+    {1, 3, 8}, {3, 7, 8}, {7, 5, 8}, {5, 1, 8},  {0, 4, 9},  {4, 6, 9},  {6, 2, 9},  {2, 0, 9},
+    {3, 2, 10}, {2, 6, 10}, {6, 7, 10}, {7, 3, 10}, {0, 1, 11}, {1, 5, 11}, {5, 4, 11}, {4, 0, 11},
+    {4, 5, 12}, {5, 7, 12}, {7, 6, 12}, {6, 4, 12}, {0, 2, 13}, {2, 3, 13}, {3, 1, 13}, {1, 0, 13}};
+
 // Structure-of-arrays particle store in device memory (136 B per particle,
 // the MC_Base_Particle fields).  `count` lives in device memory so kernels
 // can append with atomics.
@@ -57,8 +70,16 @@ struct DevTables {
     const double* planes;          // [C][24][4]
     const int32_t* adj_cell;       // [C][24]
     const uint8_t* adj_facet_event;// [C][24] facet | (event << 5)
-    int8_t facet_local[kFacets][3];
     double time_step;
+    // FP32 pre-filter of the facet search, in cell-local coordinates
+    // (origin at cell_center): plane (A, B, C, D + A cx + B cy + C cz) rounded
+    // to float, node coordinates minus the centre rounded to float, and the
+    // projection the FP64 inside test uses for each facet (u | v << 2, or
+    // 0xff when no normal component exceeds 0.5 in magnitude).
+    const float4* plane32;         // [C][24]
+    const float* node32;           // [C][14][3]
+    const uint8_t* proj;           // [C][24]
+    double abs_slack;              // bound on FP64 rounding of global-coordinate quantities
 };
 
 struct DevTally {
@@ -140,6 +161,11 @@ struct Particle {
     double num_mean_free_paths, num_segments, total_xs, mean_free_path;
     uint64_t seed, identifier;
     int32_t last_event, num_collisions, breed, species, domain, cell, facet, group;
+    // caches of values the reference recomputes every segment from unchanged
+    // inputs (same bits): |velocity| until the velocity changes, and
+    // 1/Sigma_t for the (cross-section class, group) key it was computed for
+    double speed;                  // < 0: stale
+    int32_t xs_key;                // -1: stale
 };
 
 __device__ __forceinline__ void load_particle(const DevTables& t, const DevStore& s, uint64_t i, Particle& p)
@@ -163,6 +189,8 @@ __device__ __forceinline__ void load_particle(const DevTables& t, const DevStore
     p.facet = 0;
     p.total_xs = 0.0;
     p.mean_free_path = 0.0;
+    p.speed = -1.0;
+    p.xs_key = -1;
     // direction from velocity (MC_Base_Particle.hh:317-325)
     double speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
     double factor = 1.0 / speed;
