@@ -87,17 +87,19 @@ __device__ __forceinline__ double distance_to_segment(double plane_tolerance, do
 // several times the rounding-error counts); any doubt -- a tiny dot, NaN, a
 // bound that does not separate -- answers false and the facet is evaluated
 // exactly in FP64.
-__device__ __forceinline__ bool facet_screened_out(const float4 pl, uint8_t proj, const float* n32, const int8_t* loc,
-                                                   float x, float y, float z, float a, float b, float g,
-                                                   float pos_max, float slack)
+enum ScreenResult { SCREEN_EXACT = 0, SCREEN_HUGE = 1, SCREEN_ACCEPT = 2 };
+
+__device__ __forceinline__ int facet_screen(const float4 pl, uint8_t proj, const float* n32, const int8_t* loc,
+                                            float x, float y, float z, float a, float b, float g,
+                                            float pos_max, float slack)
 {
     constexpr float u = 5.9604645e-8f;
-    if (proj == 0xff) return true;   // no dominant normal component: the FP64 test always fails
+    if (proj == 0xff) return SCREEN_HUGE;   // no dominant normal component: the FP64 test always fails
     const float s_dot = fabsf(pl.x * a) + fabsf(pl.y * b) + fabsf(pl.z * g);
     const float d = pl.x * a + pl.y * b + pl.z * g;
     const float e_d = 16.0f * u * s_dot + 1e-12f;
-    if (d < -e_d) return true;                   // FP64 dot <= 0: not a candidate
-    if (!(d > 2.0f * e_d)) return false;         // sign uncertain (or NaN): evaluate exactly
+    if (d < -e_d) return SCREEN_HUGE;            // FP64 dot <= 0: not a candidate
+    if (!(d > 2.0f * e_d)) return SCREEN_EXACT;  // sign uncertain (or NaN): evaluate exactly
     const float t_n = fabsf(pl.x * x) + fabsf(pl.y * y) + fabsf(pl.z * z) + fabsf(pl.w);
     const float n = -(pl.x * x + pl.y * y + pl.z * z + pl.w);
     const float e_n = 16.0f * u * t_n + slack;
@@ -141,7 +143,20 @@ __device__ __forceinline__ bool facet_screened_out(const float4 pl, uint8_t proj
     const float cabs = fmaxf(fabsf(cmin), fabsf(cmax));
     const float tol = 1.01e-9f * (fabsf(csum) + 3.0f * ecmax + 12.0f * u * cabs) + 1e-30f;
     const float thr = tol + ecmax;
-    return (cmin <= -thr) && (cmax >= thr);
+    if ((cmin <= -thr) && (cmax >= thr)) return SCREEN_HUGE;
+    // Proven acceptance: FP64 numerator > 0 (so the plane test of MCT.cc:303
+    // passes), the intersection lies inside the vertex range on both projected
+    // axes by more than the error bounds (bounding-box tests of MCT.cc:333-374
+    // pass), and all crosses share one sign by more than their bounds (the
+    // inside test of MCT.cc:389-393 passes).  Then the FP64 result is exactly
+    // numerator / dot.
+    const float m = e_ip + e_v + slack;
+    const float umin = fminf(vu[0], fminf(vu[1], vu[2])), umax = fmaxf(vu[0], fmaxf(vu[1], vu[2]));
+    const float vmin = fminf(vv[0], fminf(vv[1], vv[2])), vmax = fmaxf(vv[0], fmaxf(vv[1], vv[2]));
+    const bool bbox_in = (umin <= ipu - m) && (umax >= ipu + m) && (vmin <= ipv - m) && (vmax >= ipv + m);
+    const bool same_sign = (cmin > ecmax) || (cmax < -ecmax);
+    if (n > e_n && bbox_in && same_sign) return SCREEN_ACCEPT;
+    return SCREEN_EXACT;
 }
 
 // MCT_Nearest_Facet (MCT.cc:86-137) with MCT_Nearest_Facet_3D_G
@@ -171,13 +186,17 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
     for (;;) {
         const float x32 = (float)(p.x - cx), y32 = (float)(p.y - cy), z32 = (float)(p.z - cz);
         const float pos_max = fmaxf(fabsf(x32), fmaxf(fabsf(y32), fabsf(z32)));
-        uint32_t exact = 0;
+        uint32_t exact = 0, accept = 0;
 #pragma unroll 4
         for (int f = 0; f < kFacets; f++) {
-            if (!facet_screened_out(__ldg(pl32 + f), __ldg(proj + f), n32, kFacetLocal[f], x32, y32, z32, a32, b32,
-                                    g32, pos_max, slack))
-                exact |= 1u << f;
+            const int s = facet_screen(__ldg(pl32 + f), __ldg(proj + f), n32, kFacetLocal[f], x32, y32, z32, a32, b32,
+                                       g32, pos_max, slack);
+            if (s == SCREEN_EXACT) exact |= 1u << f;
+            else if (s == SCREEN_ACCEPT) accept |= 1u << f;
         }
+        // proven-accepted facets need only the reference's numerator / dot
+        // (MCT.cc:291-307, 582-585); everything else screened is _hugeDouble
+        exact |= accept;
         double best = 1e80;
         int best_f = 0;
         double neg = -kHugeDouble;
@@ -206,7 +225,9 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
         }
 #endif
         if (exact) {
-            const double plane_tolerance = 1e-16 * (p.x * p.x + p.y * p.y + p.z * p.z);
+            // (1e-8 * |r|)^2 of MCT.cc:569-571; only the full test uses it
+            const double plane_tolerance =
+                (exact & ~accept) ? 1e-16 * (p.x * p.x + p.y * p.y + p.z * p.z) : 0.0;
             uint32_t m = exact;
             while (m) {
                 const int f = __ffs(m) - 1;
@@ -215,7 +236,22 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
                 const double2 cd = __ldg(reinterpret_cast<const double2*>(planes + 4 * f + 2));
                 double d = kHugeDouble;
                 const double dot = ab.x * p.alpha + ab.y * p.beta + cd.x * p.gamma;
-                if (dot > 0.0) {
+                if ((accept >> f) & 1u) {
+                    const double numerator = -1.0 * (ab.x * p.x + ab.y * p.y + cd.x * p.z + cd.y);
+                    d = numerator / dot;
+#ifdef QSG_VERIFY_SCREEN
+                    double q0[3], q1[3], q2[3];
+                    for (int k = 0; k < 3; k++) {
+                        q0[k] = nodes[3 * kFacetLocal[f][0] + k];
+                        q1[k] = nodes[3 * kFacetLocal[f][1] + k];
+                        q2[k] = nodes[3 * kFacetLocal[f][2] + k];
+                    }
+                    const double full = (dot > 0.0) ? distance_to_segment(plane_tolerance, dot, ab.x, ab.y, cd.x, cd.y,
+                                                                          q0, q1, q2, p)
+                                                    : kHugeDouble;
+                    if (full != d) raise_flag(tally, QSG_DEV_SCREEN_MISS);
+#endif
+                } else if (dot > 0.0) {
                     double q0[3], q1[3], q2[3];
                     const double* n0 = nodes + 3 * kFacetLocal[f][0];
                     const double* n1 = nodes + 3 * kFacetLocal[f][1];
@@ -390,13 +426,14 @@ __device__ __forceinline__ bool collision_event(const DevTables& t, const DevTal
         sel = nk - 1;
     }
     const int type = t.class_reaction_type[cls * K + sel];
-    const double mass = __ldg(t.material_mass + __ldg(t.class_material + cls));
+    // 1.0 / mass of NuclearData.cc:64, divided once on the host (same bits)
+    const double inv_mass = __ldg(t.material_inv_mass + __ldg(t.class_material + cls));
     double e_out[4], a_out[4];
     int n_out = 0;
     if (type == QSG_REACT_SCATTER) {
         n_out = 1;
         double rn = rng_sample(p.seed);
-        e_out[0] = p.kinetic_energy * (1.0 - (rn * (1.0 / mass)));
+        e_out[0] = p.kinetic_energy * (1.0 - (rn * inv_mass));
         rn = rng_sample(p.seed) * 2.0 - 1.0;
         a_out[0] = rn;
     } else if (type == QSG_REACT_FISSION) {
@@ -504,7 +541,7 @@ __global__ void __launch_bounds__(BLOCK) track_kernel(DevTables t, DevTally tall
     for (int k = 0; k < LC_N; k++) cnt[k] = 0;
     const uint64_t n = *in.count;
     Particle p;
-    bool active = false, exhausted = false;
+    bool active = false, exhausted = false, pending = false;
     double* flux_row = tally.flux;
     uint64_t segs_this_history = 0;
     for (;;) {
@@ -516,7 +553,7 @@ __global__ void __launch_bounds__(BLOCK) track_kernel(DevTables t, DevTally tall
             const uint64_t i = base + g.thread_rank();
             if (i < n) {
                 load_particle(t, in, i, p);
-                if (!(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz > 0.0)) raise_flag(tally, QSG_DEV_BAD_FACET);
+                if (!(p.speed > 0.0)) raise_flag(tally, QSG_DEV_BAD_FACET);
                 // CycleTracking.cc:37-39 replica selection by particle index
                 flux_row = tally.flux + (int64_t)(i % (uint64_t)tally.flux_replicas) * t.num_cells * t.num_groups;
                 segs_this_history = 0;
@@ -526,14 +563,29 @@ __global__ void __launch_bounds__(BLOCK) track_kernel(DevTables t, DevTally tall
             }
         }
         if (__all_sync(0xffffffffu, !active)) break;
-        if (active) {
+        // Deferred collisions: a lane whose segment ends in a collision parks
+        // its particle; the warp runs the collision code (log, sincos,
+        // rotation -- most of the FP64 work) once enough lanes are parked, or
+        // when nothing else can run.  A particle's own state and random stream
+        // are untouched while it waits, so the results are unchanged.
+        const unsigned pend_mask = __ballot_sync(0xffffffffu, active && pending);
+        const unsigned run_mask = __ballot_sync(0xffffffffu, active && !pending);
+        if (pend_mask != 0u && (__popc(pend_mask) >= kCollisionBatch || run_mask == 0u)) {
+            if (pending) {
+                pending = false;
+                active = collision_event(t, tally, p, __ldg(t.cell_class + p.cell), extra, cnt);
+            }
+            continue;
+        }
+        if (active && !pending) {
             bool keep;
             const int cls = __ldg(t.cell_class + p.cell);
             int outcome = segment_outcome(t, tally, p, cls, flux_row);
             cnt[LC_SEG]++;
             p.num_segments += 1.;
             if (outcome == OUT_COLLISION) {
-                keep = collision_event(t, tally, p, cls, extra, cnt);
+                pending = true;
+                keep = true;
             } else if (outcome == OUT_FACET) {
                 // MC_Facet_Crossing_Event, MC_Facet_Crossing_Event.cc:23-70
                 const int64_t fi = (int64_t)p.cell * kFacets + p.facet;
@@ -568,6 +620,7 @@ __global__ void __launch_bounds__(BLOCK) track_kernel(DevTables t, DevTally tall
             if (keep && ++segs_this_history >= tally.max_segments) {
                 raise_flag(tally, QSG_DEV_SEGMENT_LIMIT);
                 keep = false;
+                pending = false;
             }
             active = keep;
         }
@@ -760,7 +813,8 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
         }
     }
     std::vector<double> energies(p->energies, p->energies + G + 1);
-    std::vector<double> mass(p->material_mass, p->material_mass + p->num_materials);
+    std::vector<double> mass(p->num_materials);
+    for (int m = 0; m < p->num_materials; m++) mass[m] = 1.0 / p->material_mass[m];
     int st;
     if ((st = h->energies.upload(energies)) || (st = h->sigma_total.upload(sigma_total)) ||
         (st = h->macro_xs.upload(macro)) || (st = h->class_nubar.upload(nubar)) ||
@@ -781,7 +835,7 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
     t.class_material = h->class_material.ptr;
     t.class_reaction_type = h->class_type.ptr;
     t.class_reaction_nubar = h->class_nubar.ptr;
-    t.material_mass = h->material_mass.ptr;
+    t.material_inv_mass = h->material_mass.ptr;
     t.cell_class = h->cell_class.ptr;
     t.cell_nodes = h->cell_nodes.ptr;
     t.cell_center = h->cell_center.ptr;

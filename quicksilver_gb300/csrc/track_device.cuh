@@ -24,6 +24,7 @@ constexpr double kHugeDouble = 1.0e+75;
 
 constexpr int kFacets = 24;
 constexpr int kTrackBlock = 128;      // threads per block of the tracking kernel
+constexpr int kCollisionBatch = 16;   // parked collisions that trigger a warp's collision step
 constexpr int kCellPoints = 14;
 
 // Corners of the 24 triangular facets as indices into a cell's 14 points:
@@ -63,7 +64,7 @@ struct DevTables {
     const int32_t* class_material;       // [classes]
     const int8_t* class_reaction_type;   // [classes][K]
     const double* class_reaction_nubar;  // [classes][K]
-    const double* material_mass;         // [materials]
+    const double* material_inv_mass;     // [materials] 1.0 / MaterialDatabase mass
     const int32_t* cell_class;     // [C]
     const double* cell_nodes;      // [C][14][3]
     const double* cell_center;     // [C][3] MCT_Cell_Position_3D_G
@@ -189,10 +190,11 @@ __device__ __forceinline__ void load_particle(const DevTables& t, const DevStore
     p.facet = 0;
     p.total_xs = 0.0;
     p.mean_free_path = 0.0;
-    p.speed = -1.0;
     p.xs_key = -1;
     // direction from velocity (MC_Base_Particle.hh:317-325)
+    // MC_Vector::Length(), the same value MC_Segment_Outcome computes next
     double speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
+    p.speed = speed;
     double factor = 1.0 / speed;
     p.alpha = factor * p.vx;
     p.beta = factor * p.vy;
