@@ -13,9 +13,10 @@ import numpy as np
 
 import os
 
-# QSG_LIB=verify selects the screen-verification build (libqsg_verify.so)
-LIB_PATH = Path(__file__).resolve().parent / "lib" / (
-    "libqsg_verify.so" if os.environ.get("QSG_LIB") == "verify" else "libqsg.so")
+# QSG_LIB=<name> loads lib/libqsg_<name>.so instead of lib/libqsg.so, e.g.
+# QSG_LIB=verify for the screen-verification build (build.py --verify-screen)
+_variant = os.environ.get("QSG_LIB", "")
+LIB_PATH = Path(__file__).resolve().parent / "lib" / (f"libqsg_{_variant}.so" if _variant else "libqsg.so")
 
 QSG_OK = 0
 QSG_ERR_INVALID = 1

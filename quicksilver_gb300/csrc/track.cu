@@ -533,7 +533,8 @@ __device__ __forceinline__ void flush_counters(const DevTally& tally, uint32_t* 
 // long histories do not hold idle lanes; the warp leaves when every lane has
 // finished and the queue is empty.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) track_kernel(DevTables t, DevTally tally, DevStore in, DevStore census,
+__global__ void __launch_bounds__(BLOCK, kTrackMinBlocks) track_kernel(DevTables t, DevTally tally, DevStore in,
+                                                                       DevStore census,
                                                       DevStore extra, unsigned long long* cursor)
 {
     uint32_t cnt[LC_N];

@@ -23,8 +23,16 @@ constexpr double kSmallDouble = 1.0e-10;
 constexpr double kHugeDouble = 1.0e+75;
 
 constexpr int kFacets = 24;
-constexpr int kTrackBlock = 128;      // threads per block of the tracking kernel
-constexpr int kCollisionBatch = 16;   // parked collisions that trigger a warp's collision step
+// Tracking-kernel shape (tuned on GB300; QSG_* macros override for sweeps)
+#ifndef QSG_MIN_BLOCKS
+#define QSG_MIN_BLOCKS 3
+#endif
+#ifndef QSG_COLLISION_BATCH
+#define QSG_COLLISION_BATCH 16
+#endif
+constexpr int kTrackBlock = 128;                       // threads per block
+constexpr int kTrackMinBlocks = QSG_MIN_BLOCKS;        // resident blocks per SM the registers must allow
+constexpr int kCollisionBatch = QSG_COLLISION_BATCH;   // parked collisions that trigger a warp's collision step
 constexpr int kCellPoints = 14;
 
 // Corners of the 24 triangular facets as indices into a cell's 14 points:
