@@ -150,7 +150,7 @@ typedef struct QsgOptions {
     uint64_t particle_capacity;  /* per store (0 = grow on demand)             */
     uint64_t max_segments;       /* per history per launch guard (0 = 2^40)    */
     int32_t max_passes;          /* fission passes per asynchronous cycle (0 = 8) */
-    int32_t reserved;
+    int32_t collision_batch;     /* parked collisions per warp collision step (0 = 16) */
 } QsgOptions;
 
 typedef struct QsgHandle QsgHandle;
@@ -236,6 +236,32 @@ int qsg_cycle_finalize(QsgHandle* h, void* stream);
 int qsg_cycle_history(QsgHandle* h, uint64_t first, uint64_t n, uint64_t* balance, double* flux_total);
 /* Copy the processing store (e.g. after qsg_cycle_init) to host arrays. */
 int qsg_get_processing(QsgHandle* h, QsgParticleSoA* host, uint64_t cap, uint64_t* n_out);
+
+/* ---- batches of independent problems ------------------------------------ */
+/* One handle over n independent problems (each a single domain; they must
+ * share the energy grid, the time step and the facet convention).  Every
+ * kernel covers all of them at once; counters and flux stay per problem.
+ * Tracking the batch gives each problem exactly what tracking it alone gives
+ * (Quicksilver has no such mode: it runs one problem per process). */
+int qsg_batch_create(const QsgProblem* problems, int32_t n_problems, const QsgOptions* options, QsgHandle** out);
+/* Number of problems and, when cell_offsets is not NULL, the [n+1] offsets of
+ * each problem's cells in the handle's flux array. */
+int qsg_num_problems(QsgHandle* h, int32_t* n_problems, int32_t* cell_offsets);
+/* Per-problem cycle constants (configs[n_problems]); seed_offsets (may be
+ * NULL = all 0, the reference's seeding) is added to each problem's source
+ * seeds so that problems with identical meshes get distinct streams.
+ * qsg_cycle_history then returns [n][n_problems][13] counters and
+ * [n][n_problems] flux totals. */
+int qsg_configure_cycle_batch(QsgHandle* h, const QsgCycleConfig* configs, const uint64_t* seed_offsets);
+/* n whole cycles (init, QsgOptions::max_passes tracking passes, finalize)
+ * enqueued on `stream` without host synchronisation; with use_graph each
+ * cycle is replayed from a CUDA graph captured on first use (one per role
+ * permutation of the three particle stores). */
+int qsg_run_cycles(QsgHandle* h, int32_t n_cycles, int32_t use_graph, void* stream);
+/* Kernel-shape knobs picked by the autotuner: threads per block of the
+ * tracking kernel (128 or 256), collisions batched per warp step (1-32),
+ * particles claimed per work-queue atomic (1-1024); 0 keeps a value. */
+int qsg_set_tuning(QsgHandle* h, int32_t block_size, int32_t collision_batch, int32_t queue_chunk);
 
 /* Device pointers of the stores, for zero-copy callers (e.g. torch). */
 int qsg_processing_view(QsgHandle* h, QsgParticleSoA* device_view, uint64_t* n);

@@ -72,7 +72,7 @@ class QsgParticleSoA(C.Structure):
 class QsgOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("block_size", C.c_int32), ("flux_replicas", C.c_int32),
                 ("balance_replicas", C.c_int32), ("particle_capacity", C.c_uint64),
-                ("max_segments", C.c_uint64), ("max_passes", C.c_int32), ("reserved", C.c_int32)]
+                ("max_segments", C.c_uint64), ("max_passes", C.c_int32), ("collision_batch", C.c_int32)]
 
 
 class QsgSimulation(C.Structure):
@@ -116,6 +116,11 @@ _SIGNATURES = {
     "qsg_reset_tallies": ([_VP], C.c_int),
     "qsg_device_status": ([_VP, C.POINTER(C.c_uint32), C.c_int], C.c_int),
     "qsg_configure_cycle": ([_VP, C.POINTER(QsgCycleConfig)], C.c_int),
+    "qsg_configure_cycle_batch": ([_VP, C.POINTER(QsgCycleConfig), _up], C.c_int),
+    "qsg_batch_create": ([C.POINTER(QsgProblem), C.c_int32, C.POINTER(QsgOptions), C.POINTER(_VP)], C.c_int),
+    "qsg_num_problems": ([_VP, C.POINTER(C.c_int32), _ip], C.c_int),
+    "qsg_set_tuning": ([_VP, C.c_int32, C.c_int32, C.c_int32], C.c_int),
+    "qsg_run_cycles": ([_VP, C.c_int32, C.c_int32, _VP], C.c_int),
     "qsg_cycle_init": ([_VP, _VP], C.c_int),
     "qsg_cycle_finalize": ([_VP, _VP], C.c_int),
     "qsg_cycle_history": ([_VP, C.c_uint64, C.c_uint64, _up, _dp], C.c_int),

@@ -22,7 +22,7 @@ OBJ = OUT / "obj"
 INCLUDE = ROOT / "include"
 LIB = OUT / "libqsg.so"
 
-HOST_SOURCES = ["host/status.cc", "host/deck.cc", "host/problem.cc"]
+HOST_SOURCES = ["host/status.cc", "host/deck.cc", "host/problem.cc", "host/batch.cc"]
 CUDA_SOURCES = ["track.cu", "cycle.cu"]
 
 NVCC_ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1,5 +1,5 @@
 // Device-side cycle set-up and finalisation, so that a whole cycle runs on the
-// GPU without host round trips (and can be captured in a CUDA graph):
+// GPU without host round trips and can be captured in a CUDA graph:
 //
 //   qsg_cycle_init      cycleInit (main.cc:96-121): the previous census becomes
 //                       the processing store (swapProcessingProcessedVaults,
@@ -8,19 +8,24 @@
 //                       (PopulationControl.cc:20-122) and
 //                       RouletteLowWeightParticles (PopulationControl.cc:127-171)
 //   qsg_cycle_finalize  cycleFinalize (main.cc:310-324) with the replica sum and
-//                       reset of Tallies::CycleFinalize (Tallies.cc:25-98); the
-//                       cycle's 13 counters and scalar-flux total
+//                       reset of Tallies::CycleFinalize (Tallies.cc:25-98); each
+//                       problem's 13 counters and scalar-flux total
 //                       (Tallies::ScalarFluxSum, Tallies.cc:146-171) go to a
 //                       device-resident history.
+//   qsg_run_cycles      init + tracking passes + finalize for n cycles, each
+//                       cycle replayed from a captured CUDA graph.
 //
-// Everything that is constant over the run is computed once on the host at
-// qsg_configure_cycle: the source particle weight and the per-cell source
-// counts depend only on cell volumes, source rates, dt and nParticles.
-// Each source particle, split and roulette decision draws only from its own
-// random stream, so the set of particles a cycle produces does not depend on
-// the order the device produces them in.
+// Everything here is per problem, so one handle can hold a batch of
+// independent problems (qsg_batch_create); a single problem is a batch of one.
+// What is constant over the run is computed once on the host at
+// qsg_configure_cycle_batch: a problem's source particle weight and per-cell
+// source counts depend only on its cell volumes, source rates, dt and
+// nParticles.  Each source particle, split and roulette decision draws only
+// from its own random stream, so the set of particles a cycle produces does
+// not depend on the order the device produces them in.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -34,35 +39,73 @@ namespace qsg {
 namespace {
 
 constexpr int kInitBlock = 256;
-constexpr int kFluxPartials = 1024;   // fixed shape, so the flux total is reproducible
+constexpr int kFluxPartials = 256;   // blocks per problem for the flux total (fixed shape: reproducible)
 
-// Census -> processing bookkeeping, START / SOURCE counters.
-__global__ void cycle_begin_kernel(CycleScalars* sc, unsigned long long* processing_count,
-                                   unsigned long long* processed_count, unsigned long long* balance,
-                                   unsigned long long n_source)
+struct CycleArgs {
+    CycleScalars* sc;
+    unsigned long long* balance;       // [replicas][P][13]
+    unsigned int* flags;
+    const int32_t* cell_problem;       // null: one problem
+    int32_t num_problems;
+    // per problem
+    const double* weight;              // source particle weight
+    const double* e_min;
+    const double* e_max;
+    const double* low_cut;             // lowWeightCutoff
+    const uint64_t* target;            // nParticles
+    const uint64_t* n_source;
+    const uint64_t* seed_offset;
+    const int32_t* load_balance;
+    unsigned long long* carry;         // census count carried into the cycle
+    double* factor;                    // population-control factor of the running cycle
+};
+
+__device__ __forceinline__ int problem_of(const CycleArgs& a, int cell)
 {
-    const unsigned long long start = *processing_count;
-    sc->start = start;
-    sc->source_round = sc->source_calls;
-    sc->source_calls += 1;
-    balance[QSG_BAL_START] = start;            // main.cc:110 sets _start after the swap
-    balance[QSG_BAL_SOURCE] += n_source;
-    *processing_count = start + n_source;
-    *processed_count = 0;
+    return a.cell_problem ? __ldg(a.cell_problem + cell) : 0;
+}
+
+// Census -> processing bookkeeping; START / SOURCE counters and the
+// population-control factor of every problem (PopulationControl.cc:24-58).
+__global__ void cycle_begin_kernel(CycleArgs a, unsigned long long* processing_count,
+                                   unsigned long long* processed_count, unsigned long long n_source_total)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const unsigned long long start = *processing_count;
+        a.sc->start = start;
+        a.sc->source_round = a.sc->source_calls;
+        a.sc->source_calls += 1;
+        *processing_count = start + n_source_total;
+        *processed_count = 0;
+    }
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.num_problems; p += gridDim.x * blockDim.x) {
+        const unsigned long long start = a.carry[p];
+        unsigned long long* bal = a.balance + (int64_t)p * QSG_BAL_COUNT;
+        bal[QSG_BAL_START] = start;                 // main.cc:110 sets _start after the swap
+        bal[QSG_BAL_SOURCE] += a.n_source[p];
+        const unsigned long long current = start + a.n_source[p];
+        double f;
+        if (a.load_balance[p]) {
+            const double target = ceil((double)a.target[p] / (double)1);
+            const int cur = (int)current;
+            f = (cur != 0) ? target / (double)cur : 1.0;
+        } else {
+            f = (double)a.target[p] / (double)current;
+        }
+        a.factor[p] = f;
+    }
 }
 
 struct SourceArgs {
     DevTables t;
     DevStore out;
-    const CycleScalars* sc;
+    CycleArgs c;
     const int32_t* src_cell;
     const uint64_t* src_cell_offset;
     const int32_t* src_cell_count;
     const uint64_t* cell_id;
     const double* cell_volume;
-    unsigned int* flags;
     uint64_t n_source;
-    double e_min, e_max, weight;
 };
 
 // MCT_Cell_Volume_3D_G_vector_tetDet, MCT.cc:633-648: 6x the signed tet volume.
@@ -83,10 +126,12 @@ __global__ void __launch_bounds__(kInitBlock) source_kernel(SourceArgs a)
     if (t >= a.n_source) return;
     const DevTables& tb = a.t;
     const int cell = a.src_cell[t];
+    const int prob = problem_of(a.c, cell);
     const uint64_t k = t - a.src_cell_offset[cell];
     // the cell's source tally counts every particle it ever sourced
-    uint64_t seed0 = a.sc->source_round * (uint64_t)a.src_cell_count[cell] + k;
-    seed0 += a.cell_id[cell];
+    // (MC_SourceNow.cc:90-93); the offset is 0 unless a batch asks otherwise
+    uint64_t seed0 = a.c.sc->source_round * (uint64_t)a.src_cell_count[cell] + k;
+    seed0 += a.cell_id[cell] + a.c.seed_offset[prob];
     Particle p;
     p.seed = rng_spawn(seed0);
     p.identifier = seed0;
@@ -137,7 +182,7 @@ __global__ void __launch_bounds__(kInitBlock) source_kernel(SourceArgs a)
     p.alpha = sine_gamma * cos(phi);
     p.beta = sine_gamma * sin(phi);
     // energy uniform in [eMin, eMax]; Get_Speed_From_Energy (MC_SourceNow.cc:169-177)
-    p.kinetic_energy = (a.e_max - a.e_min) * rng_sample(p.seed) + a.e_min;
+    p.kinetic_energy = (a.c.e_max[prob] - a.c.e_min[prob]) * rng_sample(p.seed) + a.c.e_min[prob];
     const double m = kNeutronRestMassEnergy;
     const double E = p.kinetic_energy;
     double speed = kSpeedOfLight * sqrt(E * (E + 2.0 * (m)) / ((E + m) * (E + m)));
@@ -146,7 +191,7 @@ __global__ void __launch_bounds__(kInitBlock) source_kernel(SourceArgs a)
     p.vz = speed * p.gamma;
     p.domain = 0;
     p.cell = cell;
-    p.weight = a.weight;
+    p.weight = a.c.weight[prob];
     p.num_mean_free_paths = -1.0 * log(rng_sample(p.seed));
     p.time_to_census = tb.time_step * rng_sample(p.seed);
     p.age = 0.0;
@@ -155,20 +200,10 @@ __global__ void __launch_bounds__(kInitBlock) source_kernel(SourceArgs a)
     p.num_collisions = 0;
     p.breed = 0;
     p.species = 0;
-    const uint64_t slot = a.sc->start + t;
+    const uint64_t slot = a.c.sc->start + t;
     if (slot < a.out.capacity) store_particle(a.out, slot, p);
-    else atomicOr(a.flags, QSG_DEV_STORE_OVERFLOW);
+    else atomicOr(a.c.flags, QSG_DEV_STORE_OVERFLOW);
 }
-
-struct PopArgs {
-    DevStore in, out;
-    unsigned long long* balance;
-    unsigned int* flags;
-    uint64_t n_target;
-    double weight_cutoff;       // lowWeightCutoff * source particle weight
-    double low_weight_cutoff;
-    int32_t load_balance;
-};
 
 __device__ __forceinline__ void load_record(const DevStore& s, uint64_t i, Particle& p)
 {
@@ -192,13 +227,13 @@ __device__ __forceinline__ void load_record(const DevStore& s, uint64_t i, Parti
 
 // RouletteLowWeightParticles' per-particle body (PopulationControl.cc:153-167);
 // returns whether the particle survives.
-__device__ __forceinline__ bool roulette(const PopArgs& a, Particle& p, uint32_t& rr)
+__device__ __forceinline__ bool roulette(double low_cut, double weight_cutoff, Particle& p, uint32_t& rr)
 {
-    if (!(a.low_weight_cutoff > 0.0)) return true;
-    if (p.weight <= a.weight_cutoff) {
+    if (!(low_cut > 0.0)) return true;
+    if (p.weight <= weight_cutoff) {
         double r = rng_sample(p.seed);
-        if (r <= a.low_weight_cutoff) {
-            p.weight /= a.low_weight_cutoff;
+        if (r <= low_cut) {
+            p.weight /= low_cut;
         } else {
             rr++;
             return false;
@@ -207,33 +242,33 @@ __device__ __forceinline__ bool roulette(const PopArgs& a, Particle& p, uint32_t
     return true;
 }
 
-__device__ __forceinline__ void emit(const PopArgs& a, const Particle& p)
+__device__ __forceinline__ void emit(const DevStore& out, unsigned int* flags, const Particle& p)
 {
-    uint64_t slot = append_slot(a.out);
-    if (slot < a.out.capacity) store_particle(a.out, slot, p);
-    else atomicOr(a.flags, QSG_DEV_STORE_OVERFLOW);
+    uint64_t slot = append_slot(out);
+    if (slot < out.capacity) store_particle(out, slot, p);
+    else atomicOr(flags, QSG_DEV_STORE_OVERFLOW);
 }
 
 // PopulationControlGuts (PopulationControl.cc:71-122) followed by the low-weight
 // roulette, fused: every particle of `in` is visited once; survivors and split
-// copies are appended to `out`.
-__global__ void __launch_bounds__(kInitBlock) population_kernel(PopArgs a)
+// copies are appended to `out`.  RR / SPLIT counts per problem gather in shared
+// memory (when the batch fits) before one global add per block.
+__global__ void __launch_bounds__(kInitBlock) population_kernel(CycleArgs a, DevStore in, DevStore out)
 {
-    __shared__ unsigned long long red[2];
-    if (threadIdx.x < 2) red[threadIdx.x] = 0;
+    extern __shared__ unsigned long long s_rr[];   // [P][2] when P <= kSmemProblems
+    const bool use_smem = a.num_problems <= kSmemProblems;
+    if (use_smem)
+        for (int k = threadIdx.x; k < 2 * a.num_problems; k += kInitBlock) s_rr[k] = 0;
     __syncthreads();
-    const uint64_t n = *a.in.count;
-    double factor;
-    if (a.load_balance) {
-        int current = (int)n;
-        factor = (current != 0) ? (double)a.n_target / (double)current : 1.0;
-    } else {
-        factor = (double)a.n_target / (double)n;
-    }
-    uint32_t rr = 0, split_count = 0;
+    const uint64_t n = *in.count;
     for (uint64_t i = (uint64_t)blockIdx.x * kInitBlock + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kInitBlock) {
         Particle p;
-        load_record(a.in, i, p);
+        load_record(in, i, p);
+        const int prob = problem_of(a, p.cell);
+        const double factor = a.factor[prob];
+        const double low_cut = a.low_cut[prob];
+        const double weight_cutoff = low_cut * a.weight[prob];   // PopulationControl.cc:142-143
+        uint32_t rr = 0, split_count = 0;
         bool survive = true;
         if (factor != 1.0) {
             double r = rng_sample(p.seed);
@@ -254,61 +289,175 @@ __global__ void __launch_bounds__(kInitBlock) population_kernel(PopArgs a)
                     child.seed = rng_spawn(p.seed);
                     child.identifier = child.seed;
                     Particle c2 = child;
-                    if (roulette(a, c2, rr)) emit(a, c2);
+                    if (roulette(low_cut, weight_cutoff, c2, rr)) emit(out, a.flags, c2);
                 }
             }
         }
-        if (survive && roulette(a, p, rr)) emit(a, p);
+        if (survive && roulette(low_cut, weight_cutoff, p, rr)) emit(out, a.flags, p);
+        if (rr | split_count) {
+            if (use_smem) {
+                if (rr) atomicAdd(&s_rr[2 * prob], (unsigned long long)rr);
+                if (split_count) atomicAdd(&s_rr[2 * prob + 1], (unsigned long long)split_count);
+            } else {
+                if (rr) atomicAdd(a.balance + (int64_t)prob * QSG_BAL_COUNT + QSG_BAL_RR, (unsigned long long)rr);
+                if (split_count)
+                    atomicAdd(a.balance + (int64_t)prob * QSG_BAL_COUNT + QSG_BAL_SPLIT,
+                              (unsigned long long)split_count);
+            }
+        }
     }
-    if (rr) atomicAdd(&red[0], (unsigned long long)rr);
-    if (split_count) atomicAdd(&red[1], (unsigned long long)split_count);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        if (red[0]) atomicAdd(a.balance + QSG_BAL_RR, red[0]);
-        if (red[1]) atomicAdd(a.balance + QSG_BAL_SPLIT, red[1]);
+    if (use_smem) {
+        __syncthreads();
+        for (int k = threadIdx.x; k < 2 * a.num_problems; k += kInitBlock) {
+            const unsigned long long v = s_rr[k];
+            if (v) atomicAdd(a.balance + (int64_t)(k / 2) * QSG_BAL_COUNT + ((k & 1) ? QSG_BAL_SPLIT : QSG_BAL_RR), v);
+        }
     }
 }
 
-// Fixed-shape partial sums of the flux array (all replicas).
-__global__ void __launch_bounds__(256) flux_partial_kernel(const double* flux, uint64_t n, double* partial)
+// Fixed-shape partial sums of each problem's flux range (all replicas):
+// block (b, p) sums chunk b of problem p.
+__global__ void __launch_bounds__(256) flux_partial_kernel(const double* flux, const int32_t* cell_offset,
+                                                           int groups, int replicas, int64_t replica_stride,
+                                                           double* partial)
 {
     __shared__ double s[256];
+    const int prob = blockIdx.y;
+    const uint64_t lo_all = (uint64_t)cell_offset[prob] * groups, hi_all = (uint64_t)cell_offset[prob + 1] * groups;
+    const uint64_t n = hi_all - lo_all;
     const uint64_t chunk = (n + gridDim.x - 1) / gridDim.x;
-    const uint64_t lo = (uint64_t)blockIdx.x * chunk;
-    const uint64_t hi = lo + chunk < n ? lo + chunk : n;
+    const uint64_t lo = lo_all + (uint64_t)blockIdx.x * chunk;
+    const uint64_t hi = min(lo + chunk, hi_all);
     double acc = 0.0;
-    for (uint64_t i = lo + threadIdx.x; i < hi; i += 256) acc += flux[i];
+    for (int r = 0; r < replicas; r++)
+        for (uint64_t i = lo + threadIdx.x; i < hi; i += 256) acc += flux[r * replica_stride + i];
     s[threadIdx.x] = acc;
     __syncthreads();
     for (int w = 128; w > 0; w >>= 1) {
         if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = s[0];
+    if (threadIdx.x == 0) partial[(int64_t)prob * gridDim.x + blockIdx.x] = s[0];
 }
 
-// Record the cycle: counters summed over replicas, END = census count, the
-// flux total; then clear the counters (flux is cleared by a memset after).
-__global__ void cycle_finalize_kernel(CycleScalars* sc, unsigned long long* balance, int replicas,
-                                      const unsigned long long* processed_count, const double* partial,
-                                      int n_partial, CycleRecord* history)
+// Block p records problem p's cycle: counters summed over replicas, END = its
+// census count (main.cc:314), the flux total; carries the census count into
+// the next cycle and clears the counters.
+__global__ void cycle_finalize_kernel(CycleArgs a, int replicas, const double* partial, int n_partial,
+                                      CycleRecord* history)
 {
-    CycleRecord* rec = history + sc->cycle;
+    const int prob = blockIdx.x;
+    CycleRecord* rec = history + a.sc->cycle * (uint64_t)a.num_problems + prob;
     if (threadIdx.x < QSG_BAL_COUNT) {
         unsigned long long s = 0;
-        for (int r = 0; r < replicas; r++) s += balance[r * QSG_BAL_COUNT + threadIdx.x];
-        if (threadIdx.x == QSG_BAL_END) s = *processed_count;   // main.cc:314
+        for (int r = 0; r < replicas; r++)
+            s += a.balance[((int64_t)r * a.num_problems + prob) * QSG_BAL_COUNT + threadIdx.x];
         rec->balance[threadIdx.x] = s;
     }
+    __syncthreads();
     if (threadIdx.x == 0) {
+        rec->balance[QSG_BAL_END] = rec->balance[QSG_BAL_CENSUS];
+        a.carry[prob] = rec->balance[QSG_BAL_CENSUS];
         double total = 0.0;
-        for (int k = 0; k < n_partial; k++) total += partial[k];
+        for (int k = 0; k < n_partial; k++) total += partial[(int64_t)prob * n_partial + k];
         rec->flux_total = total;
     }
-    __syncthreads();
-    for (int k = threadIdx.x; k < replicas * QSG_BAL_COUNT; k += blockDim.x) balance[k] = 0;
-    __syncthreads();
-    if (threadIdx.x == 0) sc->cycle += 1;
+    for (int k = threadIdx.x; k < replicas * QSG_BAL_COUNT; k += blockDim.x)
+        a.balance[((int64_t)(k / QSG_BAL_COUNT) * a.num_problems + prob) * QSG_BAL_COUNT + k % QSG_BAL_COUNT] = 0;
+}
+
+__global__ void cycle_advance_kernel(CycleScalars* sc) { sc->cycle += 1; }
+
+CycleArgs cycle_args(QsgHandle* h)
+{
+    CycleArgs a;
+    a.sc = h->scalars.ptr;
+    a.balance = h->balance.ptr;
+    a.flags = h->flags.ptr;
+    a.cell_problem = h->num_problems > 1 ? h->cell_problem.ptr : nullptr;
+    a.num_problems = h->num_problems;
+    a.weight = h->prob_weight.ptr;
+    a.e_min = h->prob_emin.ptr;
+    a.e_max = h->prob_emax.ptr;
+    a.low_cut = h->prob_lowcut.ptr;
+    a.target = h->prob_target.ptr;
+    a.n_source = h->prob_nsource.ptr;
+    a.seed_offset = h->prob_seed_offset.ptr;
+    a.load_balance = h->prob_load_balance.ptr;
+    a.carry = h->prob_carry.ptr;
+    a.factor = h->prob_factor.ptr;
+    return a;
+}
+
+// Host-side preparation that may allocate (and therefore synchronise); never
+// called while a stream is being captured.
+int cycle_prepare(QsgHandle* h)
+{
+    int st;
+    const uint64_t need = h->known_census + h->n_source;
+    if ((st = h->processed.reserve(need)) || (st = h->extra.reserve(std::max<uint64_t>(need, 2 * h->n_target))))
+        return st;
+    if (h->cycles_finalized >= h->history_capacity) {
+        DevBuf<CycleRecord> bigger;
+        const uint64_t cap = 2 * h->history_capacity;
+        if ((st = bigger.alloc(cap * h->num_problems))) return st;
+        QSG_CUDA(cudaDeviceSynchronize());
+        QSG_CUDA(cudaMemcpy(bigger.ptr, h->history.ptr, h->history_capacity * h->num_problems * sizeof(CycleRecord),
+                            cudaMemcpyDeviceToDevice));
+        h->history.free();
+        h->history = bigger;
+        bigger.ptr = nullptr;
+        h->history_capacity = cap;
+    }
+    return QSG_OK;
+}
+
+int cycle_init_enqueue(QsgHandle* h, cudaStream_t s)
+{
+    std::swap(h->processing, h->processed);
+    CycleArgs ca = cycle_args(h);
+    cycle_begin_kernel<<<1, 256, 0, s>>>(ca, h->processing.count, h->processed.count,
+                                         (unsigned long long)h->n_source);
+    QSG_CUDA(cudaGetLastError());
+    if (h->n_source) {
+        SourceArgs a;
+        a.t = h->tables;
+        a.out = h->processing.view;
+        a.c = ca;
+        a.src_cell = h->src_cell.ptr;
+        a.src_cell_offset = h->src_cell_offset.ptr;
+        a.src_cell_count = h->src_cell_count.ptr;
+        a.cell_id = h->cell_id.ptr;
+        a.cell_volume = h->cell_volume.ptr;
+        a.n_source = h->n_source;
+        unsigned blocks = (unsigned)((h->n_source + kInitBlock - 1) / kInitBlock);
+        source_kernel<<<blocks, kInitBlock, 0, s>>>(a);
+        QSG_CUDA(cudaGetLastError());
+    }
+    QSG_CUDA(cudaMemsetAsync(h->extra.count, 0, sizeof(unsigned long long), s));
+    const size_t smem = h->num_problems <= kSmemProblems ? 2 * h->num_problems * sizeof(unsigned long long) : 0;
+    population_kernel<<<h->num_sms * 8, kInitBlock, smem, s>>>(ca, h->processing.view, h->extra.view);
+    QSG_CUDA(cudaGetLastError());
+    std::swap(h->processing, h->extra);
+    h->processing_on_device = true;
+    return QSG_OK;
+}
+
+int cycle_finalize_enqueue(QsgHandle* h, cudaStream_t s)
+{
+    CycleArgs ca = cycle_args(h);
+    const int64_t stride = (int64_t)h->num_cells * h->num_groups;
+    flux_partial_kernel<<<dim3(kFluxPartials, h->num_problems), 256, 0, s>>>(
+        h->flux.ptr, h->prob_cell_offset.ptr, h->num_groups, h->flux_replicas, stride, h->flux_partial.ptr);
+    QSG_CUDA(cudaGetLastError());
+    cycle_finalize_kernel<<<h->num_problems, 64, 0, s>>>(ca, h->balance_replicas, h->flux_partial.ptr, kFluxPartials,
+                                                         h->history.ptr);
+    QSG_CUDA(cudaGetLastError());
+    cycle_advance_kernel<<<1, 1, 0, s>>>(h->scalars.ptr);
+    QSG_CUDA(cudaGetLastError());
+    QSG_CUDA(cudaMemsetAsync(h->flux.ptr, 0, (size_t)h->flux_replicas * stride * sizeof(double), s));
+    h->cycles_finalized++;
+    return QSG_OK;
 }
 
 }  // namespace
@@ -316,60 +465,100 @@ __global__ void cycle_finalize_kernel(CycleScalars* sc, unsigned long long* bala
 
 using namespace qsg;
 
-extern "C" int qsg_configure_cycle(QsgHandle* h, const QsgCycleConfig* cfg)
+extern "C" int qsg_configure_cycle_batch(QsgHandle* h, const QsgCycleConfig* cfgs, const uint64_t* seed_offsets)
 {
     QSG_API_BEGIN
-    if (!h || !cfg || !cfg->source_rate) return fail(QSG_ERR_INVALID, "qsg_configure_cycle: null argument");
+    if (!h || !cfgs) return fail(QSG_ERR_INVALID, "qsg_configure_cycle: null argument");
+    const int P = h->num_problems;
     if ((int64_t)h->h_cell_volume.size() != h->num_cells || (int64_t)h->h_cell_id.size() != h->num_cells)
         return fail(QSG_ERR_INVALID, "qsg_configure_cycle: the problem given to qsg_create had no cell_volume / cell_id");
-    if (cfg->n_particles == 0) return fail(QSG_ERR_INVALID, "qsg_configure_cycle: n_particles must be positive");
+    for (int p = 0; p < P; p++) {
+        if (!cfgs[p].source_rate) return fail(QSG_ERR_INVALID, "qsg_configure_cycle: problem %d has no source rates", p);
+        if (cfgs[p].n_particles == 0)
+            return fail(QSG_ERR_INVALID, "qsg_configure_cycle: problem %d needs n_particles > 0", p);
+    }
     int st = set_device(h);
     if (st) return st;
     const int64_t C = h->num_cells;
     const double dt = h->tables.time_step;
-    // MC_SourceNow.cc:35-64: total source weight in cell order, particle weight
-    double total_weight = 0;
-    for (int64_t c = 0; c < C; c++) total_weight += h->h_cell_volume[c] * cfg->source_rate[h->h_cell_material[c]] * dt;
-    double source_fraction = 0.1;
-    double spw = total_weight / (source_fraction * cfg->n_particles);
-    std::vector<int32_t> count(C);
+    std::vector<double> weight(P), emin(P), emax(P), lowcut(P);
+    std::vector<uint64_t> target(P), nsrc(P), seedoff(P);
+    std::vector<int32_t> lb(P), count(C), cell_off(P + 1);
     std::vector<uint64_t> offset(C);
     uint64_t n_source = 0;
-    for (int64_t c = 0; c < C; c++) {
-        double cell_weight = h->h_cell_volume[c] * cfg->source_rate[h->h_cell_material[c]] * dt;
-        double cell_num_float = cell_weight / spw;
-        int n = (int)cell_num_float;
-        if (n < 0) n = 0;
-        count[c] = n;
-        offset[c] = n_source;
-        n_source += (uint64_t)n;
+    for (int p = 0; p < P; p++) {
+        const QsgCycleConfig& cf = cfgs[p];
+        const int32_t c0 = h->h_problem_cell_offset[p], c1 = h->h_problem_cell_offset[p + 1];
+        const int32_t m0 = h->h_problem_material_offset[p];
+        cell_off[p] = c0;
+        // MC_SourceNow.cc:35-64: total source weight in cell order, particle weight
+        double total_weight = 0;
+        for (int64_t c = c0; c < c1; c++)
+            total_weight += h->h_cell_volume[c] * cf.source_rate[h->h_cell_material[c] - m0] * dt;
+        double source_fraction = 0.1;
+        double spw = total_weight / (source_fraction * cf.n_particles);
+        uint64_t ns = 0;
+        for (int64_t c = c0; c < c1; c++) {
+            double cell_weight = h->h_cell_volume[c] * cf.source_rate[h->h_cell_material[c] - m0] * dt;
+            double cell_num_float = cell_weight / spw;
+            int n = (int)cell_num_float;
+            if (n < 0) n = 0;
+            count[c] = n;
+            offset[c] = n_source;
+            n_source += (uint64_t)n;
+            ns += (uint64_t)n;
+        }
+        weight[p] = spw;
+        emin[p] = cf.e_min;
+        emax[p] = cf.e_max;
+        lowcut[p] = cf.low_weight_cutoff;
+        target[p] = cf.n_particles;
+        nsrc[p] = ns;
+        seedoff[p] = seed_offsets ? seed_offsets[p] : 0;
+        lb[p] = cf.load_balance;
     }
+    cell_off[P] = (int32_t)C;
     std::vector<int32_t> src_cell(n_source);
     for (int64_t c = 0; c < C; c++)
         for (int32_t k = 0; k < count[c]; k++) src_cell[offset[c] + k] = (int32_t)c;
     std::vector<double> vol(h->h_cell_volume.begin(), h->h_cell_volume.end());
     std::vector<uint64_t> ids(h->h_cell_id.begin(), h->h_cell_id.end());
+    std::vector<unsigned long long> carry(P, 0);
+    std::vector<double> factor(P, 1.0);
     if ((st = h->src_cell.upload(src_cell)) || (st = h->src_cell_count.upload(count)) ||
-        (st = h->src_cell_offset.upload(offset)) || (st = h->cell_volume.upload(vol)) || (st = h->cell_id.upload(ids)))
+        (st = h->src_cell_offset.upload(offset)) || (st = h->cell_volume.upload(vol)) ||
+        (st = h->cell_id.upload(ids)) || (st = h->prob_weight.upload(weight)) || (st = h->prob_emin.upload(emin)) ||
+        (st = h->prob_emax.upload(emax)) || (st = h->prob_lowcut.upload(lowcut)) ||
+        (st = h->prob_target.upload(target)) || (st = h->prob_nsource.upload(nsrc)) ||
+        (st = h->prob_seed_offset.upload(seedoff)) || (st = h->prob_load_balance.upload(lb)) ||
+        (st = h->prob_carry.upload(carry)) || (st = h->prob_factor.upload(factor)) ||
+        (st = h->prob_cell_offset.upload(cell_off)))
         return st;
-    h->n_target = cfg->n_particles;
-    h->e_min = cfg->e_min;
-    h->e_max = cfg->e_max;
-    h->low_weight_cutoff = cfg->low_weight_cutoff;
-    h->load_balance = cfg->load_balance;
-    h->source_particle_weight = spw;
+    uint64_t n_target = 0, cap = 0;
+    for (int p = 0; p < P; p++) {
+        n_target += target[p];
+        cap += cfgs[p].store_capacity ? cfgs[p].store_capacity : 4 * (target[p] + nsrc[p]);
+    }
+    h->n_target = n_target;
+    h->source_particle_weight = weight[0];
     h->n_source = n_source;
-    uint64_t cap = cfg->store_capacity ? cfg->store_capacity : 4 * (cfg->n_particles + n_source);
     if ((st = h->processing.reserve(cap)) || (st = h->processed.reserve(cap)) || (st = h->extra.reserve(cap)))
         return st;
-    if ((st = h->flux_partial.alloc(kFluxPartials))) return st;
+    if ((st = h->flux_partial.alloc((size_t)kFluxPartials * P))) return st;
     if (!h->history.ptr) {
-        if ((st = h->history.alloc(1024))) return st;
+        if ((st = h->history.alloc(1024 * (size_t)P))) return st;
         h->history_capacity = 1024;
     }
     h->cycle_configured = true;
     return QSG_OK;
     QSG_API_END
+}
+
+extern "C" int qsg_configure_cycle(QsgHandle* h, const QsgCycleConfig* cfg)
+{
+    if (h && h->num_problems != 1)
+        return fail(QSG_ERR_INVALID, "qsg_configure_cycle: a batch needs qsg_configure_cycle_batch");
+    return qsg_configure_cycle_batch(h, cfg, nullptr);
 }
 
 extern "C" int qsg_cycle_init(QsgHandle* h, void* stream)
@@ -379,51 +568,8 @@ extern "C" int qsg_cycle_init(QsgHandle* h, void* stream)
     if (!h->cycle_configured) return fail(QSG_ERR_INVALID, "qsg_cycle_init: call qsg_configure_cycle first");
     int st = set_device(h);
     if (st) return st;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    // room for the census carried in plus this cycle's source, and for the
-    // population-controlled output (growing a store synchronises once)
-    const uint64_t need = h->known_census + h->n_source;
-    if ((st = h->processed.reserve(need)) ||
-        (st = h->extra.reserve(std::max<uint64_t>(need, 2 * h->n_target))))
-        return st;
-    std::swap(h->processing, h->processed);
-    cycle_begin_kernel<<<1, 1, 0, s>>>(h->scalars.ptr, h->processing.count, h->processed.count, h->balance.ptr,
-                                       (unsigned long long)h->n_source);
-    QSG_CUDA(cudaGetLastError());
-    if (h->n_source) {
-        SourceArgs a;
-        a.t = h->tables;
-        a.out = h->processing.view;
-        a.sc = h->scalars.ptr;
-        a.src_cell = h->src_cell.ptr;
-        a.src_cell_offset = h->src_cell_offset.ptr;
-        a.src_cell_count = h->src_cell_count.ptr;
-        a.cell_id = h->cell_id.ptr;
-        a.cell_volume = h->cell_volume.ptr;
-        a.n_source = h->n_source;
-        a.flags = h->flags.ptr;
-        a.e_min = h->e_min;
-        a.e_max = h->e_max;
-        a.weight = h->source_particle_weight;
-        unsigned blocks = (unsigned)((h->n_source + kInitBlock - 1) / kInitBlock);
-        source_kernel<<<blocks, kInitBlock, 0, s>>>(a);
-        QSG_CUDA(cudaGetLastError());
-    }
-    QSG_CUDA(cudaMemsetAsync(h->extra.count, 0, sizeof(unsigned long long), s));
-    PopArgs pa;
-    pa.in = h->processing.view;
-    pa.out = h->extra.view;
-    pa.balance = h->balance.ptr;
-    pa.flags = h->flags.ptr;
-    pa.n_target = h->n_target;
-    pa.low_weight_cutoff = h->low_weight_cutoff;
-    pa.weight_cutoff = h->low_weight_cutoff * h->source_particle_weight;
-    pa.load_balance = h->load_balance;
-    population_kernel<<<h->num_sms * 8, kInitBlock, 0, s>>>(pa);
-    QSG_CUDA(cudaGetLastError());
-    std::swap(h->processing, h->extra);
-    h->processing_on_device = true;
-    return QSG_OK;
+    if ((st = cycle_prepare(h))) return st;
+    return cycle_init_enqueue(h, static_cast<cudaStream_t>(stream));
     QSG_API_END
 }
 
@@ -434,27 +580,93 @@ extern "C" int qsg_cycle_finalize(QsgHandle* h, void* stream)
     if (!h->cycle_configured) return fail(QSG_ERR_INVALID, "qsg_cycle_finalize: call qsg_configure_cycle first");
     int st = set_device(h);
     if (st) return st;
+    if ((st = cycle_prepare(h))) return st;
+    return cycle_finalize_enqueue(h, static_cast<cudaStream_t>(stream));
+    QSG_API_END
+}
+
+// Key of the role -> store permutation (the stores swap roles during a cycle;
+// a graph captured for one permutation only fits cycles that start from it).
+static bool same_roles(const QsgHandle* h, const QsgHandle::GraphEntry& g)
+{
+    return g.proc == h->processing.base && g.done == h->processed.base && g.extra == h->extra.base &&
+           g.generation == h->store_generation;
+}
+
+extern "C" int qsg_run_cycles(QsgHandle* h, int32_t n_cycles, int32_t use_graph, void* stream)
+{
+    QSG_API_BEGIN
+    if (!h || n_cycles < 0) return fail(QSG_ERR_INVALID, "qsg_run_cycles: bad argument");
+    if (!h->cycle_configured) return fail(QSG_ERR_INVALID, "qsg_run_cycles: call qsg_configure_cycle first");
+    int st = set_device(h);
+    if (st) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (h->cycles_finalized >= h->history_capacity) {
-        // grow the history (synchronous; happens once per 1024 cycles)
-        DevBuf<CycleRecord> bigger;
-        if ((st = bigger.alloc(2 * h->history_capacity))) return st;
-        QSG_CUDA(cudaStreamSynchronize(s));
-        QSG_CUDA(cudaMemcpy(bigger.ptr, h->history.ptr, h->history_capacity * sizeof(CycleRecord),
-                            cudaMemcpyDeviceToDevice));
-        h->history.free();
-        h->history = bigger;
-        bigger.ptr = nullptr;
-        h->history_capacity *= 2;
+    for (int c = 0; c < n_cycles; c++) {
+        // allocation-free from here on unless a store or the history must grow;
+        // a reallocated store invalidates every captured graph
+        const uint64_t gen_before = h->processing.generation + h->processed.generation + h->extra.generation;
+        if ((st = cycle_prepare(h))) return st;
+        const uint64_t gen_after = h->processing.generation + h->processed.generation + h->extra.generation;
+        if (gen_after != gen_before) {
+            h->store_generation++;
+            h->clear_graphs();
+        }
+        if (!use_graph) {
+            if ((st = cycle_init_enqueue(h, s)) || (st = track_passes_async(h, s)) ||
+                (st = cycle_finalize_enqueue(h, s)))
+                return st;
+            continue;
+        }
+        // the history may be reallocated: graphs captured with the old buffer are stale
+        if (h->history.ptr != h->graph_history) {
+            h->clear_graphs();
+            h->graph_history = h->history.ptr;
+        }
+        QsgHandle::GraphEntry* entry = nullptr;
+        for (auto& g : h->graphs)
+            if (same_roles(h, g)) entry = &g;
+        if (!entry) {
+            QsgHandle::GraphEntry g;
+            g.proc = h->processing.base;
+            g.done = h->processed.base;
+            g.extra = h->extra.base;
+            g.generation = h->store_generation;
+            if (!h->capture_stream) QSG_CUDA(cudaStreamCreateWithFlags(&h->capture_stream, cudaStreamNonBlocking));
+            // capture one cycle (it swaps the host-side roles as it goes; restore
+            // them afterwards so the graph is launched from the same roles)
+            Store sp = h->processing, sd = h->processed, se = h->extra;
+            const uint64_t fin = h->cycles_finalized;
+            QSG_CUDA(cudaStreamBeginCapture(h->capture_stream, cudaStreamCaptureModeThreadLocal));
+            int cst = cycle_init_enqueue(h, h->capture_stream);
+            if (!cst) cst = track_passes_async(h, h->capture_stream);
+            if (!cst) cst = cycle_finalize_enqueue(h, h->capture_stream);
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamEndCapture(h->capture_stream, &graph);
+            g.after_proc = h->processing;
+            g.after_done = h->processed;
+            g.after_extra = h->extra;
+            h->processing = sp;
+            h->processed = sd;
+            h->extra = se;
+            h->cycles_finalized = fin;
+            if (cst) {
+                if (graph) cudaGraphDestroy(graph);
+                return cst;
+            }
+            if (e != cudaSuccess) return fail(QSG_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&g.exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return fail(QSG_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+            h->graphs.push_back(g);
+            entry = &h->graphs.back();
+        }
+        QSG_CUDA(cudaGraphLaunch(entry->exec, s));
+        h->processing = entry->after_proc;
+        h->processed = entry->after_done;
+        h->extra = entry->after_extra;
+        h->cycles_finalized++;
+        h->processing_on_device = true;
     }
-    const uint64_t nflux = (uint64_t)h->flux_replicas * h->num_cells * h->num_groups;
-    flux_partial_kernel<<<kFluxPartials, 256, 0, s>>>(h->flux.ptr, nflux, h->flux_partial.ptr);
-    QSG_CUDA(cudaGetLastError());
-    cycle_finalize_kernel<<<1, 64, 0, s>>>(h->scalars.ptr, h->balance.ptr, h->balance_replicas, h->processed.count,
-                                           h->flux_partial.ptr, kFluxPartials, h->history.ptr);
-    QSG_CUDA(cudaGetLastError());
-    QSG_CUDA(cudaMemsetAsync(h->flux.ptr, 0, nflux * sizeof(double), s));
-    h->cycles_finalized++;
     return QSG_OK;
     QSG_API_END
 }
@@ -469,10 +681,11 @@ extern "C" int qsg_cycle_history(QsgHandle* h, uint64_t first, uint64_t n, uint6
     int st = set_device(h);
     if (st) return st;
     if (n == 0) return QSG_OK;
-    std::vector<CycleRecord> rec(n);
+    const int P = h->num_problems;
+    std::vector<CycleRecord> rec(n * P);
     QSG_CUDA(cudaDeviceSynchronize());
-    QSG_CUDA(cudaMemcpy(rec.data(), h->history.ptr + first, n * sizeof(CycleRecord), cudaMemcpyDeviceToHost));
-    for (uint64_t i = 0; i < n; i++) {
+    QSG_CUDA(cudaMemcpy(rec.data(), h->history.ptr + first * P, n * P * sizeof(CycleRecord), cudaMemcpyDeviceToHost));
+    for (uint64_t i = 0; i < n * P; i++) {
         if (balance)
             for (int k = 0; k < QSG_BAL_COUNT; k++) balance[i * QSG_BAL_COUNT + k] = rec[i].balance[k];
         if (flux_total) flux_total[i] = rec[i].flux_total;

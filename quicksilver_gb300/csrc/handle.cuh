@@ -57,6 +57,7 @@ struct Store {
     void* base = nullptr;
     unsigned long long* count = nullptr;  // device counter
     uint64_t capacity = 0;
+    uint64_t generation = 0;              // bumped on every reallocation
     DevStore view{};
 
     int reserve(uint64_t cap)
@@ -90,6 +91,7 @@ struct Store {
         view = nv;
         count = nv.count;
         capacity = nc;
+        generation++;
         return QSG_OK;
     }
 
@@ -177,6 +179,11 @@ struct QsgHandle {
     int num_sms = 0;
     int track_blocks = 0;            // persistent grid of the tracking kernel
     int max_passes = 8;              // fission passes per asynchronous cycle
+    int collision_batch = qsg::kCollisionBatch;
+    int queue_chunk = 1;
+    int32_t num_problems = 1;        // > 1: a batch built by qsg_batch_create
+    std::vector<int32_t> h_problem_cell_offset;   // [problems + 1]
+    qsg::DevBuf<int32_t> cell_problem;            // [C] (batches only)
     int32_t flux_replicas = 1, balance_replicas = 1;
     uint64_t max_segments = (uint64_t)1 << 40;
     int32_t num_cells = 0, num_groups = 0, num_materials = 0;
@@ -213,9 +220,32 @@ struct QsgHandle {
     qsg::DevBuf<int32_t> src_cell, src_cell_count;   // [n_source] cell of each source particle, [C] per-cell count
     qsg::DevBuf<uint64_t> src_cell_offset;            // [C] first source slot of each cell
     qsg::DevBuf<qsg::CycleScalars> scalars;
-    qsg::DevBuf<qsg::CycleRecord> history;
-    uint64_t history_capacity = 0;
+    qsg::DevBuf<qsg::CycleRecord> history;        // [cycles][problems]
+    uint64_t history_capacity = 0;                // in cycles
     uint64_t cycles_finalized = 0;
+    // per problem (index p of a batch; one entry for a single problem)
+    std::vector<int32_t> h_problem_material_offset;   // [problems + 1]
+    qsg::DevBuf<double> prob_weight, prob_emin, prob_emax, prob_lowcut, prob_factor;
+    qsg::DevBuf<uint64_t> prob_target, prob_nsource, prob_seed_offset;
+    qsg::DevBuf<int32_t> prob_load_balance, prob_cell_offset;
+    qsg::DevBuf<unsigned long long> prob_carry;
+    // CUDA graphs of whole cycles, one per role permutation of the stores
+    struct GraphEntry {
+        void *proc = nullptr, *done = nullptr, *extra = nullptr;
+        uint64_t generation = 0;
+        cudaGraphExec_t exec = nullptr;
+        qsg::Store after_proc, after_done, after_extra;
+    };
+    std::vector<GraphEntry> graphs;
+    uint64_t store_generation = 0;
+    const qsg::CycleRecord* graph_history = nullptr;
+    cudaStream_t capture_stream = nullptr;
+    void clear_graphs()
+    {
+        for (auto& g : graphs)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+        graphs.clear();
+    }
 };
 
 namespace qsg {

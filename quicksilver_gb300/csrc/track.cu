@@ -30,6 +30,7 @@
 #include "qsg.h"
 #include "status.h"
 #include "track_device.cuh"
+#include "batch.h"
 
 namespace cg = cooperative_groups;
 
@@ -507,24 +508,64 @@ __device__ __forceinline__ int balance_slot(int local)
     }
 }
 
-template <int BLOCK>
-__device__ __forceinline__ void flush_counters(const DevTally& tally, uint32_t* cnt, int replica)
-{
-    __shared__ unsigned long long red[BLOCK / 32][LC_N];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// Per-problem balance counters of a tracking block: a lane keeps the counts of
+// the problem it is tracking in registers and adds them here when it moves to
+// a particle of another problem or finishes; the block adds the table to
+// global memory once at the end.
+struct BlockCounters {
+    unsigned long long* smem;   // [problems][LC_N], or null when the batch is too large
+    const DevTally* tally;
+    int replica;
+
+    __device__ __forceinline__ void add(int prob, uint32_t* cnt) const
+    {
 #pragma unroll
-    for (int k = 0; k < LC_N; k++) {
-        unsigned long long v = cnt[k];
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-        if (lane == 0) red[warp][k] = v;
+        for (int k = 0; k < LC_N; k++) {
+            if (cnt[k]) {
+                if (smem) atomicAdd(smem + prob * LC_N + k, (unsigned long long)cnt[k]);
+                else
+                    atomicAdd(tally->balance + ((int64_t)replica * tally->num_problems + prob) * QSG_BAL_COUNT +
+                                  balance_slot(k),
+                              (unsigned long long)cnt[k]);
+                cnt[k] = 0;
+            }
+        }
     }
-    __syncthreads();
-    if (threadIdx.x < LC_N) {
-        unsigned long long sum = 0;
-        for (int w = 0; w < BLOCK / 32; w++) sum += red[w][threadIdx.x];
-        if (sum) atomicAdd(tally.balance + (int64_t)replica * QSG_BAL_COUNT + balance_slot(threadIdx.x), sum);
+
+    // Final add of every lane's counts: when the whole warp holds the same
+    // problem, the counts are summed with shuffles first.
+    __device__ __forceinline__ void add_final(int prob, uint32_t* cnt) const
+    {
+        const int p0 = __shfl_sync(0xffffffffu, prob, 0);
+        if (__all_sync(0xffffffffu, prob == p0)) {
+            if (p0 < 0) return;
+#pragma unroll
+            for (int k = 0; k < LC_N; k++) {
+                uint32_t v = cnt[k];
+                for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+                cnt[k] = ((threadIdx.x & 31) == 0) ? v : 0;
+            }
+            if ((threadIdx.x & 31) == 0) add(p0, cnt);
+        } else if (prob >= 0) {
+            add(prob, cnt);
+        }
     }
-}
+
+    template <int BLOCK>
+    __device__ __forceinline__ void flush_block() const
+    {
+        if (!smem) return;
+        __syncthreads();
+        const int n = tally->num_problems * LC_N;
+        for (int k = threadIdx.x; k < n; k += BLOCK) {
+            const unsigned long long v = smem[k];
+            if (v)
+                atomicAdd(tally->balance + ((int64_t)replica * tally->num_problems + k / LC_N) * QSG_BAL_COUNT +
+                              balance_slot(k % LC_N),
+                          v);
+        }
+    }
+};
 
 // Persistent tracking pass over the store `in` (its count is read on the
 // device): CycleTrackingGuts + CycleTrackingFunction (CycleTracking.cc:14-120)
@@ -533,28 +574,50 @@ __device__ __forceinline__ void flush_counters(const DevTally& tally, uint32_t* 
 // long histories do not hold idle lanes; the warp leaves when every lane has
 // finished and the queue is empty.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK, kTrackMinBlocks) track_kernel(DevTables t, DevTally tally, DevStore in,
+__global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / BLOCK) track_kernel(DevTables t,
+                                                                                                 DevTally tally,
+                                                                                                 DevStore in,
                                                                        DevStore census,
                                                       DevStore extra, unsigned long long* cursor)
 {
+    extern __shared__ unsigned long long s_counts[];
+    BlockCounters bc;
+    bc.smem = (tally.num_problems <= kSmemProblems) ? s_counts : nullptr;
+    bc.tally = &tally;
+    bc.replica = (int)(blockIdx.x % (unsigned)tally.balance_replicas);
+    if (bc.smem)
+        for (int k = threadIdx.x; k < tally.num_problems * LC_N; k += BLOCK) s_counts[k] = 0;
+    __syncthreads();
     uint32_t cnt[LC_N];
 #pragma unroll
     for (int k = 0; k < LC_N; k++) cnt[k] = 0;
+    int cur_prob = -1;
     const uint64_t n = *in.count;
     Particle p;
     bool active = false, exhausted = false, pending = false;
     double* flux_row = tally.flux;
     uint64_t segs_this_history = 0;
+    uint64_t next = 0, end = 0;   // this lane's claimed run of queue positions
+    const uint64_t chunk = (uint64_t)tally.queue_chunk;
     for (;;) {
         if (!active && !exhausted) {
-            cg::coalesced_group g = cg::coalesced_threads();
-            unsigned long long base = 0;
-            if (g.thread_rank() == 0) base = atomicAdd(cursor, (unsigned long long)g.size());
-            base = g.shfl(base, 0);
-            const uint64_t i = base + g.thread_rank();
+            if (next >= end) {
+                cg::coalesced_group g = cg::coalesced_threads();
+                unsigned long long base = 0;
+                if (g.thread_rank() == 0) base = atomicAdd(cursor, (unsigned long long)g.size() * chunk);
+                base = g.shfl(base, 0);
+                next = base + g.thread_rank() * chunk;
+                end = next + chunk;
+            }
+            const uint64_t i = next++;
             if (i < n) {
                 load_particle(t, in, i, p);
                 if (!(p.speed > 0.0)) raise_flag(tally, QSG_DEV_BAD_FACET);
+                const int prob = tally.cell_problem ? __ldg(tally.cell_problem + p.cell) : 0;
+                if (prob != cur_prob) {
+                    if (cur_prob >= 0) bc.add(cur_prob, cnt);
+                    cur_prob = prob;
+                }
                 // CycleTracking.cc:37-39 replica selection by particle index
                 flux_row = tally.flux + (int64_t)(i % (uint64_t)tally.flux_replicas) * t.num_cells * t.num_groups;
                 segs_this_history = 0;
@@ -571,7 +634,7 @@ __global__ void __launch_bounds__(BLOCK, kTrackMinBlocks) track_kernel(DevTables
         // are untouched while it waits, so the results are unchanged.
         const unsigned pend_mask = __ballot_sync(0xffffffffu, active && pending);
         const unsigned run_mask = __ballot_sync(0xffffffffu, active && !pending);
-        if (pend_mask != 0u && (__popc(pend_mask) >= kCollisionBatch || run_mask == 0u)) {
+        if (pend_mask != 0u && (__popc(pend_mask) >= tally.collision_batch || run_mask == 0u)) {
             if (pending) {
                 pending = false;
                 active = collision_event(t, tally, p, __ldg(t.cell_class + p.cell), extra, cnt);
@@ -626,7 +689,8 @@ __global__ void __launch_bounds__(BLOCK, kTrackMinBlocks) track_kernel(DevTables
             active = keep;
         }
     }
-    flush_counters<BLOCK>(tally, cnt, (int)(blockIdx.x % (unsigned)tally.balance_replicas));
+    bc.add_final(cur_prob, cnt);
+    bc.flush_block<BLOCK>();
 }
 
 // ------------------------------------------------------------------------
@@ -652,7 +716,29 @@ DevTally tally_view(QsgHandle* h)
     t.flux_replicas = h->flux_replicas;
     t.balance_replicas = h->balance_replicas;
     t.max_segments = h->max_segments;
+    t.cell_problem = h->num_problems > 1 ? h->cell_problem.ptr : nullptr;
+    t.num_problems = h->num_problems;
+    t.collision_batch = h->collision_batch;
+    t.queue_chunk = h->queue_chunk;
     return t;
+}
+
+size_t track_smem_bytes(const QsgHandle* h)
+{
+    return h->num_problems <= kSmemProblems ? (size_t)h->num_problems * LC_N * sizeof(unsigned long long) : 0;
+}
+
+// Persistent grid for the current block size: SMs x resident blocks.
+int configure_track_grid(QsgHandle* h)
+{
+    int per_sm = 0;
+    const size_t smem = track_smem_bytes(h);
+    if (h->block_size == 256)
+        QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel<256>, 256, smem));
+    else
+        QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel<128>, 128, smem));
+    h->track_blocks = h->num_sms * (per_sm > 0 ? per_sm : 1);
+    return QSG_OK;
 }
 
 namespace {
@@ -928,8 +1014,13 @@ int launch_pass(QsgHandle* h, cudaStream_t s)
     unsigned long long* cursor = &h->scalars.ptr->cursor;
     QSG_CUDA(cudaMemsetAsync(h->extra.count, 0, sizeof(unsigned long long), s));
     QSG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s));
-    track_kernel<kTrackBlock><<<h->track_blocks, kTrackBlock, 0, s>>>(h->tables, tally_view(h), h->processing.view,
-                                                                       h->processed.view, h->extra.view, cursor);
+    const size_t smem = track_smem_bytes(h);
+    if (h->block_size == 256)
+        track_kernel<256><<<h->track_blocks, 256, smem, s>>>(h->tables, tally_view(h), h->processing.view,
+                                                             h->processed.view, h->extra.view, cursor);
+    else
+        track_kernel<128><<<h->track_blocks, 128, smem, s>>>(h->tables, tally_view(h), h->processing.view,
+                                                             h->processed.view, h->extra.view, cursor);
     QSG_CUDA(cudaGetLastError());
     // the extra store becomes the next pass's input; the old input is free
     std::swap(h->processing, h->extra);
@@ -995,10 +1086,13 @@ extern "C" int qsg_device_count(int* count)
     return QSG_OK;
 }
 
-extern "C" int qsg_create(const QsgProblem* problem, const QsgOptions* options, QsgHandle** out)
+namespace {
+
+// Shared by qsg_create (one problem) and qsg_batch_create (the union of
+// several; `uni` holds the per-problem cell ranges).
+int create_impl(const QsgProblem* problem, const QsgOptions* options, const UnionProblem* uni, int n_problems,
+                QsgHandle** out)
 {
-    QSG_API_BEGIN
-    if (!problem || !out) return fail(QSG_ERR_INVALID, "qsg_create: null argument");
     *out = nullptr;
     int st = validate_problem(problem);
     if (st) return st;
@@ -1012,22 +1106,32 @@ extern "C" int qsg_create(const QsgProblem* problem, const QsgOptions* options, 
         if (options->balance_replicas > 0) h->balance_replicas = options->balance_replicas;
         if (options->max_segments > 0) h->max_segments = options->max_segments;
         if (options->max_passes > 0) h->max_passes = options->max_passes;
+        if (options->block_size == 128 || options->block_size == 256) h->block_size = options->block_size;
+        if (options->collision_batch > 0) h->collision_batch = std::min<int>(options->collision_batch, 32);
     }
     h->num_cells = problem->num_cells;
     h->num_groups = problem->num_groups;
+    h->num_problems = n_problems;
+    if (uni) {
+        h->h_problem_cell_offset = uni->problem_cell_offset;
+        h->h_problem_material_offset = uni->problem_material_offset;
+    } else {
+        h->h_problem_cell_offset = {0, problem->num_cells};
+        h->h_problem_material_offset = {0, problem->num_materials};
+    }
     auto cleanup = [&](int code) {
         qsg_destroy(h);
         return code;
     };
     if ((st = set_device(h))) return cleanup(st);
     if ((st = upload_tables(h, problem))) return cleanup(st);
+    if (uni && (st = h->cell_problem.upload(uni->cell_problem))) return cleanup(st);
     {
         cudaDeviceProp prop;
-        QSG_CUDA(cudaGetDeviceProperties(&prop, h->device));
+        if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess)
+            return cleanup(fail(QSG_ERR_CUDA, "cudaGetDeviceProperties failed"));
         h->num_sms = prop.multiProcessorCount;
-        int per_sm = 0;
-        QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel<kTrackBlock>, kTrackBlock, 0));
-        h->track_blocks = h->num_sms * (per_sm > 0 ? per_sm : 1);
+        if ((st = configure_track_grid(h))) return cleanup(st);
     }
     h->num_materials = problem->num_materials;
     if (problem->cell_volume) h->h_cell_volume.assign(problem->cell_volume, problem->cell_volume + problem->num_cells);
@@ -1037,7 +1141,7 @@ extern "C" int qsg_create(const QsgProblem* problem, const QsgOptions* options, 
     if (cudaMemset(h->scalars.ptr, 0, sizeof(CycleScalars)) != cudaSuccess)
         return cleanup(fail(QSG_ERR_CUDA, "qsg_create: memset failed"));
     if ((st = h->flux.alloc((size_t)h->flux_replicas * h->num_cells * h->num_groups))) return cleanup(st);
-    if ((st = h->balance.alloc((size_t)h->balance_replicas * QSG_BAL_COUNT))) return cleanup(st);
+    if ((st = h->balance.alloc((size_t)h->balance_replicas * h->num_problems * QSG_BAL_COUNT))) return cleanup(st);
     if ((st = h->flags.alloc(1))) return cleanup(st);
     if (cudaMemset(h->flux.ptr, 0, h->flux.n * sizeof(double)) != cudaSuccess ||
         cudaMemset(h->balance.ptr, 0, h->balance.n * sizeof(unsigned long long)) != cudaSuccess ||
@@ -1048,7 +1152,51 @@ extern "C" int qsg_create(const QsgProblem* problem, const QsgOptions* options, 
         return cleanup(st);
     *out = h;
     return QSG_OK;
+}
+
+}  // namespace
+
+extern "C" int qsg_create(const QsgProblem* problem, const QsgOptions* options, QsgHandle** out)
+{
+    QSG_API_BEGIN
+    if (!problem || !out) return fail(QSG_ERR_INVALID, "qsg_create: null argument");
+    return create_impl(problem, options, nullptr, 1, out);
     QSG_API_END
+}
+
+extern "C" int qsg_batch_create(const QsgProblem* problems, int32_t n_problems, const QsgOptions* options,
+                                QsgHandle** out)
+{
+    QSG_API_BEGIN
+    if (!problems || !out || n_problems < 1) return fail(QSG_ERR_INVALID, "qsg_batch_create: bad argument");
+    *out = nullptr;
+    UnionProblem u;
+    build_union(problems, n_problems, u);
+    return create_impl(&u.view, options, &u, n_problems, out);
+    QSG_API_END
+}
+
+extern "C" int qsg_num_problems(QsgHandle* h, int32_t* n, int32_t* cell_offsets)
+{
+    if (!h || !n) return fail(QSG_ERR_INVALID, "qsg_num_problems: null argument");
+    *n = h->num_problems;
+    if (cell_offsets)
+        for (int k = 0; k <= h->num_problems; k++) cell_offsets[k] = h->h_problem_cell_offset[k];
+    return QSG_OK;
+}
+
+extern "C" int qsg_set_tuning(QsgHandle* h, int32_t block_size, int32_t collision_batch, int32_t queue_chunk)
+{
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_set_tuning: null handle");
+    if (block_size != 0 && block_size != 128 && block_size != 256)
+        return fail(QSG_ERR_INVALID, "qsg_set_tuning: block size must be 128 or 256");
+    int st = set_device(h);
+    if (st) return st;
+    if (block_size) h->block_size = block_size;
+    if (collision_batch > 0) h->collision_batch = std::min<int>(collision_batch, 32);
+    if (queue_chunk > 0) h->queue_chunk = std::min<int>(queue_chunk, 1024);
+    h->clear_graphs();   // captured launches carry the old shape
+    return configure_track_grid(h);
 }
 
 extern "C" int qsg_destroy(QsgHandle* h)
@@ -1063,6 +1211,11 @@ extern "C" int qsg_destroy(QsgHandle* h)
     h->flux.free(); h->balance.free(); h->flags.free(); h->flux_partial.free();
     h->cell_volume.free(); h->cell_id.free(); h->src_cell.free(); h->src_cell_count.free();
     h->src_cell_offset.free(); h->scalars.free(); h->history.free();
+    h->cell_problem.free(); h->prob_weight.free(); h->prob_emin.free(); h->prob_emax.free(); h->prob_lowcut.free();
+    h->prob_factor.free(); h->prob_target.free(); h->prob_nsource.free(); h->prob_seed_offset.free();
+    h->prob_load_balance.free(); h->prob_cell_offset.free(); h->prob_carry.free();
+    h->clear_graphs();
+    if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
     h->processing.release(); h->processed.release(); h->extra.release();
     delete h;
     return QSG_OK;
@@ -1179,7 +1332,7 @@ extern "C" int qsg_read_tallies(QsgHandle* h, uint64_t* balance, double* flux)
         QSG_CUDA(cudaMemcpy(b.data(), h->balance.ptr, b.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
         for (int k = 0; k < QSG_BAL_COUNT; k++) {
             uint64_t s = 0;
-            for (int r = 0; r < h->balance_replicas; r++) s += b[(size_t)r * QSG_BAL_COUNT + k];
+            for (int r = 0; r < h->balance_replicas * h->num_problems; r++) s += b[(size_t)r * QSG_BAL_COUNT + k];
             balance[k] = s;
         }
     }

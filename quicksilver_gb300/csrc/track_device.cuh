@@ -93,12 +93,20 @@ struct DevTables {
 
 struct DevTally {
     double* flux;                  // [replicas][C][G]
-    unsigned long long* balance;   // [replicas][QSG_BAL_COUNT]
+    unsigned long long* balance;   // [replicas][problems][QSG_BAL_COUNT]
     unsigned int* error_flags;
+    const int32_t* cell_problem;   // [C] problem of each cell (null: one problem)
+    int32_t num_problems;
     int32_t flux_replicas;
     int32_t balance_replicas;
+    int32_t collision_batch;       // parked collisions that trigger a warp's collision step
+    int32_t queue_chunk;           // consecutive particles a lane claims per work-queue atomic
     uint64_t max_segments;
 };
+
+// Problems whose counters a tracking block accumulates in shared memory
+// before one global flush; larger batches add to global memory directly.
+constexpr int kSmemProblems = 256;
 
 __device__ __forceinline__ void raise_flag(const DevTally& tally, unsigned int bit)
 {

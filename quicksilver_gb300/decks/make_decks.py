@@ -101,6 +101,31 @@ def config4() -> str:
             drawn_materials(rng, ["matA", "matB", "matC"]))
 
 
+def config3(n_problems: int = 64, seed: int = 3) -> list:
+    """The uneven ensemble tracked as one batch: mesh edge n drawn from
+    {8, 16, 24, 32, 48} with 1-cm cells (lx = n), particle count log-uniform in
+    [1e4, 2e6], 1-3 materials as nested spheres of radii 0.2n and 0.4n about the
+    centre with config-2-style polynomial cross sections, 230 groups, 10
+    cycles; problem p carries seed 3000 + p (numpy default_rng(seed))."""
+    rng = np.random.default_rng(seed)
+    decks = []
+    for p in range(n_problems):
+        n = int(rng.choice([8, 16, 24, 32, 48]))
+        n_part = int(round(float(np.exp(rng.uniform(np.log(1e4), np.log(2e6))))))
+        n_mat = int(rng.integers(1, 4))
+        names = [f"m{p}_{k}" for k in range(n_mat)]
+        c = n / 2
+        geo = brick(names[0], 0, n, 0, n, 0, n)
+        if n_mat >= 2:
+            geo += sphere(names[1], repr(0.4 * n), c, c, c)
+        if n_mat >= 3:
+            geo += sphere(names[2], repr(0.2 * n), c, c, c)
+        text = (simulation(lx=n, ly=n, lz=n, nx=n, ny=n, nz=n, nParticles=n_part, nSteps=10, seed=3000 + p) +
+                geo + drawn_materials(rng, names))
+        decks.append(text)
+    return decks
+
+
 def small(**kw) -> str:
     sim = dict(lx=5, ly=5, lz=5, nx=5, ny=5, nz=5, nParticles=4000, nSteps=3, nGroups=16)
     sim.update(kw)

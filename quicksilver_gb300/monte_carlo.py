@@ -4,9 +4,13 @@
 main.cc's cycle loop (main.cc:38-85): ``cycle_init`` / ``cycle_tracking`` /
 ``cycle_finalize`` have the meaning of cycleInit / cycleTracking /
 cycleFinalize (main.cc:96-121, 138-307, 310-324), but every step runs on the
-GPU through libqsg.so; the host only enqueues work.  ``run`` executes
-``nSteps`` cycles and returns the per-cycle balance counters and scalar-flux
-totals, the numbers the reference prints each cycle (Tallies.cc:123-144).
+GPU through libqsg.so; the host only enqueues work.  ``run`` executes cycles
+and returns the per-cycle balance counters and scalar-flux totals, the numbers
+the reference prints each cycle (Tallies.cc:123-144).
+
+``BatchMonteCarlo`` runs many independent decks together: one persistent
+tracking launch per pass covers every problem, and ``run(use_graph=True)``
+replays each whole cycle from a captured CUDA graph.
 """
 from __future__ import annotations
 
@@ -22,11 +26,11 @@ from .tracker import Tracker
 
 @dataclass
 class CycleHistory:
-    balance: np.ndarray      # [cycles, 13] uint64, BALANCE_FIELDS order
-    flux_total: np.ndarray   # [cycles] float64
+    balance: np.ndarray      # [cycles, 13] (single) or [cycles, problems, 13] uint64, BALANCE_FIELDS order
+    flux_total: np.ndarray   # [cycles] or [cycles, problems] float64
 
     def segments(self) -> int:
-        return int(self.balance[:, N.BAL["num_segments"]].sum())
+        return int(self.balance[..., N.BAL["num_segments"]].sum())
 
 
 def _stream_ptr(stream) -> C.c_void_p:
@@ -38,25 +42,31 @@ def _stream_ptr(stream) -> C.c_void_p:
     return C.c_void_p(int(stream))
 
 
-class MonteCarlo:
-    def __init__(self, deck: Deck, flux_replicas: int = 1, balance_replicas: int = 1, max_passes: int = 8,
-                 store_capacity: int = 0, device: int = 0, problem: HostProblem | None = None):
-        self.deck = deck
-        self.params = deck.simulation
-        self.problem = problem if problem is not None else deck.build()
-        self.tracker = Tracker(self.problem, flux_replicas=flux_replicas, balance_replicas=balance_replicas,
-                               device=device, max_passes=max_passes)
-        self._rates = np.ascontiguousarray(self.problem.source_rates())
-        cfg = N.QsgCycleConfig(source_rate=self._rates.ctypes.data_as(C.POINTER(C.c_double)),
-                               n_particles=self.params.n_particles, e_min=self.params.e_min,
-                               e_max=self.params.e_max, low_weight_cutoff=self.params.low_weight_cutoff,
-                               load_balance=self.params.load_balance, reserved=0, store_capacity=store_capacity)
-        N.check(N.lib().qsg_configure_cycle(self.tracker.handle, C.byref(cfg)))
-        self.cycles = 0
+def seed_offset(seed: int) -> int:
+    """A 64-bit offset derived from a deck's `seed`, for batches that want
+    distinct random streams per problem (the reference itself never uses
+    `seed`: its source seeds come from cell ids, MC_SourceNow.cc:90-97)."""
+    z = (int(seed) + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    return z ^ (z >> 31)
 
-    @property
-    def n_steps(self) -> int:
-        return self.params.n_steps
+
+class _Driver:
+    def _configure(self, decks, problems, store_capacity, seed_offsets):
+        sims = [d.simulation for d in decks]
+        self._rates = [np.ascontiguousarray(p.source_rates()) for p in problems]
+        cfgs = (N.QsgCycleConfig * len(decks))()
+        for k, (s, r) in enumerate(zip(sims, self._rates)):
+            cfgs[k] = N.QsgCycleConfig(source_rate=r.ctypes.data_as(C.POINTER(C.c_double)), n_particles=s.n_particles,
+                                       e_min=s.e_min, e_max=s.e_max, low_weight_cutoff=s.low_weight_cutoff,
+                                       load_balance=s.load_balance, reserved=0, store_capacity=store_capacity)
+        offs = None
+        if seed_offsets is not None:
+            self._offs = np.ascontiguousarray(seed_offsets, dtype=np.uint64)
+            offs = self._offs.ctypes.data_as(C.POINTER(C.c_uint64))
+        N.check(N.lib().qsg_configure_cycle_batch(self.tracker.handle, cfgs, offs))
+        self.cycles = 0
 
     def cycle_init(self, stream=None) -> None:
         N.check(N.lib().qsg_cycle_init(self.tracker.handle, _stream_ptr(stream)))
@@ -68,14 +78,14 @@ class MonteCarlo:
         N.check(N.lib().qsg_cycle_finalize(self.tracker.handle, _stream_ptr(stream)))
         self.cycles += 1
 
-    def history(self, first: int = 0, n: int | None = None) -> CycleHistory:
+    def _history(self, first, n, problems):
         n = self.cycles - first if n is None else n
-        bal = np.zeros((max(n, 0), 13), dtype=np.uint64)
-        tot = np.zeros(max(n, 0), dtype=np.float64)
+        bal = np.zeros((max(n, 0), problems, 13), dtype=np.uint64)
+        tot = np.zeros((max(n, 0), problems), dtype=np.float64)
         N.check(N.lib().qsg_cycle_history(self.tracker.handle, first, n,
                                           bal.ctypes.data_as(C.POINTER(C.c_uint64)),
                                           tot.ctypes.data_as(C.POINTER(C.c_double))))
-        return CycleHistory(bal, tot)
+        return bal, tot
 
     def processing(self) -> np.ndarray:
         """Host copy of the processing store (the particles a cycle will track)."""
@@ -89,6 +99,37 @@ class MonteCarlo:
     def device_status(self, clear: bool = True) -> int:
         return self.tracker.device_status(clear)
 
+    def run_cycles(self, n_cycles: int, use_graph: bool = False, stream=None) -> None:
+        """n whole cycles enqueued without host synchronisation: each cycle is
+        init + QsgOptions.max_passes tracking passes + finalize, replayed from a
+        captured CUDA graph when use_graph is set."""
+        N.check(N.lib().qsg_run_cycles(self.tracker.handle, n_cycles, int(use_graph), _stream_ptr(stream)))
+        self.cycles += n_cycles
+
+    def close(self):
+        self.tracker.close()
+
+
+class MonteCarlo(_Driver):
+    def __init__(self, deck: Deck, flux_replicas: int = 1, balance_replicas: int = 1, max_passes: int = 8,
+                 store_capacity: int = 0, device: int = 0, problem: HostProblem | None = None,
+                 block_size: int = 0, collision_batch: int = 0):
+        self.deck = deck
+        self.params = deck.simulation
+        self.problem = problem if problem is not None else deck.build()
+        self.tracker = Tracker(self.problem, flux_replicas=flux_replicas, balance_replicas=balance_replicas,
+                               device=device, max_passes=max_passes, block_size=block_size,
+                               collision_batch=collision_batch)
+        self._configure([deck], [self.problem], store_capacity, None)
+
+    @property
+    def n_steps(self) -> int:
+        return self.params.n_steps
+
+    def history(self, first: int = 0, n: int | None = None) -> CycleHistory:
+        bal, tot = self._history(first, n, 1)
+        return CycleHistory(bal[:, 0, :], tot[:, 0])
+
     def run(self, n_steps: int | None = None, stream=None) -> CycleHistory:
         first = self.cycles
         for _ in range(self.n_steps if n_steps is None else n_steps):
@@ -101,5 +142,36 @@ class MonteCarlo:
             raise N.QsgError(N.QSG_ERR_DEVICE, f"device flags 0x{flags:x} raised during the run")
         return hist
 
-    def close(self):
-        self.tracker.close()
+
+class BatchMonteCarlo(_Driver):
+    """Independent decks tracked together (they must share eMin, eMax, nGroups and dt)."""
+
+    def __init__(self, decks: list, flux_replicas: int = 1, balance_replicas: int = 1, max_passes: int = 8,
+                 store_capacity: int = 0, device: int = 0, problems: list | None = None,
+                 seed_offsets=None, block_size: int = 0, collision_batch: int = 0):
+        self.decks = list(decks)
+        self.problems = problems if problems is not None else [d.build() for d in self.decks]
+        self.tracker = Tracker(self.problems, flux_replicas=flux_replicas, balance_replicas=balance_replicas,
+                               device=device, max_passes=max_passes, block_size=block_size,
+                               collision_batch=collision_batch)
+        self._configure(self.decks, self.problems, store_capacity, seed_offsets)
+
+    @property
+    def num_problems(self) -> int:
+        return len(self.problems)
+
+    def history(self, first: int = 0, n: int | None = None) -> CycleHistory:
+        bal, tot = self._history(first, n, self.num_problems)
+        return CycleHistory(bal, tot)
+
+    def run(self, n_cycles: int, use_graph: bool = True, stream=None) -> CycleHistory:
+        first = self.cycles
+        self.run_cycles(n_cycles, use_graph, stream)
+        hist = self.history(first)
+        flags = self.device_status()
+        if flags:
+            raise N.QsgError(N.QSG_ERR_DEVICE, f"device flags 0x{flags:x} raised during the run")
+        return hist
+
+    def tune(self, block_size: int = 0, collision_batch: int = 0, queue_chunk: int = 0) -> None:
+        N.check(N.lib().qsg_set_tuning(self.tracker.handle, block_size, collision_batch, queue_chunk))

@@ -15,16 +15,30 @@ from .problem import HostProblem
 
 
 class Tracker:
-    def __init__(self, problem: HostProblem, flux_replicas: int = 1, balance_replicas: int = 1,
-                 particle_capacity: int = 0, max_segments: int = 0, device: int = 0, max_passes: int = 0):
-        self.problem = problem
-        opts = N.QsgOptions(device=device, block_size=0, flux_replicas=flux_replicas,
+    def __init__(self, problem: HostProblem | list, flux_replicas: int = 1, balance_replicas: int = 1,
+                 particle_capacity: int = 0, max_segments: int = 0, device: int = 0, max_passes: int = 0,
+                 block_size: int = 0, collision_batch: int = 0):
+        """One problem, or a list of problems tracked together as a batch
+        (qsg_batch_create: they must share the energy grid and time step)."""
+        opts = N.QsgOptions(device=device, block_size=block_size, flux_replicas=flux_replicas,
                             balance_replicas=balance_replicas, particle_capacity=particle_capacity,
-                            max_segments=max_segments, max_passes=max_passes, reserved=0)
+                            max_segments=max_segments, max_passes=max_passes, collision_batch=collision_batch)
         self._h = C.c_void_p()
-        N.check(N.lib().qsg_create(C.byref(problem.view), C.byref(opts), C.byref(self._h)))
-        self.num_cells = problem.num_cells
-        self.num_groups = problem.num_groups
+        if isinstance(problem, (list, tuple)):
+            self.problems = list(problem)
+            views = (N.QsgProblem * len(self.problems))(*[p.view for p in self.problems])
+            N.check(N.lib().qsg_batch_create(views, len(self.problems), C.byref(opts), C.byref(self._h)))
+            self.problem = self.problems[0]
+        else:
+            self.problems = [problem]
+            self.problem = problem
+            N.check(N.lib().qsg_create(C.byref(problem.view), C.byref(opts), C.byref(self._h)))
+        n = C.c_int32()
+        offs = np.zeros(len(self.problems) + 1, dtype=np.int32)
+        N.check(N.lib().qsg_num_problems(self._h, C.byref(n), offs.ctypes.data_as(C.POINTER(C.c_int32))))
+        self.cell_offsets = offs
+        self.num_cells = int(offs[-1])
+        self.num_groups = self.problem.num_groups
 
     @property
     def handle(self) -> C.c_void_p:
