@@ -263,6 +263,42 @@ int qsg_run_cycles(QsgHandle* h, int32_t n_cycles, int32_t use_graph, void* stre
  * particles claimed per work-queue atomic (1-1024); 0 keeps a value. */
 int qsg_set_tuning(QsgHandle* h, int32_t block_size, int32_t collision_batch, int32_t queue_chunk);
 
+/* ---- tracking without allocation ---------------------------------------- */
+/* No counterpart in the reference (Quicksilver allocates its vaults itself).
+ * For callers that cannot let a library call cudaMalloc or cudaFree while
+ * they run: a process that has given (nearly) all of the GPU's memory to a
+ * pool allocator -- PyTorch's caching allocator, an application arena -- would
+ * see such an allocation fail or escape the pool's accounting, and cudaFree
+ * synchronises the whole device, stalling the caller's other streams.
+ *
+ * Tracks the n particles of `particles` (device arrays, read only) through
+ * the handle's tables exactly as qsg_track_cycle_sync does, fission passes
+ * included.  Census particles go to `census` (device arrays with room for
+ * census_capacity particles; *n_census receives the count); scalar flux is
+ * ADDED into `flux` (device, [num_cells * G], the handle's cell numbering) and
+ * the balance counters into `balance` (device, [problems * 13], QSG_BAL_*
+ * order), so zero them first for fresh tallies.  The handle's own stores and
+ * tallies are left alone.  The call returns when the work on `stream` (a
+ * cudaStream_t, or NULL) has finished.
+ *
+ * Allocates nothing: the fission products handed from one pass to the next
+ * live in a fixed array inside the library, two stores of
+ * QSG_NOALLOC_MAX_PRODUCTS particles (QSG_NOALLOC_SCRATCH_BYTES in all), which
+ * every GPU that loads libqsg.so holds until the process exits.  A pass that
+ * makes more fission products than that, or a census beyond census_capacity,
+ * ends the call with QSG_ERR_CAPACITY and a message naming the limit; the
+ * outputs of that call are then incomplete.  The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress), so make that first
+ * call before any stream capture begins.  Every call on a device shares the
+ * one array, and each call clears the parts that must start at zero: calls
+ * whose work overlaps on the GPU (other threads, other streams) race on it and
+ * must be serialised by the caller. */
+#define QSG_NOALLOC_MAX_PRODUCTS 32768
+#define QSG_NOALLOC_SCRATCH_BYTES 8913664u /* 256 + 2 x 4456704 */
+int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* particles, uint64_t n,
+                                QsgParticleSoA* census, uint64_t census_capacity, uint64_t* n_census,
+                                double* flux, uint64_t* balance, void* stream);
+
 /* Device pointers of the stores, for zero-copy callers (e.g. torch). */
 int qsg_processing_view(QsgHandle* h, QsgParticleSoA* device_view, uint64_t* n);
 int qsg_processed_view(QsgHandle* h, QsgParticleSoA* device_view, uint64_t* n);

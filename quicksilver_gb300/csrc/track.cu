@@ -1402,3 +1402,198 @@ extern "C" int qsg_processed_view(QsgHandle* h, QsgParticleSoA* v, uint64_t* n)
     *n = c;
     return QSG_OK;
 }
+
+// ------------------------------------------------------------------------
+// Tracking without allocation (qsg_track_particles_noalloc).
+//
+// Callers whose device memory all belongs to a pool allocator (PyTorch's
+// caching allocator, an application arena) cannot have this library call
+// cudaMalloc or cudaFree while they run: the allocation may fail or escape the
+// pool's accounting, and cudaFree synchronises the whole device.  For them
+// the fission products that one tracking pass hands to the next live in the
+// fixed array below instead of the handle's growable stores.  Layout: a
+// 256-byte header of 64-bit words (0: work cursor, 1: input count, 2: census
+// count, 3: device error flags) and two particle stores of
+// QSG_NOALLOC_MAX_PRODUCTS particles each, carved like the handle's stores.
+// The array is shared by every call on a device and keeps what the last call
+// left in it; each call clears the header and the store counts first.
+
+namespace qsg {
+namespace {
+
+constexpr size_t noalloc_field_bytes(size_t esz)
+{
+    return ((size_t)QSG_NOALLOC_MAX_PRODUCTS * esz + 255) & ~size_t(255);
+}
+constexpr size_t kNoallocHeaderBytes = 256;
+// per store: its count word (256 bytes), 14 eight-byte and 6 four-byte fields
+constexpr size_t kNoallocStoreBytes = 256 + 14 * noalloc_field_bytes(8) + 6 * noalloc_field_bytes(4);
+static_assert(kNoallocHeaderBytes + 2 * kNoallocStoreBytes == QSG_NOALLOC_SCRATCH_BYTES,
+              "QSG_NOALLOC_SCRATCH_BYTES does not match the scratch layout");
+
+}  // namespace
+
+}  // namespace qsg
+
+// The scratch itself.  In host code this name only stands in for the symbol;
+// its device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char qsg_noalloc_scratch[QSG_NOALLOC_SCRATCH_BYTES];
+
+namespace qsg {
+namespace {
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+unsigned char* g_noalloc_address[kNoallocMaxDevices] = {};
+
+// Device address of the scratch on `device`, which must be current.  The first
+// call on each device performs the lookup; later calls reuse it.
+int noalloc_scratch_address(int device, unsigned char** out)
+{
+    if (device < 0 || device >= kNoallocMaxDevices)
+        return fail(QSG_ERR_INVALID, "qsg_track_particles_noalloc: device %d outside 0..%d", device,
+                    kNoallocMaxDevices - 1);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_address[device]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, qsg_noalloc_scratch);
+        if (e != cudaSuccess || !ptr)
+            return fail(QSG_ERR_CUDA, "qsg_track_particles_noalloc: cudaGetSymbolAddress of the scratch array on "
+                        "device %d failed: %s", device, cudaGetErrorString(e));
+        g_noalloc_address[device] = static_cast<unsigned char*>(ptr);
+    }
+    *out = g_noalloc_address[device];
+    return QSG_OK;
+}
+
+// Zero the header and both store counts, then set the input count.
+__global__ void noalloc_begin_kernel(unsigned long long* header, unsigned long long* count0,
+                                     unsigned long long* count1, unsigned long long n)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        for (int k = 0; k < (int)(kNoallocHeaderBytes / 8); k++) header[k] = 0;
+        header[1] = n;
+        *count0 = 0;
+        *count1 = 0;
+    }
+}
+
+DevStore noalloc_caller_store(const QsgParticleSoA* s, uint64_t capacity, unsigned long long* count)
+{
+    DevStore v{};
+    v.x = s->x; v.y = s->y; v.z = s->z; v.vx = s->vx; v.vy = s->vy; v.vz = s->vz;
+    v.kinetic_energy = s->kinetic_energy; v.weight = s->weight; v.time_to_census = s->time_to_census;
+    v.age = s->age; v.num_mean_free_paths = s->num_mean_free_paths; v.num_segments = s->num_segments;
+    v.seed = s->random_number_seed; v.identifier = s->identifier;
+    v.last_event = s->last_event; v.num_collisions = s->num_collisions; v.breed = s->breed;
+    v.species = s->species; v.domain = s->domain; v.cell = s->cell;
+    v.count = count;
+    v.capacity = capacity;
+    return v;
+}
+
+// The caller's arrays must be device memory of the handle's device (or
+// managed), aligned for their element type.
+int noalloc_check_pointer(const void* p, size_t align, int device, const char* what)
+{
+    if (!p) return fail(QSG_ERR_INVALID, "qsg_track_particles_noalloc: %s is null", what);
+    if (reinterpret_cast<uintptr_t>(p) % align)
+        return fail(QSG_ERR_INVALID, "qsg_track_particles_noalloc: %s is not %zu-byte aligned", what, align);
+    cudaPointerAttributes a{};
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(QSG_ERR_INVALID, "qsg_track_particles_noalloc: %s is not a CUDA pointer (%s)", what,
+                    cudaGetErrorString(e));
+    }
+    if (a.type == cudaMemoryTypeManaged) return QSG_OK;
+    if (a.type != cudaMemoryTypeDevice || a.device != device)
+        return fail(QSG_ERR_INVALID, "qsg_track_particles_noalloc: %s must be device memory on device %d", what,
+                    device);
+    return QSG_OK;
+}
+
+int noalloc_check_soa(const QsgParticleSoA* s, int device, const char* which)
+{
+    if (!s) return fail(QSG_ERR_INVALID, "qsg_track_particles_noalloc: %s is null", which);
+    const void* p8[14] = {s->x, s->y, s->z, s->vx, s->vy, s->vz, s->kinetic_energy, s->weight,
+                          s->time_to_census, s->age, s->num_mean_free_paths, s->num_segments,
+                          s->random_number_seed, s->identifier};
+    const void* p4[6] = {s->last_event, s->num_collisions, s->breed, s->species, s->domain, s->cell};
+    int st;
+    for (const void* p : p8)
+        if ((st = noalloc_check_pointer(p, 8, device, which))) return st;
+    for (const void* p : p4)
+        if ((st = noalloc_check_pointer(p, 4, device, which))) return st;
+    return QSG_OK;
+}
+
+}  // namespace
+}  // namespace qsg
+
+extern "C" int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* particles, uint64_t n,
+                                           QsgParticleSoA* census, uint64_t census_capacity, uint64_t* n_census,
+                                           double* flux, uint64_t* balance, void* stream)
+{
+    QSG_API_BEGIN
+    if (!h || !n_census) return fail(QSG_ERR_INVALID, "qsg_track_particles_noalloc: null handle or n_census");
+    int st = set_device(h);
+    if (st) return st;
+    if ((st = noalloc_check_soa(particles, h->device, "particles")) ||
+        (st = noalloc_check_soa(census, h->device, "census")) ||
+        (st = noalloc_check_pointer(flux, 8, h->device, "flux")) ||
+        (st = noalloc_check_pointer(balance, 8, h->device, "balance")))
+        return st;
+    unsigned char* scratch = nullptr;
+    if ((st = noalloc_scratch_address(h->device, &scratch))) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    unsigned long long* header = reinterpret_cast<unsigned long long*>(scratch);
+    unsigned long long* cursor = header + 0;
+    DevStore prod[2] = {Store::carve(scratch + kNoallocHeaderBytes, QSG_NOALLOC_MAX_PRODUCTS),
+                        Store::carve(scratch + kNoallocHeaderBytes + kNoallocStoreBytes, QSG_NOALLOC_MAX_PRODUCTS)};
+    const DevStore in0 = noalloc_caller_store(particles, n, header + 1);
+    const DevStore out = noalloc_caller_store(census, census_capacity, header + 2);
+    DevTally tally = tally_view(h);
+    tally.flux = flux;
+    tally.balance = reinterpret_cast<unsigned long long*>(balance);
+    tally.error_flags = reinterpret_cast<unsigned int*>(header + 3);
+    tally.flux_replicas = 1;
+    tally.balance_replicas = 1;
+
+    noalloc_begin_kernel<<<1, 1, 0, s>>>(header, prod[0].count, prod[1].count, (unsigned long long)n);
+    QSG_CUDA(cudaGetLastError());
+    const size_t smem = track_smem_bytes(h);
+    unsigned long long remaining = n, counts[3] = {0, 0, 0};
+    for (int pass = 0; remaining != 0; pass++) {
+        const DevStore in = pass == 0 ? in0 : prod[(pass + 1) & 1];
+        const DevStore extra = prod[pass & 1];
+        QSG_CUDA(cudaMemsetAsync(extra.count, 0, sizeof(unsigned long long), s));
+        QSG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s));
+        if (h->block_size == 256)
+            track_kernel<256><<<h->track_blocks, 256, smem, s>>>(h->tables, tally, in, out, extra, cursor);
+        else
+            track_kernel<128><<<h->track_blocks, 128, smem, s>>>(h->tables, tally, in, out, extra, cursor);
+        QSG_CUDA(cudaGetLastError());
+        // products of this pass, census so far, device flags
+        QSG_CUDA(cudaMemcpyAsync(&counts[0], extra.count, 8, cudaMemcpyDeviceToHost, s));
+        QSG_CUDA(cudaMemcpyAsync(&counts[1], header + 2, 8, cudaMemcpyDeviceToHost, s));
+        QSG_CUDA(cudaMemcpyAsync(&counts[2], header + 3, 8, cudaMemcpyDeviceToHost, s));
+        QSG_CUDA(cudaStreamSynchronize(s));
+        const unsigned int flags = (unsigned int)counts[2];
+        if (counts[0] > (unsigned long long)QSG_NOALLOC_MAX_PRODUCTS)
+            return fail(QSG_ERR_CAPACITY, "qsg_track_particles_noalloc: tracking pass %d made %llu fission products; "
+                        "the no-allocation scratch holds at most %d per pass (QSG_NOALLOC_MAX_PRODUCTS) -- "
+                        "outputs are incomplete", pass, counts[0], QSG_NOALLOC_MAX_PRODUCTS);
+        if (counts[1] > census_capacity)
+            return fail(QSG_ERR_CAPACITY, "qsg_track_particles_noalloc: %llu census particles exceed "
+                        "census_capacity %llu -- outputs are incomplete", counts[1],
+                        (unsigned long long)census_capacity);
+        if (flags) return fail(QSG_ERR_DEVICE, "tracking kernel raised device flags 0x%x", flags);
+        remaining = counts[0];
+    }
+    QSG_CUDA(cudaStreamSynchronize(s));
+    *n_census = counts[1];
+    return QSG_OK;
+    QSG_API_END
+}
