@@ -44,7 +44,7 @@ sys.path.insert(0, str(ROOT))
 DECK = ROOT / "quicksilver_gb300" / "decks" / "config2.inp"
 WORKLOAD = ("config2: 40^3-cell 40 cm cube, 3 materials in spherical shells (r=8, 16 cm), 2 isotopes x "
             "3 reactions each, polynomial cross sections, 230 groups, 1e6 particles, FP64")
-METRIC = "segments/s per cycle (cycleTracking phase)"
+METRIC = "segments/s per cycle on 1 GB300; batched+adjoint vs plain at matched tally error"
 B_ALG_PER_SEGMENT = 288          # algorithmic HBM bytes per segment (136-B record read+write + 16-B flux RMW)
 PROFILE_SUMMARY = ROOT / "profiles" / "track_kernel_config2.md"
 
@@ -153,6 +153,164 @@ def cpu_port_rate(deck_path: Path, cycles: int, threads: int):
     return seg / secs, seg, secs
 
 
+def _sync():
+    import torch
+    torch.cuda.synchronize()
+
+
+def measure_batched(tune_space=None):
+    """Batched form on the uneven ensemble (64 problems, mesh edge in
+    {8..48}, 1e4-2e6 particles, 10 cycles): one persistent launch per pass
+    for all problems, cycles replayed from CUDA graphs, kernel shape from the
+    autotuner -- against the plain path run problem by problem
+    (MonteCarlo.run: host-driven cycles, one handle per problem).  Both runs
+    track the same histories (same per-problem seeds), so the tally standard
+    errors are equal by construction; the balance counters are compared bit
+    for bit."""
+    from quicksilver_gb300 import Deck
+    from quicksilver_gb300.autotune import autotune
+    from quicksilver_gb300.decks.make_decks import config3
+    from quicksilver_gb300.monte_carlo import BatchMonteCarlo, MonteCarlo, seed_offset
+    texts = config3()
+    decks = [Deck.from_string(t) for t in texts]
+    problems = [d.build() for d in decks]
+    offs = [seed_offset(d.simulation.seed) for d in decks]
+    cycles = decks[0].simulation.n_steps
+    t0 = time.perf_counter()
+    space = tune_space or {"block_size": (128, 256), "collision_batch": (16,), "queue_chunk": (1, 4),
+                           "flux_replicas": (1,)}
+    best = autotune(texts, scale=0.1, cycles=1, warmup=1, cache_path=None, space=space, problems=problems)
+    tune_s = time.perf_counter() - t0
+    bmc = BatchMonteCarlo(decks, problems=problems, seed_offsets=offs, flux_replicas=best["flux_replicas"])
+    try:
+        bmc.tune(best["block_size"], best["collision_batch"], best["queue_chunk"])
+        bmc.run(1, use_graph=True)             # warm-up cycle (captures the graphs)
+        first = bmc.cycles
+        _sync()
+        t0 = time.perf_counter()
+        bmc.run_cycles(cycles, use_graph=True)
+        _sync()
+        t_batch = time.perf_counter() - t0
+        hb = bmc.history(first, cycles)
+        flags = bmc.device_status()
+    finally:
+        bmc.close()
+    # the plain path, problem by problem, from the same starting state (one warm-up cycle)
+    t_plain, seg_plain, same = 0.0, 0, True
+    for p, (d, hp, off) in enumerate(zip(decks, problems, offs)):
+        mc = MonteCarlo(d, problem=hp, seed_offset=off)
+        try:
+            mc.run(1)
+            _sync()
+            t0 = time.perf_counter()
+            h = mc.run(cycles)
+            _sync()
+            t_plain += time.perf_counter() - t0
+            seg_plain += h.segments()
+            same &= bool(np.array_equal(h.balance, hb.balance[:, p, :]))
+        finally:
+            mc.close()
+    seg_b = hb.segments()
+    for hp in problems:
+        hp.close()
+    return {"workload": "64 independent problems (mesh edge from {8,16,24,32,48} cm, 1e4-2e6 particles "
+                        "log-uniform, 1-3 materials, 230 groups), 10 cycles each after 1 warm-up cycle",
+            "batched_segments_per_s": seg_b / t_batch, "batched_s": t_batch,
+            "plain_problem_by_problem_segments_per_s": seg_plain / t_plain, "plain_s": t_plain,
+            "speedup_at_equal_tally_error": (seg_b / t_batch) / (seg_plain / t_plain),
+            "segments": seg_b, "balance_bit_exact_vs_plain": same, "device_flags": flags,
+            "tuning": {k: best[k] for k in ("block_size", "collision_batch", "queue_chunk", "flux_replicas")},
+            "tune_s": tune_s, "timing": "wall clock, whole cycles, synchronised"}
+
+
+def measure_adjoint(replicas=6):
+    """Differentiated form on the differentiated homogeneous-box problem
+    (config4: 3 materials, escape boundaries, 1e6 particles, 20 cycles,
+    12 parameters = 3 materials x {scatter, absorption} x 2 bands split at
+    1 MeV).  One sensitivity run gives d(total flux)/dtheta and
+    d(leakage)/dtheta for all 12 parameters; the plain kernel needs a central
+    difference per parameter (2 runs each, common random numbers).  Replica
+    variances (distinct seed offsets) of both estimators give the number of
+    plain runs needed to match the sensitivity run's standard error:
+    speedup = 2 K median_j(var_FD_j / var_score_j) T_plain / T_sens over the
+    24 components j.  The central differences use step 1e-2 (lower variance
+    than 1e-4, so the comparison favours the plain path); the step-1e-4
+    variance ratio is reported beside it."""
+    from quicksilver_gb300 import Deck
+    from quicksilver_gb300.monte_carlo import MonteCarlo, seed_offset
+    from quicksilver_gb300.sensitivity import Param, band_params, scaled_problem
+    deck = Deck.from_file(ROOT / "quicksilver_gb300" / "decks" / "config4.inp")
+    hp0 = deck.build()
+    params = band_params(hp0.array("energies"), hp0.num_materials)
+    hp0.close()
+    K = len(params)
+
+    def one_run(prms, off, sens=True):
+        problem = scaled_problem(deck, prms)
+        mc = MonteCarlo(deck, problem=problem, seed_offset=off)
+        try:
+            if sens:
+                mc.tracker.enable_sensitivity(prms)
+            _sync()
+            t0 = time.perf_counter()
+            h = mc.run()
+            _sync()
+            dt = time.perf_counter() - t0
+            out = mc.tracker.read_sensitivity() if sens else None
+            return out, dt, h.segments()
+        finally:
+            mc.close()
+            problem.close()
+
+    steps = (1e-2, 1e-4)
+    lr = np.zeros((replicas, 2, K))
+    fd = {h: np.zeros((replicas, 2, K)) for h in steps}
+    t_sens = t_plain = 0.0
+    seg_sens = seg_plain = 0
+    one_run(params, 1, sens=False)   # warm-up (module load, first allocations)
+    for i in range(replicas):
+        off = seed_offset(4000 + i)
+        out, dt, seg = one_run(params, off)
+        t_sens += dt
+        seg_sens += seg
+        lr[i, 0] = out["dflux"].sum(axis=0)
+        lr[i, 1] = out["dleak"][0]
+        _, dt, seg = one_run(params, off, sens=False)
+        t_plain += dt
+        seg_plain += seg
+        for h in steps:
+            for k in range(K):
+                vals = []
+                for sgn in (1.0, -1.0):
+                    sh = [p if j != k else Param(p.material, p.reaction, p.group_lo, p.group_hi, 1.0 + sgn * h)
+                          for j, p in enumerate(params)]
+                    o, _, _ = one_run(sh, off)
+                    vals.append((o["flux_cell"].sum(), o["leak"][0]))
+                fd[h][i, 0, k] = (vals[0][0] - vals[1][0]) / (2 * h)
+                fd[h][i, 1, k] = (vals[0][1] - vals[1][1]) / (2 * h)
+    var_lr = lr.var(axis=0, ddof=1).ravel()
+    res = {}
+    for h in steps:
+        var_fd = fd[h].var(axis=0, ddof=1).ravel()
+        ok = var_lr > 0
+        ratio = var_fd[ok] / var_lr[ok]
+        res[h] = (float(np.median(ratio)), float(ratio.min()), float(ratio.max()))
+    rate_plain = seg_plain / t_plain
+    rate_sens = seg_sens / t_sens
+    speedup = 2 * K * res[1e-2][0] * (t_plain / t_sens)
+    return {"workload": "config4: 10^3 cells, 10 cm box, 3 materials (spheres r=2, 4 cm), escape boundaries, "
+                        "230 groups, 1e6 particles, 20 cycles; 12 scale parameters",
+            "params": K, "replicas": replicas,
+            "plain_segments_per_s": rate_plain, "sens_segments_per_s": rate_sens,
+            "sens_time_over_plain": t_sens / t_plain,
+            "fd_step": 1e-2, "variance_ratio_fd_over_score": {"median": res[1e-2][0], "min": res[1e-2][1],
+                                                              "max": res[1e-2][2]},
+            "variance_ratio_fd_step_1e-4": {"median": res[1e-4][0], "min": res[1e-4][1], "max": res[1e-4][2]},
+            "speedup_at_equal_tally_error": speedup,
+            "effective_segments_per_s": speedup * rate_plain,
+            "timing": "wall clock of MonteCarlo.run (20 whole cycles), synchronised; handle set-up excluded"}
+
+
 def run_reference_arm(args, world, rank):
     """--impl reference: the CPU port of the reference algorithm on the host cores."""
     if rank != 0:
@@ -200,6 +358,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--flux-replicas", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched and differentiated forms")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()
@@ -333,6 +492,8 @@ def main():
         "device_flags": flags,
         "clocks": clocks.summary(),
     }
+    if not args.no_forms:
+        line["forms"] = {"batched": measure_batched(), "adjoint": measure_adjoint()}
     if not args.no_cpu_baseline:
         rate, seg, secs = cpu_port_rate(DECK, 2, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": rate, "unit": "segments/s", "cores": os.cpu_count(), "kind": "port",

@@ -237,6 +237,51 @@ int qsg_cycle_history(QsgHandle* h, uint64_t first, uint64_t n, uint64_t* balanc
 /* Copy the processing store (e.g. after qsg_cycle_init) to host arrays. */
 int qsg_get_processing(QsgHandle* h, QsgParticleSoA* host, uint64_t cap, uint64_t* n_out);
 
+/* ---- sensitivities (adjoint / differential-operator tallies) ------------- */
+#define QSG_MAX_PARAMS 32
+/* K scale parameters theta_k.  Entry e says that theta[param[e]] multiplies
+ * the microscopic cross sections of every reaction of type reaction[e]
+ * (QSG_REACT_*) of every isotope of material material[e] (the handle's
+ * material index: for a batch, problem p's materials start at
+ * qsg_material_offsets()[p]) in groups [group_lo[e], group_hi[e]).  One
+ * parameter may have several entries (e.g. the same physical parameter in
+ * every problem of a batch); entries must not overlap.  The tables given to
+ * qsg_create must already be scaled by theta.
+ *
+ * Each history then carries a score vector S (d log-probability / d theta):
+ * a flight of length l in a cell adds -l dSigma_t/dtheta; a collision adds
+ * d log Sigma_r / dtheta of the selected reaction; fission products, census
+ * and population-control copies inherit their parent's S.  Tallied:
+ *   flux_cell[cell]  += l w,  dflux[cell][k] += l w (S_k + [flight ends in a collision] dSigma_t/dtheta_k / Sigma_t)
+ *   leak[problem]    += w at escape,  dleak[problem][k] += w S_k at escape
+ * (group-summed per-cell flux, leakage and their derivatives).  Forward
+ * tracking is unchanged, bit for bit.  No counterpart in the reference, which
+ * has no sensitivity tallies. */
+typedef struct QsgSensitivity {
+    int32_t num_params;          /* K (0 switches sensitivities off)          */
+    const double* theta;         /* [K] value of each parameter (> 0)         */
+    int32_t num_entries;
+    const int32_t* param;        /* [num_entries] parameter index, 0..K-1     */
+    const int32_t* material;     /* [num_entries]                             */
+    const int32_t* reaction;     /* [num_entries] QSG_REACT_*                 */
+    const int32_t* group_lo;     /* [num_entries]                             */
+    const int32_t* group_hi;     /* [num_entries]                             */
+} QsgSensitivity;
+/* num_params == 0 switches the sensitivity tallies off.  Enabling (re)sizes
+ * the particle stores to carry K scores per particle (particles already
+ * stored keep their records and get zero scores) and zeroes the tallies. */
+int qsg_enable_sensitivity(QsgHandle* h, const QsgSensitivity* s);
+/* Group-summed track-length flux flux_cell [num_cells] (the forward value
+ * whose derivatives dflux holds), dflux [num_cells][K], leak [problems],
+ * dleak [problems][K] (any may be NULL), accumulated over every tracking call
+ * since the last qsg_reset_sensitivity / qsg_enable_sensitivity (they are not
+ * cleared by qsg_cycle_finalize).  qsg_track_particles_noalloc tallies no
+ * sensitivities. */
+int qsg_read_sensitivity(QsgHandle* h, double* flux_cell, double* dflux, double* leak, double* dleak);
+int qsg_reset_sensitivity(QsgHandle* h);
+/* [problems + 1] offsets of each problem's materials in the handle. */
+int qsg_material_offsets(QsgHandle* h, int32_t* offsets);
+
 /* ---- batches of independent problems ------------------------------------ */
 /* One handle over n independent problems (each a single domain; they must
  * share the energy grid, the time step and the facet convention).  Every

@@ -25,6 +25,26 @@ PARTICLE_DTYPE = np.dtype([
     ("domain", "<i4"), ("cell", "<i4"),
 ])
 
+MAX_PARAMS = 32
+
+
+class OracleSens(C.Structure):
+    """Mirror of OracleSens (qs_oracle.h)."""
+    _fields_ = [("K", C.c_int32), ("material", C.c_int32 * MAX_PARAMS), ("reaction", C.c_int32 * MAX_PARAMS),
+                ("group_lo", C.c_int32 * MAX_PARAMS), ("group_hi", C.c_int32 * MAX_PARAMS),
+                ("theta", C.c_double * MAX_PARAMS), ("flux_cell", C.POINTER(C.c_double)),
+                ("dflux", C.POINTER(C.c_double)), ("leak", C.POINTER(C.c_double)), ("dleak", C.POINTER(C.c_double))]
+
+
+def make_sens(params) -> OracleSens:
+    """params: sequence of (material, reaction type, group_lo, group_hi, theta)."""
+    s = OracleSens()
+    s.K = len(params)
+    for k, (m, r, lo, hi, th) in enumerate(params):
+        s.material[k], s.reaction[k], s.group_lo[k], s.group_hi[k], s.theta[k] = m, r, lo, hi, th
+    return s
+
+
 _lib = None
 
 
@@ -67,6 +87,16 @@ def lib() -> C.CDLL:
         h.oracle_track.argtypes = [vp, vp, C.c_uint64, vp, C.c_uint64, C.POINTER(C.c_uint64),
                                    C.POINTER(C.c_uint64), C.POINTER(C.c_double), C.c_int]
         h.oracle_track.restype = C.c_int
+        h.oracle_track_sens.argtypes = [vp, C.POINTER(OracleSens), vp, vp, C.c_uint64, vp, vp, C.c_uint64,
+                                        C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_double), C.c_int]
+        h.oracle_track_sens.restype = C.c_int
+        h.oracle_enable_sensitivity.argtypes = [vp, C.POINTER(OracleSens)]
+        h.oracle_enable_sensitivity.restype = C.c_int
+        h.oracle_read_sensitivity.argtypes = [vp, vp, vp, vp, vp]
+        h.oracle_read_sensitivity.restype = C.c_int
+        for name in ("oracle_processing_scores", "oracle_processed_scores"):
+            getattr(h, name).argtypes = [vp]
+            getattr(h, name).restype = vp
         h.oracle_rng_sample.argtypes = [C.POINTER(C.c_uint64)]
         h.oracle_rng_sample.restype = C.c_double
         h.oracle_rng_spawn.argtypes = [C.POINTER(C.c_uint64)]
@@ -143,6 +173,37 @@ class OracleRun:
     def warnings(self) -> int:
         return int(lib().oracle_warning_count(self._h))
 
+    def enable_sensitivity(self, params):
+        """params: (material, reaction type, group_lo, group_hi, theta) per parameter."""
+        self._sens = make_sens(params)
+        if lib().oracle_enable_sensitivity(self._h, C.byref(self._sens)):
+            raise RuntimeError("oracle_enable_sensitivity failed (call it before the first cycle)")
+        self.K = len(params)
+
+    def read_sensitivity(self):
+        """(flux_cell [C], dflux [C, K], leak, dleak [K]) accumulated over all cycles."""
+        fc = np.zeros(self.num_cells)
+        df = np.zeros(self.num_cells * self.K)
+        lk = np.zeros(1)
+        dl = np.zeros(self.K)
+        if lib().oracle_read_sensitivity(self._h, fc.ctypes.data, df.ctypes.data, lk.ctypes.data, dl.ctypes.data):
+            raise RuntimeError("oracle_read_sensitivity failed")
+        return fc, df.reshape(self.num_cells, self.K), float(lk[0]), dl
+
+    def processing_scores(self) -> np.ndarray:
+        n = lib().oracle_num_processing(self._h)
+        if n == 0:
+            return np.zeros((0, self.K))
+        buf = (C.c_double * (n * self.K)).from_address(lib().oracle_processing_scores(self._h))
+        return np.frombuffer(buf, dtype=np.float64).copy().reshape(n, self.K)
+
+    def processed_scores(self) -> np.ndarray:
+        n = lib().oracle_num_processed(self._h)
+        if n == 0:
+            return np.zeros((0, self.K))
+        buf = (C.c_double * (n * self.K)).from_address(lib().oracle_processed_scores(self._h))
+        return np.frombuffer(buf, dtype=np.float64).copy().reshape(n, self.K)
+
 
 def track(problem_ptr, num_cells: int, num_groups: int, particles: np.ndarray, nthreads: int = 0):
     """One-shot tracking: returns (census records, balance[13], flux[C, G])."""
@@ -158,6 +219,44 @@ def track(problem_ptr, num_cells: int, num_groups: int, particles: np.ndarray, n
     if st:
         raise RuntimeError(f"oracle_track failed ({st})")
     return census[: n_census.value].copy(), np.array(bal, dtype=np.uint64), flux.reshape(num_cells, num_groups)
+
+
+def track_sens(problem_ptr, num_cells: int, num_groups: int, particles: np.ndarray, params, scores=None,
+               nthreads: int = 0):
+    """One-shot tracking with sensitivity scores.  Returns a dict: census,
+    census_scores [n, K], balance[13], flux[C, G], flux_cell [C], dflux [C, K],
+    leak, dleak [K]."""
+    recs = np.ascontiguousarray(particles, dtype=PARTICLE_DTYPE)
+    n = len(recs)
+    K = len(params)
+    sc_in = None if scores is None else np.ascontiguousarray(scores, dtype=np.float64).reshape(n, K)
+    cap = max(4 * n + 16, 1024)
+    while True:   # a census larger than cap: run again with room for it (outputs start from zero)
+        sens = make_sens(params)
+        fc, df, lk, dl = np.zeros(num_cells), np.zeros(num_cells * K), np.zeros(1), np.zeros(K)
+        sens.flux_cell = fc.ctypes.data_as(C.POINTER(C.c_double))
+        sens.dflux = df.ctypes.data_as(C.POINTER(C.c_double))
+        sens.leak = lk.ctypes.data_as(C.POINTER(C.c_double))
+        sens.dleak = dl.ctypes.data_as(C.POINTER(C.c_double))
+        census = np.empty(cap, dtype=PARTICLE_DTYPE)
+        census_sc = np.empty((cap, K))
+        bal = (C.c_uint64 * 13)()
+        flux = np.zeros(num_cells * num_groups, dtype=np.float64)
+        n_census = C.c_uint64(0)
+        st = lib().oracle_track_sens(problem_ptr, C.byref(sens), recs.ctypes.data if n else None,
+                                     sc_in.ctypes.data if sc_in is not None and n else None, n, census.ctypes.data,
+                                     census_sc.ctypes.data, cap, C.byref(n_census), bal,
+                                     flux.ctypes.data_as(C.POINTER(C.c_double)), nthreads)
+        if st == -3:
+            cap = n_census.value + 16
+            continue
+        if st:
+            raise RuntimeError(f"oracle_track_sens failed ({st})")
+        break
+    m = n_census.value
+    return {"census": census[:m].copy(), "census_scores": census_sc[:m].copy(),
+            "balance": np.array(bal, dtype=np.uint64), "flux": flux.reshape(num_cells, num_groups),
+            "flux_cell": fc, "dflux": df.reshape(num_cells, K), "leak": float(lk[0]), "dleak": dl}
 
 
 def rng_sample(seed: int):

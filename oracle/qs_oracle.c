@@ -69,6 +69,7 @@ typedef struct WorkParticle {
     double num_mean_free_paths, mean_free_path, segment_path_length, num_segments;
     uint64_t seed, identifier;
     int32_t last_event, num_collisions, species, breed, group, domain, cell, facet;
+    double S[QSG_MAX_PARAMS];   /* sensitivity scores (when enabled) */
 } WorkParticle;
 
 typedef struct Counters {
@@ -78,6 +79,8 @@ typedef struct Counters {
 typedef struct Store {
     OracleParticle* p;
     uint64_t n, cap;
+    double* sc;              /* [cap*K] sensitivity scores, row per particle (K > 0) */
+    int K;
 } Store;
 
 typedef struct TrackCtx {
@@ -88,6 +91,7 @@ typedef struct TrackCtx {
     Store* extra;
     uint64_t* warnings;
     int overflow;
+    OracleSens* sens;        /* NULL: no sensitivity scores */
 } TrackCtx;
 
 static void atomic_inc(uint64_t* a, uint64_t v)
@@ -110,19 +114,34 @@ static int store_reserve(Store* s, uint64_t want)
     OracleParticle* np = (OracleParticle*)realloc(s->p, nc * sizeof(OracleParticle));
     if (!np) return -1;
     s->p = np;
+    if (s->K > 0) {
+        double* ns = (double*)realloc(s->sc, nc * (size_t)s->K * sizeof(double));
+        if (!ns) return -1;
+        s->sc = ns;
+    }
     s->cap = nc;
     return 0;
 }
 
+/* Scores of slot i of s: copied from sc (NULL: zeros). */
+static void store_set_scores(Store* s, uint64_t i, const double* sc)
+{
+    if (s->K <= 0) return;
+    if (sc) memcpy(s->sc + i * (size_t)s->K, sc, (size_t)s->K * sizeof(double));
+    else memset(s->sc + i * (size_t)s->K, 0, (size_t)s->K * sizeof(double));
+}
+
 /* Append from inside a parallel region: capacity is reserved beforehand by
  * the caller; an overflow is reported, never written. */
-static void store_push_atomic(TrackCtx* ctx, Store* s, const OracleParticle* p)
+static void store_push_atomic(TrackCtx* ctx, Store* s, const OracleParticle* p, const double* sc)
 {
     uint64_t idx;
 #pragma omp atomic capture
     idx = s->n++;
-    if (idx < s->cap) s->p[idx] = *p;
-    else {
+    if (idx < s->cap) {
+        s->p[idx] = *p;
+        store_set_scores(s, idx, sc);
+    } else {
 #pragma omp atomic write
         ctx->overflow = 1;
     }
@@ -400,6 +419,64 @@ static int segment_outcome(TrackCtx* ctx, WorkParticle* w)
     return outcome;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Sensitivity scores (no counterpart in the reference; what the CUDA
+ * library's qsg_enable_sensitivity tallies).  Parameter of (material,
+ * reaction type, group), or -1. */
+static int sens_param(const OracleSens* se, int mat, int type, int group)
+{
+    for (int k = 0; k < se->K; k++)
+        if (se->material[k] == mat && se->reaction[k] == type && group >= se->group_lo[k] && group < se->group_hi[k])
+            return k;
+    return -1;
+}
+
+/* dSigma_t/dtheta_k contributed by reaction type `type` in this cell and
+ * group: the macroscopic cross sections af * nd * xs of that type summed in
+ * isotope / reaction order (MacroscopicCrossSection.cc:14-48), over theta_k. */
+static double sens_dsig(const QsgProblem* pb, const OracleSens* se, int k, int cell, int group, int type)
+{
+    const int G = pb->num_groups;
+    int mat = pb->cell_material[cell];
+    double nd = pb->cell_number_density[cell];
+    double sum = 0.0;
+    for (int j = pb->material_isotope_offset[mat]; j < pb->material_isotope_offset[mat + 1]; j++) {
+        int iso = pb->material_isotope_gid[j];
+        double af = pb->material_atom_fraction[j];
+        for (int r = pb->isotope_reaction_offset[iso]; r < pb->isotope_reaction_offset[iso + 1]; r++)
+            if (pb->reaction_type[r] == type) sum += af * nd * pb->reaction_xs[(int64_t)r * G + group];
+    }
+    return sum / se->theta[k];
+}
+
+/* One flight of length l through cell / group: scores gain -l dSigma_t/dtheta;
+ * the flight's track-length flux l w is tallied with its full score
+ * l w (S_k + [collision] dSigma_t/dtheta_k / Sigma_t). */
+static void sens_segment(TrackCtx* ctx, WorkParticle* w, int collided)
+{
+    OracleSens* se = ctx->sens;
+    const QsgProblem* pb = ctx->pb;
+    const double l = w->segment_path_length;
+    if (l == 0.0) return;
+    int mat = pb->cell_material[w->cell];
+    int pk[3];
+    double pd[3];
+    for (int j = 0; j < 3; j++) {
+        pk[j] = sens_param(se, mat, j + 1, w->group);
+        pd[j] = pk[j] >= 0 ? sens_dsig(pb, se, pk[j], w->cell, w->group, j + 1) : 0.0;
+        if (pk[j] >= 0) w->S[pk[j]] -= l * pd[j];
+    }
+    const double lw = l * w->weight;
+    atomic_add_d(&se->flux_cell[w->cell], lw);
+    for (int k = 0; k < se->K; k++) {
+        double v = w->S[k];
+        if (collided)
+            for (int j = 0; j < 3; j++)
+                if (pk[j] == k) v += pd[j] * w->mean_free_path;
+        if (v != 0.0) atomic_add_d(&se->dflux[(int64_t)w->cell * se->K + k], lw * v);
+    }
+}
+
 /* DirectionCosine::Rotate3DVector, DirectionCosine.hh:122-147. */
 static void rotate3d(WorkParticle* w, double sin_Theta, double cos_Theta, double sin_Phi, double cos_Phi)
 {
@@ -475,6 +552,11 @@ static int collision_event(TrackCtx* ctx, WorkParticle* w)
     int n_out = 0;
     double mass = pb->material_mass[mat];
     int type = pb->reaction_type[sel_r];
+    if (ctx->sens) {
+        /* d log Sigma_r / dtheta of the selected reaction, in the incoming group */
+        int k = sens_param(ctx->sens, mat, type, w->group);
+        if (k >= 0) w->S[k] += 1.0 / ctx->sens->theta[k];
+    }
     switch (type) {
     case QSG_REACT_SCATTER: {
         n_out = 1;
@@ -517,13 +599,13 @@ static int collision_event(TrackCtx* ctx, WorkParticle* w)
         update_trajectory(energy_out[s], angle_out[s], &sec);
         OracleParticle b;
         to_base(&sec, &b);
-        store_push_atomic(ctx, ctx->extra, &b);
+        store_push_atomic(ctx, ctx->extra, &b, sec.S);
     }
     update_trajectory(energy_out[0], angle_out[0], w);
     if (n_out > 1) {
         OracleParticle b;
         to_base(w, &b);
-        store_push_atomic(ctx, ctx->extra, &b);
+        store_push_atomic(ctx, ctx->extra, &b, w->S);
     }
     w->group = energy_group(pb, w->kinetic_energy);
     return n_out == 1;
@@ -547,14 +629,17 @@ static void reflect_particle(const QsgProblem* pb, WorkParticle* w)
 }
 
 /* CycleTrackingGuts + CycleTrackingFunction, CycleTracking.cc:14-120. */
-static void track_one(TrackCtx* ctx, const OracleParticle* in)
+static void track_one(TrackCtx* ctx, const OracleParticle* in, const double* in_scores)
 {
     const QsgProblem* pb = ctx->pb;
     WorkParticle w;
     load_particle(pb, in, &w, ctx->warnings);
+    if (ctx->sens && in_scores) memcpy(w.S, in_scores, (size_t)ctx->sens->K * sizeof(double));
     int keep;
     do {
+        if (ctx->sens) w.segment_path_length = 0.0;   /* a segment that returns early moves nothing */
         int outcome = segment_outcome(ctx, &w);
+        if (ctx->sens) sens_segment(ctx, &w, outcome == OUT_COLLISION);
         atomic_inc(&ctx->bal->v[QSG_BAL_NUM_SEGMENTS], 1);
         w.num_segments += 1.;
         switch (outcome) {
@@ -574,6 +659,12 @@ static void track_one(TrackCtx* ctx, const OracleParticle* in)
                 keep = 1;
             } else if (ev == QSG_ADJ_BOUNDARY_ESCAPE) {
                 atomic_inc(&ctx->bal->v[QSG_BAL_ESCAPE], 1);
+                if (ctx->sens) {
+                    OracleSens* se = ctx->sens;
+                    atomic_add_d(&se->leak[0], w.weight);
+                    for (int k = 0; k < se->K; k++)
+                        if (w.S[k] != 0.0) atomic_add_d(&se->dleak[k], w.weight * w.S[k]);
+                }
                 w.last_event = QSG_EVENT_FACET_ESCAPE;
                 w.species = -1;
                 keep = 0;
@@ -593,7 +684,7 @@ static void track_one(TrackCtx* ctx, const OracleParticle* in)
         default: { /* census: ParticleVault::pushParticle, ParticleVault.hh:86-93 */
             OracleParticle b;
             to_base(&w, &b);
-            store_push_atomic(ctx, ctx->census, &b);
+            store_push_atomic(ctx, ctx->census, &b, w.S);
             atomic_inc(&ctx->bal->v[QSG_BAL_CENSUS], 1);
             keep = 0;
             break;
@@ -617,9 +708,9 @@ static void set_threads(int nthreads)
  * (ParticleVaultContainer::addExtraParticle, :340-349) become the next
  * processing list (cleanExtraVaults, :357-400) until none are left. */
 static int track_all(const QsgProblem* pb, Store* processing, Store* census, Counters* bal, double* flux,
-                     uint64_t* warnings, int nthreads)
+                     uint64_t* warnings, int nthreads, OracleSens* sens)
 {
-    Store extra = {0, 0, 0};
+    Store extra = {0, 0, 0, NULL, processing->K};
     set_threads(nthreads);
     int status = 0;
     while (processing->n > 0) {
@@ -627,10 +718,12 @@ static int track_all(const QsgProblem* pb, Store* processing, Store* census, Cou
         /* worst case: every particle censuses; every fission makes <= 4 */
         if (store_reserve(census, census->n + n) || store_reserve(&extra, 4 * n)) { status = -1; break; }
         extra.n = 0;
-        TrackCtx ctx = {pb, flux, bal, census, &extra, warnings, 0};
+        TrackCtx ctx = {pb, flux, bal, census, &extra, warnings, 0, sens};
         const OracleParticle* src = processing->p;
+        const double* src_sc = processing->K > 0 ? processing->sc : NULL;
+        const int K = processing->K;
 #pragma omp parallel for schedule(dynamic, 64)
-        for (int64_t i = 0; i < (int64_t)n; i++) track_one(&ctx, &src[i]);
+        for (int64_t i = 0; i < (int64_t)n; i++) track_one(&ctx, &src[i], src_sc ? src_sc + i * (size_t)K : NULL);
         if (ctx.overflow) { status = -2; break; }
         /* swap: extras become the processing list */
         Store tmp = *processing;
@@ -639,6 +732,7 @@ static int track_all(const QsgProblem* pb, Store* processing, Store* census, Cou
         extra.n = 0;
     }
     free(extra.p);
+    free(extra.sc);
     processing->n = 0;
     return status;
 }
@@ -656,6 +750,8 @@ struct OracleRun {
     uint64_t* source_tally;     /* MC_Cell_State::_sourceTally, persists across cycles */
     double source_particle_weight;
     uint64_t warnings;
+    OracleSens sens;            /* sens.K == 0: off */
+    int has_sens;
 };
 
 OracleRun* oracle_create(const QsgProblem* pb, const double* source_rate, uint64_t n_particles,
@@ -681,14 +777,24 @@ void oracle_destroy(OracleRun* r)
     if (!r) return;
     free(r->processing.p);
     free(r->processed.p);
+    free(r->processing.sc);
+    free(r->processed.sc);
+    if (r->has_sens) {
+        free(r->sens.flux_cell);
+        free(r->sens.dflux);
+        free(r->sens.leak);
+        free(r->sens.dleak);
+    }
     free(r->flux);
     free(r->source_tally);
     free(r);
 }
 
-static int store_push(Store* s, const OracleParticle* p)
+/* Append p with scores sc (NULL: zeros). */
+static int store_push(Store* s, const OracleParticle* p, const double* sc)
 {
     if (store_reserve(s, s->n + 1)) return -1;
+    store_set_scores(s, s->n, sc);
     s->p[s->n++] = *p;
     return 0;
 }
@@ -698,6 +804,7 @@ static int store_push(Store* s, const OracleParticle* p)
 static void store_erase_swap(Store* s, uint64_t i)
 {
     s->p[i] = s->p[s->n - 1];
+    if (s->K > 0) store_set_scores(s, i, s->sc + (s->n - 1) * (size_t)s->K);
     s->n--;
 }
 
@@ -799,7 +906,7 @@ static int source_now(OracleRun* run)
             w.species = 0;
             OracleParticle b;
             to_base(&w, &b);
-            if (store_push(&run->processing, &b)) return -1;
+            if (store_push(&run->processing, &b, NULL)) return -1;
             run->bal.v[QSG_BAL_SOURCE]++;
         }
     }
@@ -838,11 +945,15 @@ static int population_control(OracleRun* run)
                 if (r > (factor - split)) split--;
                 p->weight /= factor;
                 OracleParticle sp = *p;
+                double parent_sc[QSG_MAX_PARAMS];   /* split copies inherit the scores */
+                if (run->processing.K > 0)
+                    memcpy(parent_sc, run->processing.sc + (size_t)i * run->processing.K,
+                           (size_t)run->processing.K * sizeof(double));
                 for (int k = 0; k < split; k++) {
                     run->bal.v[QSG_BAL_SPLIT]++;
                     sp.random_number_seed = oracle_rng_spawn(&run->processing.p[i].random_number_seed);
                     sp.identifier = sp.random_number_seed;
-                    if (store_push(&run->processing, &sp)) return -1;
+                    if (store_push(&run->processing, &sp, run->processing.K > 0 ? parent_sc : NULL)) return -1;
                 }
             }
         }
@@ -886,7 +997,8 @@ int oracle_cycle_init(OracleRun* run)
 
 int oracle_cycle_tracking(OracleRun* run, int nthreads)
 {
-    return track_all(run->pb, &run->processing, &run->processed, &run->bal, run->flux, &run->warnings, nthreads);
+    return track_all(run->pb, &run->processing, &run->processed, &run->bal, run->flux, &run->warnings, nthreads,
+                     run->has_sens ? &run->sens : NULL);
 }
 
 int oracle_cycle_finalize(OracleRun* run)
@@ -909,9 +1021,44 @@ int oracle_set_processing(OracleRun* r, const OracleParticle* p, uint64_t n)
 {
     if (store_reserve(&r->processing, n)) return -1;
     memcpy(r->processing.p, p, n * sizeof(OracleParticle));
+    for (uint64_t i = 0; i < n; i++) store_set_scores(&r->processing, i, NULL);
     r->processing.n = n;
     return 0;
 }
+
+int oracle_enable_sensitivity(OracleRun* r, const OracleSens* spec)
+{
+    if (!spec || spec->K < 1 || spec->K > QSG_MAX_PARAMS || r->has_sens) return -1;
+    if (r->processing.n || r->processed.n) return -1;   /* before the first cycle */
+    r->sens = *spec;
+    const size_t C = (size_t)r->pb->num_cells, K = (size_t)spec->K;
+    r->sens.flux_cell = (double*)calloc(C, sizeof(double));
+    r->sens.dflux = (double*)calloc(C * K, sizeof(double));
+    r->sens.leak = (double*)calloc(1, sizeof(double));
+    r->sens.dleak = (double*)calloc(K, sizeof(double));
+    if (!r->sens.flux_cell || !r->sens.dflux || !r->sens.leak || !r->sens.dleak) return -1;
+    r->has_sens = 1;
+    free(r->processing.p);
+    free(r->processed.p);
+    memset(&r->processing, 0, sizeof(Store));
+    memset(&r->processed, 0, sizeof(Store));
+    r->processing.K = r->processed.K = spec->K;
+    return 0;
+}
+
+int oracle_read_sensitivity(const OracleRun* r, double* flux_cell, double* dflux, double* leak, double* dleak)
+{
+    if (!r->has_sens) return -1;
+    const size_t C = (size_t)r->pb->num_cells, K = (size_t)r->sens.K;
+    if (flux_cell) memcpy(flux_cell, r->sens.flux_cell, C * sizeof(double));
+    if (dflux) memcpy(dflux, r->sens.dflux, C * K * sizeof(double));
+    if (leak) memcpy(leak, r->sens.leak, sizeof(double));
+    if (dleak) memcpy(dleak, r->sens.dleak, K * sizeof(double));
+    return 0;
+}
+
+const double* oracle_processing_scores(const OracleRun* r) { return r->processing.sc; }
+const double* oracle_processed_scores(const OracleRun* r) { return r->processed.sc; }
 
 void oracle_balance(const OracleRun* r, uint64_t* out) { memcpy(out, r->bal.v, sizeof(r->bal.v)); }
 void oracle_last_balance(const OracleRun* r, uint64_t* out) { memcpy(out, r->last.v, sizeof(r->last.v)); }
@@ -920,20 +1067,48 @@ const double* oracle_flux(const OracleRun* r) { return r->flux; }
 int oracle_track(const QsgProblem* pb, const OracleParticle* in, uint64_t n, OracleParticle* census_out,
                  uint64_t cap, uint64_t* n_census, uint64_t* balance13, double* flux, int nthreads)
 {
-    Store processing = {0, 0, 0}, census = {0, 0, 0};
+    Store processing = {0, 0, 0, NULL, 0}, census = {0, 0, 0, NULL, 0};
     if (store_reserve(&processing, n ? n : 1)) return -1;
     memcpy(processing.p, in, n * sizeof(OracleParticle));
     processing.n = n;
     Counters bal;
     memset(&bal, 0, sizeof(bal));
     uint64_t warnings = 0;
-    int st = track_all(pb, &processing, &census, &bal, flux, &warnings, nthreads);
+    int st = track_all(pb, &processing, &census, &bal, flux, &warnings, nthreads, NULL);
     for (int k = 0; k < QSG_BAL_COUNT; k++) balance13[k] += bal.v[k];
     uint64_t ncopy = census.n < cap ? census.n : cap;
     if (census_out && ncopy) memcpy(census_out, census.p, ncopy * sizeof(OracleParticle));
     *n_census = census.n;
     free(processing.p);
     free(census.p);
+    if (st) return st;
+    return census.n > cap ? -3 : 0;
+}
+
+int oracle_track_sens(const QsgProblem* pb, OracleSens* sens, const OracleParticle* in, const double* in_scores,
+                      uint64_t n, OracleParticle* census_out, double* census_scores, uint64_t cap, uint64_t* n_census,
+                      uint64_t* balance13, double* flux, int nthreads)
+{
+    if (!sens || sens->K < 1 || sens->K > QSG_MAX_PARAMS) return -1;
+    const int K = sens->K;
+    Store processing = {0, 0, 0, NULL, K}, census = {0, 0, 0, NULL, K};
+    if (store_reserve(&processing, n ? n : 1)) return -1;
+    memcpy(processing.p, in, n * sizeof(OracleParticle));
+    for (uint64_t i = 0; i < n; i++) store_set_scores(&processing, i, in_scores ? in_scores + i * (size_t)K : NULL);
+    processing.n = n;
+    Counters bal;
+    memset(&bal, 0, sizeof(bal));
+    uint64_t warnings = 0;
+    int st = track_all(pb, &processing, &census, &bal, flux, &warnings, nthreads, sens);
+    for (int k = 0; k < QSG_BAL_COUNT; k++) balance13[k] += bal.v[k];
+    uint64_t ncopy = census.n < cap ? census.n : cap;
+    if (census_out && ncopy) memcpy(census_out, census.p, ncopy * sizeof(OracleParticle));
+    if (census_scores && ncopy) memcpy(census_scores, census.sc, ncopy * (size_t)K * sizeof(double));
+    *n_census = census.n;
+    free(processing.p);
+    free(processing.sc);
+    free(census.p);
+    free(census.sc);
     if (st) return st;
     return census.n > cap ? -3 : 0;
 }

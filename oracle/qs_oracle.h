@@ -59,6 +59,38 @@ void oracle_last_balance(const OracleRun* run, uint64_t* out13);
 /* Warnings the reference would print and continue from (qs_assert). */
 uint64_t oracle_warning_count(const OracleRun* run);
 
+/* Sensitivity (differential-operator) scores, restating what the CUDA
+ * library's sensitivity tallies compute (qsg_enable_sensitivity in qsg.h; the
+ * reference has no such capability).  Parameter k scales the cross sections
+ * of reaction type reaction[k] of every isotope of material[k] in groups
+ * [group_lo[k], group_hi[k]).  Outputs are accumulated: flux_cell [C],
+ * dflux [C*K], leak [1], dleak [K]. */
+typedef struct OracleSens {
+    int32_t K;
+    int32_t material[QSG_MAX_PARAMS], reaction[QSG_MAX_PARAMS];
+    int32_t group_lo[QSG_MAX_PARAMS], group_hi[QSG_MAX_PARAMS];
+    double theta[QSG_MAX_PARAMS];
+    double* flux_cell;
+    double* dflux;
+    double* leak;
+    double* dleak;
+} OracleSens;
+
+/* Switch a run's sensitivity tallies on (before its first cycle); the run
+ * copies the parameters and owns the output arrays. */
+int oracle_enable_sensitivity(OracleRun* run, const OracleSens* spec);
+/* Accumulated flux_cell [C], dflux [C*K], leak [1], dleak [K] (any may be NULL). */
+int oracle_read_sensitivity(const OracleRun* run, double* flux_cell, double* dflux, double* leak, double* dleak);
+/* Scores [n*K] of the processing / processed particles (row per particle). */
+const double* oracle_processing_scores(const OracleRun* run);
+const double* oracle_processed_scores(const OracleRun* run);
+
+/* One-shot tracking with sensitivity scores: in_scores [n*K] (NULL: zero),
+ * census_scores [cap*K] (may be NULL); tallies accumulate into sens's outputs. */
+int oracle_track_sens(const QsgProblem* problem, OracleSens* sens, const OracleParticle* in, const double* in_scores,
+                      uint64_t n, OracleParticle* census_out, double* census_scores, uint64_t cap, uint64_t* n_census,
+                      uint64_t* balance13, double* flux, int nthreads);
+
 /* One-shot tracking of a particle set (no cycle init): census particles go to
  * census_out (capacity cap), counters and flux accumulate into the outputs
  * (flux must hold num_cells*G doubles, zeroed by the caller). */

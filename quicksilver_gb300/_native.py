@@ -90,6 +90,16 @@ class QsgCycleConfig(C.Structure):
                 ("store_capacity", C.c_uint64)]
 
 
+MAX_PARAMS = 32
+
+
+class QsgSensitivity(C.Structure):
+    _fields_ = [("num_params", C.c_int32), ("theta", C.POINTER(C.c_double)), ("num_entries", C.c_int32),
+                ("param", C.POINTER(C.c_int32)), ("material", C.POINTER(C.c_int32)),
+                ("reaction", C.POINTER(C.c_int32)), ("group_lo", C.POINTER(C.c_int32)),
+                ("group_hi", C.POINTER(C.c_int32))]
+
+
 class QsgError(RuntimeError):
     def __init__(self, code: int, message: str):
         super().__init__(f"qsg error {code}: {message}")
@@ -128,6 +138,10 @@ _SIGNATURES = {
     "qsg_cycle_history": ([_VP, C.c_uint64, C.c_uint64, _up, _dp], C.c_int),
     "qsg_get_processing": ([_VP, C.POINTER(QsgParticleSoA), C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
     "qsg_processing_view": ([_VP, C.POINTER(QsgParticleSoA), C.POINTER(C.c_uint64)], C.c_int),
+    "qsg_enable_sensitivity": ([_VP, C.POINTER(QsgSensitivity)], C.c_int),
+    "qsg_read_sensitivity": ([_VP, _dp, _dp, _dp, _dp], C.c_int),
+    "qsg_reset_sensitivity": ([_VP], C.c_int),
+    "qsg_material_offsets": ([_VP, _ip], C.c_int),
     "qsg_processed_view": ([_VP, C.POINTER(QsgParticleSoA), C.POINTER(C.c_uint64)], C.c_int),
     "qsg_deck_parse_file": ([C.c_char_p, C.POINTER(_VP)], C.c_int),
     "qsg_deck_parse_string": ([C.c_char_p, C.POINTER(_VP)], C.c_int),

@@ -40,10 +40,10 @@ def signature(decks: list) -> str:
     return hashlib.sha256(json.dumps(sorted(shape)).encode()).hexdigest()[:16]
 
 
-def _time_candidate(deck_texts, scale, cand, cycles, warmup, max_passes):
+def _time_candidate(deck_texts, scale, cand, cycles, warmup, max_passes, problems=None):
     decks = [Deck.from_string(t, {"nParticles": max(1000, int(Deck.from_string(t).simulation.n_particles * scale))})
              for t in deck_texts]
-    bmc = BatchMonteCarlo(decks, flux_replicas=cand["flux_replicas"], max_passes=max_passes)
+    bmc = BatchMonteCarlo(decks, flux_replicas=cand["flux_replicas"], max_passes=max_passes, problems=problems)
     try:
         bmc.tune(cand["block_size"], cand["collision_batch"], cand["queue_chunk"])
         bmc.run(warmup, use_graph=True)
@@ -56,9 +56,12 @@ def _time_candidate(deck_texts, scale, cand, cycles, warmup, max_passes):
 
 
 def autotune(deck_texts: list, scale: float = 0.25, cycles: int = 2, warmup: int = 1, max_passes: int = 16,
-             cache_path: Path | None = DEFAULT_CACHE, space: dict | None = None, refresh: bool = False) -> dict:
+             cache_path: Path | None = DEFAULT_CACHE, space: dict | None = None, refresh: bool = False,
+             problems: list | None = None) -> dict:
     """Return the fastest candidate for these decks (dict with the four knobs plus
-    `segments_per_s` and `trials`).  `deck_texts` are Quicksilver deck strings."""
+    `segments_per_s` and `trials`).  `deck_texts` are Quicksilver deck strings;
+    `problems` (optional) are their already-built tables, reused by every
+    candidate (the tables do not depend on the particle count)."""
     decks = [Deck.from_string(t) for t in deck_texts]
     key = signature(decks)
     cache = {}
@@ -75,7 +78,7 @@ def autotune(deck_texts: list, scale: float = 0.25, cycles: int = 2, warmup: int
     best = None
     for values in itertools.product(*(space[n] for n in names)):
         cand = dict(zip(names, values))
-        rate = _time_candidate(deck_texts, scale, cand, cycles, warmup, max_passes)
+        rate = _time_candidate(deck_texts, scale, cand, cycles, warmup, max_passes, problems)
         trials.append({**cand, "segments_per_s": rate})
         if best is None or rate > best["segments_per_s"]:
             best = {**cand, "segments_per_s": rate}

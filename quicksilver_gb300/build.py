@@ -23,7 +23,7 @@ INCLUDE = ROOT / "include"
 LIB = OUT / "libqsg.so"
 
 HOST_SOURCES = ["host/status.cc", "host/deck.cc", "host/problem.cc", "host/batch.cc"]
-CUDA_SOURCES = ["track.cu", "cycle.cu"]
+CUDA_SOURCES = ["track.cu", "cycle.cu", "sens.cu"]
 
 NVCC_ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: no contraction into FMA, so every FP64 rounding matches the

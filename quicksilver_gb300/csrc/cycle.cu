@@ -201,8 +201,13 @@ __global__ void __launch_bounds__(kInitBlock) source_kernel(SourceArgs a)
     p.breed = 0;
     p.species = 0;
     const uint64_t slot = a.c.sc->start + t;
-    if (slot < a.out.capacity) store_particle(a.out, slot, p);
-    else atomicOr(a.c.flags, QSG_DEV_STORE_OVERFLOW);
+    if (slot < a.out.capacity) {
+        store_particle(a.out, slot, p);
+        // a source particle starts with zero sensitivity scores
+        for (int k = 0; k < a.out.score_fields; k++) a.out.score[(uint64_t)k * a.out.capacity + slot] = 0.0;
+    } else {
+        atomicOr(a.c.flags, QSG_DEV_STORE_OVERFLOW);
+    }
 }
 
 __device__ __forceinline__ void load_record(const DevStore& s, uint64_t i, Particle& p)
@@ -242,11 +247,20 @@ __device__ __forceinline__ bool roulette(double low_cut, double weight_cutoff, P
     return true;
 }
 
-__device__ __forceinline__ void emit(const DevStore& out, unsigned int* flags, const Particle& p)
+// Append p to `out`; its sensitivity scores (if the stores carry them) are
+// those of particle i of `in`, the particle it was copied or split from.
+__device__ __forceinline__ void emit(const DevStore& out, unsigned int* flags, const Particle& p, const DevStore& in,
+                                     uint64_t i)
 {
     uint64_t slot = append_slot(out);
-    if (slot < out.capacity) store_particle(out, slot, p);
-    else atomicOr(flags, QSG_DEV_STORE_OVERFLOW);
+    if (slot < out.capacity) {
+        store_particle(out, slot, p);
+        for (int k = 0; k < out.score_fields; k++)
+            out.score[(uint64_t)k * out.capacity + slot] =
+                k < in.score_fields ? in.score[(uint64_t)k * in.capacity + i] : 0.0;
+    } else {
+        atomicOr(flags, QSG_DEV_STORE_OVERFLOW);
+    }
 }
 
 // PopulationControlGuts (PopulationControl.cc:71-122) followed by the low-weight
@@ -289,11 +303,11 @@ __global__ void __launch_bounds__(kInitBlock) population_kernel(CycleArgs a, Dev
                     child.seed = rng_spawn(p.seed);
                     child.identifier = child.seed;
                     Particle c2 = child;
-                    if (roulette(low_cut, weight_cutoff, c2, rr)) emit(out, a.flags, c2);
+                    if (roulette(low_cut, weight_cutoff, c2, rr)) emit(out, a.flags, c2, in, i);
                 }
             }
         }
-        if (survive && roulette(low_cut, weight_cutoff, p, rr)) emit(out, a.flags, p);
+        if (survive && roulette(low_cut, weight_cutoff, p, rr)) emit(out, a.flags, p, in, i);
         if (rr | split_count) {
             if (use_smem) {
                 if (rr) atomicAdd(&s_rr[2 * prob], (unsigned long long)rr);

@@ -58,18 +58,28 @@ struct Store {
     unsigned long long* count = nullptr;  // device counter
     uint64_t capacity = 0;
     uint64_t generation = 0;              // bumped on every reallocation
+    int score_fields = 0;                 // sensitivity score arrays carried per particle
     DevStore view{};
 
-    int reserve(uint64_t cap)
+    // Grow to at least `cap` particles (keeping the contents); `force`
+    // reallocates even when large enough (after score_fields changed).
+    int reserve(uint64_t cap, bool force = false)
     {
-        if (cap <= capacity && base) return QSG_OK;
+        if (cap <= capacity && base && !force) return QSG_OK;
         uint64_t nc = capacity ? capacity : 1024;
         while (nc < cap) nc *= 2;
-        size_t bytes = nc * 136 + 256 * 21;
+        size_t bytes = nc * 136 + 256 * 21 + (size_t)score_fields * (nc * 8 + 256);
         void* nb = nullptr;
         cudaError_t e = cudaMalloc(&nb, bytes);
         if (e != cudaSuccess) return fail(QSG_ERR_CUDA, "cudaMalloc store (%zu bytes): %s", bytes, cudaGetErrorString(e));
-        DevStore nv = carve(nb, nc);
+        if (score_fields) {
+            e = cudaMemset(nb, 0, bytes);
+            if (e != cudaSuccess) {
+                cudaFree(nb);
+                return fail(QSG_ERR_CUDA, "store init: %s", cudaGetErrorString(e));
+            }
+        }
+        DevStore nv = carve(nb, nc, score_fields);
         if (base) {
             unsigned long long n_old = 0;
             e = cudaMemcpy(&n_old, count, sizeof(n_old), cudaMemcpyDeviceToHost);
@@ -95,7 +105,7 @@ struct Store {
         return QSG_OK;
     }
 
-    static DevStore carve(void* b, uint64_t cap)
+    static DevStore carve(void* b, uint64_t cap, int score_fields)
     {
         DevStore v{};
         char* p = static_cast<char*>(b);
@@ -113,6 +123,8 @@ struct Store {
         v.identifier = reinterpret_cast<uint64_t*>(take(8));
         int32_t** ifields[6] = {&v.last_event, &v.num_collisions, &v.breed, &v.species, &v.domain, &v.cell};
         for (int32_t** f : ifields) *f = reinterpret_cast<int32_t*>(take(4));
+        v.score = score_fields ? reinterpret_cast<double*>(take(8 * (size_t)score_fields)) : nullptr;
+        v.score_fields = score_fields;
         v.capacity = cap;
         return v;
     }
@@ -139,6 +151,12 @@ struct Store {
         int32_t* si[6] = {src.last_event, src.num_collisions, src.breed, src.species, src.domain, src.cell};
         for (int k = 0; k < 6; k++) {
             cudaError_t e = cudaMemcpyAsync(di[k] + dst_off, si[k] + src_off, n * 4, cudaMemcpyDeviceToDevice, s);
+            if (e != cudaSuccess) return e;
+        }
+        for (int k = 0; k < dst.score_fields && k < src.score_fields; k++) {
+            cudaError_t e = cudaMemcpyAsync(dst.score + (size_t)k * dst.capacity + dst_off,
+                                            src.score + (size_t)k * src.capacity + src_off, n * 8,
+                                            cudaMemcpyDeviceToDevice, s);
             if (e != cudaSuccess) return e;
         }
         return cudaSuccess;
@@ -229,6 +247,17 @@ struct QsgHandle {
     qsg::DevBuf<uint64_t> prob_target, prob_nsource, prob_seed_offset;
     qsg::DevBuf<int32_t> prob_load_balance, prob_cell_offset;
     qsg::DevBuf<unsigned long long> prob_carry;
+    // host copies of the cross-section classes (sensitivity tables are built from them)
+    std::vector<int32_t> h_class_material;        // [classes]
+    std::vector<int8_t> h_class_type;             // [classes][max_reactions]
+    std::vector<uint8_t> h_class_const;           // [classes][max_reactions] 1: the 1e-20 placeholder entry
+    std::vector<double> h_class_macro;            // [classes][G][max_reactions]
+    int32_t num_classes = 0, max_reactions = 0;
+    // sensitivities (qsg_enable_sensitivity); sens.K == 0: off
+    qsg::DevSens sens{};
+    int sens_track_blocks = 0;
+    qsg::DevBuf<int16_t> sens_param;              // [classes][G][3]
+    qsg::DevBuf<double> sens_dsig, sens_inv_theta, sens_flux_cell, sens_dflux, sens_leak, sens_dleak;
     // CUDA graphs of whole cycles, one per role permutation of the stores
     struct GraphEntry {
         void *proc = nullptr, *done = nullptr, *extra = nullptr;
@@ -259,6 +288,8 @@ inline int copy_store_to_host(const DevStore& d, const QsgParticleSoA* h, uint64
     int st = check_soa(h);
     return st ? st : copy_soa(d, h, n, false);
 }
+// Persistent grids of the tracking kernels for the handle's block size (track.cu).
+int configure_track_grid(QsgHandle* h);
 // Tracking passes of one cycle (track.cu).
 int track_passes_async(QsgHandle* h, cudaStream_t s);
 int track_passes_sync(QsgHandle* h, cudaStream_t s);

@@ -310,6 +310,7 @@ __device__ __forceinline__ int segment_outcome(const DevTables& t, const DevTall
                                                int cls, double* flux_row)
 {
     double d_coll, d_facet, d_census;
+    p.seg_len = 0.0;
     if (p.speed < 0.0) p.speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
     const double speed = p.speed;
     bool force_collision = false;
@@ -344,6 +345,7 @@ __device__ __forceinline__ int segment_outcome(const DevTables& t, const DevTall
     if (d_facet < seg) { seg = d_facet; outcome = OUT_FACET; }
     if (d_census < seg) { seg = d_census; outcome = OUT_CENSUS; }
     if (seg < 0) raise_flag(tally, QSG_DEV_NEGATIVE_DISTANCE);
+    p.seg_len = seg;
     p.num_mean_free_paths -= seg / p.mean_free_path;
     if (outcome == OUT_COLLISION) {
         p.last_event = QSG_EVENT_COLLISION;
@@ -407,8 +409,12 @@ __device__ __forceinline__ void update_trajectory(double energy, double angle, P
 
 // CollisionEvent, CollisionEvent.cc:48-148, with NuclearDataReaction::
 // sampleCollision (NuclearData.cc:52-88).  Returns true to keep tracking.
+// SENS: the selected reaction adds d log Sigma_r / dtheta to the history's
+// scores S (stride `ss`), and fission products carry the scores along.
+template <bool SENS>
 __device__ __forceinline__ bool collision_event(const DevTables& t, const DevTally& tally, Particle& p, int cls,
-                                                const DevStore& extra, uint32_t* cnt)
+                                                const DevStore& extra, uint32_t* cnt, const DevSens& sens,
+                                                double* S, int ss)
 {
     const int G = t.num_groups;
     const int K = t.max_reactions;
@@ -427,6 +433,11 @@ __device__ __forceinline__ bool collision_event(const DevTables& t, const DevTal
         sel = nk - 1;
     }
     const int type = t.class_reaction_type[cls * K + sel];
+    if (SENS) {
+        // group of the incoming particle: the reaction was sampled in it
+        const int k = __ldg(sens.param_of + ((int64_t)cls * G + p.group) * 3 + (type - 1));
+        if (k >= 0) S[k * ss] += __ldg(sens.inv_theta + k);
+    }
     // 1.0 / mass of NuclearData.cc:64, divided once on the host (same bits)
     const double inv_mass = __ldg(t.material_inv_mass + __ldg(t.class_material + cls));
     double e_out[4], a_out[4];
@@ -462,14 +473,22 @@ __device__ __forceinline__ bool collision_event(const DevTables& t, const DevTal
         sec.identifier = sec.seed;
         update_trajectory(e_out[s], a_out[s], sec);
         uint64_t slot = append_slot(extra);
-        if (slot < extra.capacity) store_particle(extra, slot, sec);
-        else raise_flag(tally, QSG_DEV_STORE_OVERFLOW);
+        if (slot < extra.capacity) {
+            store_particle(extra, slot, sec);
+            if (SENS) store_scores(extra, slot, S, ss, sens.K);
+        } else {
+            raise_flag(tally, QSG_DEV_STORE_OVERFLOW);
+        }
     }
     update_trajectory(e_out[0], a_out[0], p);
     if (n_out > 1) {
         uint64_t slot = append_slot(extra);
-        if (slot < extra.capacity) store_particle(extra, slot, p);
-        else raise_flag(tally, QSG_DEV_STORE_OVERFLOW);
+        if (slot < extra.capacity) {
+            store_particle(extra, slot, p);
+            if (SENS) store_scores(extra, slot, S, ss, sens.K);
+        } else {
+            raise_flag(tally, QSG_DEV_STORE_OVERFLOW);
+        }
     }
     p.group = energy_group(t, p.kinetic_energy);
     return n_out == 1;
@@ -567,22 +586,65 @@ struct BlockCounters {
     }
 };
 
+// Differential-operator (likelihood-ratio) scores of one flight of length
+// l = p.seg_len through cell p.cell in group p.group: the flight's probability
+// exp(-Sigma_t l) (times Sigma_t when it ends in a collision) gives
+// d log / dtheta_k = -l dSigma_t/dtheta_k (+ dSigma_t/dtheta_k / Sigma_t).  The
+// scores S then carry -l dSigma_t/dtheta_k; the collision's own factor is
+// folded with reaction selection into d log Sigma_r / dtheta_k in
+// collision_event.  The flight's track-length flux l w is tallied with the
+// flight's full score, l w (S_k + [collision] dSigma_t/dtheta_k / Sigma_t).
+// No counterpart in the reference, which has no sensitivity tallies; the flux
+// estimator is Tallies::TallyScalarFlux (Tallies.hh:350-354) summed over groups.
+__device__ __forceinline__ void sens_segment(const DevTables& t, const DevSens& sens, const Particle& p, int cls,
+                                             bool collided, double* S, int ss)
+{
+    const double l = p.seg_len;
+    if (l == 0.0) return;   // nothing moved: no flight score and no flux tally
+    const int64_t base = ((int64_t)cls * t.num_groups + p.group) * 3;
+    int pk[3];
+    double pd[3];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        pk[j] = __ldg(sens.param_of + base + j);
+        pd[j] = pk[j] >= 0 ? __ldg(sens.dsig + base + j) : 0.0;
+        if (pk[j] >= 0) S[pk[j] * ss] -= l * pd[j];
+    }
+    const double lw = l * p.weight;
+    atomicAdd(sens.flux_cell + p.cell, lw);
+    double* row = sens.dflux + (int64_t)p.cell * sens.K;
+    for (int k = 0; k < sens.K; k++) {
+        double v = S[k * ss];
+        if (collided) {
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+                if (pk[j] == k) v += pd[j] * p.mean_free_path;
+        }
+        if (v != 0.0) atomicAdd(row + k, lw * v);
+    }
+}
+
 // Persistent tracking pass over the store `in` (its count is read on the
 // device): CycleTrackingGuts + CycleTrackingFunction (CycleTracking.cc:14-120)
 // one segment per loop trip.  A lane whose history ends pulls the next
 // particle index from the work cursor at once (warp-aggregated atomic), so
 // long histories do not hold idle lanes; the warp leaves when every lane has
 // finished and the queue is empty.
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / BLOCK) track_kernel(DevTables t,
-                                                                                                 DevTally tally,
-                                                                                                 DevStore in,
-                                                                       DevStore census,
-                                                      DevStore extra, unsigned long long* cursor)
+//
+// SENS: every history also carries sensitivity scores (shared memory, one
+// column per thread after the counters), tallied by sens_segment, at escape
+// (leakage and its derivatives) and stored with census / fission particles.
+template <int BLOCK, bool SENS>
+__global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / BLOCK)
+    track_kernel(DevTables t, DevTally tally, DevStore in, DevStore census, DevStore extra,
+                 unsigned long long* cursor, DevSens sens)
 {
     extern __shared__ unsigned long long s_counts[];
     BlockCounters bc;
-    bc.smem = (tally.num_problems <= kSmemProblems) ? s_counts : nullptr;
+    const bool counts_in_smem = tally.num_problems <= kSmemProblems;
+    bc.smem = counts_in_smem ? s_counts : nullptr;
+    double* S = nullptr;
+    if (SENS) S = reinterpret_cast<double*>(s_counts + (counts_in_smem ? tally.num_problems * LC_N : 0)) + threadIdx.x;
     bc.tally = &tally;
     bc.replica = (int)(blockIdx.x % (unsigned)tally.balance_replicas);
     if (bc.smem)
@@ -612,6 +674,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
             const uint64_t i = next++;
             if (i < n) {
                 load_particle(t, in, i, p);
+                if (SENS) load_scores(in, i, S, BLOCK, sens.K);
                 if (!(p.speed > 0.0)) raise_flag(tally, QSG_DEV_BAD_FACET);
                 const int prob = tally.cell_problem ? __ldg(tally.cell_problem + p.cell) : 0;
                 if (prob != cur_prob) {
@@ -637,7 +700,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
         if (pend_mask != 0u && (__popc(pend_mask) >= tally.collision_batch || run_mask == 0u)) {
             if (pending) {
                 pending = false;
-                active = collision_event(t, tally, p, __ldg(t.cell_class + p.cell), extra, cnt);
+                active = collision_event<SENS>(t, tally, p, __ldg(t.cell_class + p.cell), extra, cnt, sens, S, BLOCK);
             }
             continue;
         }
@@ -645,6 +708,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
             bool keep;
             const int cls = __ldg(t.cell_class + p.cell);
             int outcome = segment_outcome(t, tally, p, cls, flux_row);
+            if (SENS) sens_segment(t, sens, p, cls, outcome == OUT_COLLISION, S, BLOCK);
             cnt[LC_SEG]++;
             p.num_segments += 1.;
             if (outcome == OUT_COLLISION) {
@@ -662,6 +726,14 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
                     keep = true;
                 } else if (ev == QSG_ADJ_BOUNDARY_ESCAPE) {
                     cnt[LC_ESC]++;
+                    if (SENS) {
+                        // leakage (escaping weight) and d leakage / dtheta
+                        atomicAdd(sens.leak + cur_prob, p.weight);
+                        for (int k = 0; k < sens.K; k++) {
+                            const double v = S[k * BLOCK];
+                            if (v != 0.0) atomicAdd(sens.dleak + (int64_t)cur_prob * sens.K + k, p.weight * v);
+                        }
+                    }
                     p.last_event = QSG_EVENT_FACET_ESCAPE;
                     p.species = -1;
                     keep = false;
@@ -676,8 +748,12 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
             } else {
                 // census: ParticleVault::pushParticle (ParticleVault.hh:86-93)
                 uint64_t slot = append_slot(census);
-                if (slot < census.capacity) store_particle(census, slot, p);
-                else raise_flag(tally, QSG_DEV_STORE_OVERFLOW);
+                if (slot < census.capacity) {
+                    store_particle(census, slot, p);
+                    if (SENS) store_scores(census, slot, S, BLOCK, sens.K);
+                } else {
+                    raise_flag(tally, QSG_DEV_STORE_OVERFLOW);
+                }
                 cnt[LC_CEN]++;
                 keep = false;
             }
@@ -728,16 +804,34 @@ size_t track_smem_bytes(const QsgHandle* h)
     return h->num_problems <= kSmemProblems ? (size_t)h->num_problems * LC_N * sizeof(unsigned long long) : 0;
 }
 
+size_t track_smem_bytes_sens(const QsgHandle* h)
+{
+    return track_smem_bytes(h) + (size_t)h->sens.K * h->block_size * sizeof(double);
+}
+
 // Persistent grid for the current block size: SMs x resident blocks.
 int configure_track_grid(QsgHandle* h)
 {
     int per_sm = 0;
     const size_t smem = track_smem_bytes(h);
     if (h->block_size == 256)
-        QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel<256>, 256, smem));
+        QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel<256, false>, 256, smem));
     else
-        QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel<128>, 128, smem));
+        QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel<128, false>, 128, smem));
     h->track_blocks = h->num_sms * (per_sm > 0 ? per_sm : 1);
+    if (h->sens.K > 0) {
+        // the sensitivity kernel adds one column of K scores per thread
+        const size_t ss = track_smem_bytes_sens(h);
+        per_sm = 0;
+        if (h->block_size == 256) {
+            QSG_CUDA(cudaFuncSetAttribute(track_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ss));
+            QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel<256, true>, 256, ss));
+        } else {
+            QSG_CUDA(cudaFuncSetAttribute(track_kernel<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ss));
+            QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel<128, true>, 128, ss));
+        }
+        h->sens_track_blocks = h->num_sms * (per_sm > 0 ? per_sm : 1);
+    }
     return QSG_OK;
 }
 
@@ -838,6 +932,7 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
     std::vector<double> sigma_total((size_t)NCL * G), macro((size_t)NCL * G * K, 0.0), nubar((size_t)NCL * K, 0.0);
     std::vector<int32_t> nreact(NCL), cmat(NCL);
     std::vector<int8_t> ctype((size_t)NCL * K, 0);
+    std::vector<uint8_t> cconst((size_t)NCL * K, 0);
     for (int ci = 0; ci < NCL; ci++) {
         int m = classes[ci].first;
         double nd = classes[ci].second;
@@ -866,6 +961,7 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
                 sum += zero ? 1e-20 : af * nd * micro_total;
                 for (int r = p->isotope_reaction_offset[iso]; r < p->isotope_reaction_offset[iso + 1]; r++) {
                     macro[((size_t)ci * G + g) * K + kk] = zero ? 1e-20 : af * nd * p->reaction_xs[(int64_t)r * G + g];
+                    cconst[(size_t)ci * K + kk] = zero ? 1 : 0;
                     kk++;
                 }
             }
@@ -911,6 +1007,12 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
         (st = h->cell_class.upload(cell_class)) || (st = h->adj_cell.upload(adj_cell)) ||
         (st = h->class_type.upload(ctype)) || (st = h->adj_facet_event.upload(adj_fe)))
         return st;
+    h->h_class_material = cmat;
+    h->h_class_type = ctype;
+    h->h_class_const = cconst;
+    h->h_class_macro = macro;
+    h->num_classes = NCL;
+    h->max_reactions = K;
     DevTables& t = h->tables;
     t.num_groups = G;
     t.num_cells = (int32_t)C;
@@ -1014,13 +1116,26 @@ int launch_pass(QsgHandle* h, cudaStream_t s)
     unsigned long long* cursor = &h->scalars.ptr->cursor;
     QSG_CUDA(cudaMemsetAsync(h->extra.count, 0, sizeof(unsigned long long), s));
     QSG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s));
-    const size_t smem = track_smem_bytes(h);
-    if (h->block_size == 256)
-        track_kernel<256><<<h->track_blocks, 256, smem, s>>>(h->tables, tally_view(h), h->processing.view,
-                                                             h->processed.view, h->extra.view, cursor);
-    else
-        track_kernel<128><<<h->track_blocks, 128, smem, s>>>(h->tables, tally_view(h), h->processing.view,
-                                                             h->processed.view, h->extra.view, cursor);
+    const DevTally tv = tally_view(h);
+    if (h->sens.K > 0) {
+        const size_t smem = track_smem_bytes_sens(h);
+        if (h->block_size == 256)
+            track_kernel<256, true><<<h->sens_track_blocks, 256, smem, s>>>(
+                h->tables, tv, h->processing.view, h->processed.view, h->extra.view, cursor, h->sens);
+        else
+            track_kernel<128, true><<<h->sens_track_blocks, 128, smem, s>>>(
+                h->tables, tv, h->processing.view, h->processed.view, h->extra.view, cursor, h->sens);
+    } else {
+        const size_t smem = track_smem_bytes(h);
+        if (h->block_size == 256)
+            track_kernel<256, false><<<h->track_blocks, 256, smem, s>>>(h->tables, tv, h->processing.view,
+                                                                        h->processed.view, h->extra.view, cursor,
+                                                                        DevSens{});
+        else
+            track_kernel<128, false><<<h->track_blocks, 128, smem, s>>>(h->tables, tv, h->processing.view,
+                                                                        h->processed.view, h->extra.view, cursor,
+                                                                        DevSens{});
+    }
     QSG_CUDA(cudaGetLastError());
     // the extra store becomes the next pass's input; the old input is free
     std::swap(h->processing, h->extra);
@@ -1214,6 +1329,8 @@ extern "C" int qsg_destroy(QsgHandle* h)
     h->cell_problem.free(); h->prob_weight.free(); h->prob_emin.free(); h->prob_emax.free(); h->prob_lowcut.free();
     h->prob_factor.free(); h->prob_target.free(); h->prob_nsource.free(); h->prob_seed_offset.free();
     h->prob_load_balance.free(); h->prob_cell_offset.free(); h->prob_carry.free();
+    h->sens_param.free(); h->sens_dsig.free(); h->sens_inv_theta.free(); h->sens_flux_cell.free();
+    h->sens_dflux.free(); h->sens_leak.free(); h->sens_dleak.free();
     h->clear_graphs();
     if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
     h->processing.release(); h->processed.release(); h->extra.release();
@@ -1230,6 +1347,9 @@ extern "C" int qsg_set_particles(QsgHandle* h, const QsgParticleSoA* host, uint6
     if ((st = set_device(h))) return st;
     if ((st = h->processing.reserve(n))) return st;
     if ((st = copy_soa(h->processing.view, host, n, true))) return st;
+    if (h->processing.view.score)   // particles from the host start with zero sensitivity scores
+        QSG_CUDA(cudaMemset(h->processing.view.score, 0,
+                            (size_t)h->processing.view.score_fields * h->processing.capacity * sizeof(double)));
     unsigned long long nn = n;
     QSG_CUDA(cudaMemcpy(h->processing.count, &nn, sizeof(nn), cudaMemcpyHostToDevice));
     QSG_CUDA(cudaMemset(h->processed.count, 0, sizeof(unsigned long long)));
@@ -1550,8 +1670,9 @@ extern "C" int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* p
 
     unsigned long long* header = reinterpret_cast<unsigned long long*>(scratch);
     unsigned long long* cursor = header + 0;
-    DevStore prod[2] = {Store::carve(scratch + kNoallocHeaderBytes, QSG_NOALLOC_MAX_PRODUCTS),
-                        Store::carve(scratch + kNoallocHeaderBytes + kNoallocStoreBytes, QSG_NOALLOC_MAX_PRODUCTS)};
+    DevStore prod[2] = {Store::carve(scratch + kNoallocHeaderBytes, QSG_NOALLOC_MAX_PRODUCTS, 0),
+                        Store::carve(scratch + kNoallocHeaderBytes + kNoallocStoreBytes, QSG_NOALLOC_MAX_PRODUCTS,
+                                     0)};
     const DevStore in0 = noalloc_caller_store(particles, n, header + 1);
     const DevStore out = noalloc_caller_store(census, census_capacity, header + 2);
     DevTally tally = tally_view(h);
@@ -1571,9 +1692,11 @@ extern "C" int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* p
         QSG_CUDA(cudaMemsetAsync(extra.count, 0, sizeof(unsigned long long), s));
         QSG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s));
         if (h->block_size == 256)
-            track_kernel<256><<<h->track_blocks, 256, smem, s>>>(h->tables, tally, in, out, extra, cursor);
+            track_kernel<256, false><<<h->track_blocks, 256, smem, s>>>(h->tables, tally, in, out, extra, cursor,
+                                                                        DevSens{});
         else
-            track_kernel<128><<<h->track_blocks, 128, smem, s>>>(h->tables, tally, in, out, extra, cursor);
+            track_kernel<128, false><<<h->track_blocks, 128, smem, s>>>(h->tables, tally, in, out, extra, cursor,
+                                                                        DevSens{});
         QSG_CUDA(cudaGetLastError());
         // products of this pass, census so far, device flags
         QSG_CUDA(cudaMemcpyAsync(&counts[0], extra.count, 8, cudaMemcpyDeviceToHost, s));

@@ -56,8 +56,22 @@ struct DevStore {
     double *kinetic_energy, *weight, *time_to_census, *age, *num_mean_free_paths, *num_segments;
     uint64_t *seed, *identifier;
     int32_t *last_event, *num_collisions, *breed, *species, *domain, *cell;
+    double* score;          // [score_fields][capacity] sensitivity scores (null: none)
+    int32_t score_fields;
     unsigned long long* count;
     uint64_t capacity;
+};
+
+// Sensitivity tables and tallies (qsg_enable_sensitivity).
+struct DevSens {
+    int32_t K;                 // parameters (0: sensitivities off)
+    const int16_t* param_of;   // [classes][G][3] parameter of (class, group, reaction type - 1), or -1
+    const double* dsig;        // [classes][G][3] dSigma_t/dtheta contributed by that reaction type
+    const double* inv_theta;   // [K] d log Sigma_r / dtheta for a reaction the parameter scales
+    double* flux_cell;         // [C] group-summed track-length flux (the differentiated forward tally)
+    double* dflux;             // [C][K]
+    double* leak;              // [problems]
+    double* dleak;             // [problems][K]
 };
 
 // Read-only problem tables in device memory.
@@ -183,6 +197,7 @@ struct Particle {
     // 1/Sigma_t for the (cross-section class, group) key it was computed for
     double speed;                  // < 0: stale
     int32_t xs_key;                // -1: stale
+    double seg_len;                // length of the last segment (MC_Particle::segment_path_length)
 };
 
 __device__ __forceinline__ void load_particle(const DevTables& t, const DevStore& s, uint64_t i, Particle& p)
@@ -219,6 +234,19 @@ __device__ __forceinline__ void load_particle(const DevTables& t, const DevStore
     if (p.time_to_census <= 0.0) p.time_to_census += t.time_step;
     if (p.age < 0.0) p.age = 0.0;
     p.group = energy_group(t, p.kinetic_energy);
+}
+
+// A history's sensitivity scores live in shared memory, S[k * stride] for
+// parameter k (stride = threads per block), so that the parameter picked by a
+// collision can index them without spilling a register array.
+__device__ __forceinline__ void load_scores(const DevStore& s, uint64_t i, double* S, int stride, int K)
+{
+    for (int k = 0; k < K; k++) S[k * stride] = (k < s.score_fields) ? s.score[(uint64_t)k * s.capacity + i] : 0.0;
+}
+
+__device__ __forceinline__ void store_scores(const DevStore& s, uint64_t i, const double* S, int stride, int K)
+{
+    for (int k = 0; k < K && k < s.score_fields; k++) s.score[(uint64_t)k * s.capacity + i] = S[k * stride];
 }
 
 __device__ __forceinline__ void store_particle(const DevStore& s, uint64_t i, const Particle& p)

@@ -162,6 +162,11 @@ def test_decks() -> dict:
     rng = np.random.default_rng(11)
     d["t_nonflat.inp"] = (small(nx=6, ny=6, nz=6, lx=6, ly=6, lz=6, nGroups=40) + brick("matA", 0, 6, 0, 6, 0, 6) +
                           sphere("matB", 2, 3, 3, 3) + drawn_materials(rng, ["matA", "matB"]))
+    # config-4 geometry in small: escape boundaries, 3 nested materials (sensitivity tests)
+    rng = np.random.default_rng(5)
+    d["t_sens.inp"] = (small(boundaryCondition="escape", nx=6, ny=6, nz=6, lx=6, ly=6, lz=6, nGroups=40) +
+                       brick("matA", 0, 6, 0, 6, 0, 6) + sphere("matB", "2.4", 3, 3, 3) +
+                       sphere("matC", "1.2", 3, 3, 3) + drawn_materials(rng, ["matA", "matB", "matC"]))
     # no Geometry block: supplyDefaults problem (Parameters.cc:350-379)
     d["t_default.inp"] = small(nParticles=3000, nSteps=2, lx=10, ly=10, lz=10)
     return d

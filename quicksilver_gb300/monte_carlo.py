@@ -113,14 +113,16 @@ class _Driver:
 class MonteCarlo(_Driver):
     def __init__(self, deck: Deck, flux_replicas: int = 1, balance_replicas: int = 1, max_passes: int = 8,
                  store_capacity: int = 0, device: int = 0, problem: HostProblem | None = None,
-                 block_size: int = 0, collision_batch: int = 0):
+                 block_size: int = 0, collision_batch: int = 0, seed_offset: int = 0):
+        """seed_offset (0 = the reference's seeding) is added to every source
+        seed, giving an independent replica of the same problem."""
         self.deck = deck
         self.params = deck.simulation
         self.problem = problem if problem is not None else deck.build()
         self.tracker = Tracker(self.problem, flux_replicas=flux_replicas, balance_replicas=balance_replicas,
                                device=device, max_passes=max_passes, block_size=block_size,
                                collision_batch=collision_batch)
-        self._configure([deck], [self.problem], store_capacity, None)
+        self._configure([deck], [self.problem], store_capacity, [seed_offset] if seed_offset else None)
 
     @property
     def n_steps(self) -> int:

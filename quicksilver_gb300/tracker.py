@@ -87,6 +87,37 @@ class Tracker:
     def reset_tallies(self) -> None:
         N.check(N.lib().qsg_reset_tallies(self._h))
 
+    # ---- sensitivities (qsg_enable_sensitivity) ----
+    def material_offsets(self) -> np.ndarray:
+        """[problems + 1] offsets of each problem's materials in this handle."""
+        out = np.zeros(len(self.problems) + 1, dtype=np.int32)
+        N.check(N.lib().qsg_material_offsets(self._h, out.ctypes.data_as(C.POINTER(C.c_int32))))
+        return out
+
+    def enable_sensitivity(self, params) -> None:
+        """params: sequence of sensitivity.Param (material indices of this handle)."""
+        rows = [(k, *e) for k, p in enumerate(params) for e in p.entries()]
+        cols = [np.ascontiguousarray([r[j] for r in rows], dtype=np.int32) for j in range(5)]
+        theta = np.ascontiguousarray([p.theta for p in params], dtype=np.float64)
+        ip = C.POINTER(C.c_int32)
+        s = N.QsgSensitivity(len(params), theta.ctypes.data_as(C.POINTER(C.c_double)), len(rows),
+                             *(c.ctypes.data_as(ip) for c in cols))
+        N.check(N.lib().qsg_enable_sensitivity(self._h, C.byref(s)))
+        self.num_params = len(params)
+
+    def read_sensitivity(self) -> dict:
+        """flux_cell [C], dflux [C, K], leak [P], dleak [P, K] accumulated since enable / reset."""
+        K, P = self.num_params, len(self.problems)
+        out = {"flux_cell": np.zeros(self.num_cells), "dflux": np.zeros((self.num_cells, K)),
+               "leak": np.zeros(P), "dleak": np.zeros((P, K))}
+        dp = C.POINTER(C.c_double)
+        N.check(N.lib().qsg_read_sensitivity(self._h, *(out[k].ctypes.data_as(dp)
+                                                       for k in ("flux_cell", "dflux", "leak", "dleak"))))
+        return out
+
+    def reset_sensitivity(self) -> None:
+        N.check(N.lib().qsg_reset_sensitivity(self._h))
+
     def device_status(self, clear: bool = True) -> int:
         f = C.c_uint32()
         N.check(N.lib().qsg_device_status(self._h, C.byref(f), int(clear)))
