@@ -359,6 +359,8 @@ def main():
     ap.add_argument("--flux-replicas", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and differentiated forms")
+    ap.add_argument("--kernel", type=int, default=1, choices=[0, 1],
+                    help="tracking kernel: 1 warp particle pool (default), 0 one history per lane")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()
@@ -388,6 +390,7 @@ def main():
     mc = MonteCarlo(deck, flux_replicas=args.flux_replicas, device=local)
     h = mc.tracker.handle
     lib = N.lib()
+    N.check(lib.qsg_set_track_kernel(h, args.kernel))
     stream = torch.cuda.current_stream()
     sp = C.c_void_p(stream.cuda_stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # 256 MiB > 129 MB L2
@@ -479,7 +482,8 @@ def main():
         "config": {"workload": WORKLOAD, "step": "one cycle's tracking (cycleTracking phase)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "flushed (256 MiB write) before every timed step", "particles_in_hbm": True,
-                   "flux_replicas": args.flux_replicas, "wall_s_timed_region": wall},
+                   "flux_replicas": args.flux_replicas, "wall_s_timed_region": wall,
+                   "kernel": "warp particle pool" if args.kernel == 1 else "one history per lane"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "traffic": (tps * seg_per_launch) if tps else None,

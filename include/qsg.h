@@ -307,6 +307,11 @@ int qsg_run_cycles(QsgHandle* h, int32_t n_cycles, int32_t use_graph, void* stre
  * tracking kernel (128 or 256), collisions batched per warp step (1-32),
  * particles claimed per work-queue atomic (1-1024); 0 keeps a value. */
 int qsg_set_tuning(QsgHandle* h, int32_t block_size, int32_t collision_batch, int32_t queue_chunk);
+/* Tracking kernel: 1 (default) = each warp keeps a pool of 64 particles in
+ * shared memory and hands 32 of one kind (segment or collision) to its lanes
+ * per step; 0 = one history per lane (collisions batched per warp).  Both
+ * give the same results. */
+int qsg_set_track_kernel(QsgHandle* h, int32_t kind);
 
 /* ---- tracking without allocation ---------------------------------------- */
 /* No counterpart in the reference (Quicksilver allocates its vaults itself).

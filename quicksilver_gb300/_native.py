@@ -132,6 +132,7 @@ _SIGNATURES = {
     "qsg_batch_create": ([C.POINTER(QsgProblem), C.c_int32, C.POINTER(QsgOptions), C.POINTER(_VP)], C.c_int),
     "qsg_num_problems": ([_VP, C.POINTER(C.c_int32), _ip], C.c_int),
     "qsg_set_tuning": ([_VP, C.c_int32, C.c_int32, C.c_int32], C.c_int),
+    "qsg_set_track_kernel": ([_VP, C.c_int32], C.c_int),
     "qsg_run_cycles": ([_VP, C.c_int32, C.c_int32, _VP], C.c_int),
     "qsg_cycle_init": ([_VP, _VP], C.c_int),
     "qsg_cycle_finalize": ([_VP, _VP], C.c_int),

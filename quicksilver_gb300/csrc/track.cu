@@ -346,7 +346,9 @@ __device__ __forceinline__ int segment_outcome(const DevTables& t, const DevTall
     if (d_census < seg) { seg = d_census; outcome = OUT_CENSUS; }
     if (seg < 0) raise_flag(tally, QSG_DEV_NEGATIVE_DISTANCE);
     p.seg_len = seg;
-    p.num_mean_free_paths -= seg / p.mean_free_path;
+    // a collision resets the mean free paths to 0 below: the reference's
+    // subtraction there is dead, so it is skipped (same bits)
+    if (outcome != OUT_COLLISION) p.num_mean_free_paths -= seg / p.mean_free_path;
     if (outcome == OUT_COLLISION) {
         p.last_event = QSG_EVENT_COLLISION;
         p.num_mean_free_paths = 0.0;
@@ -407,14 +409,21 @@ __device__ __forceinline__ void update_trajectory(double energy, double angle, P
     p.num_mean_free_paths = -1.0 * log(r);
 }
 
-// CollisionEvent, CollisionEvent.cc:48-148, with NuclearDataReaction::
-// sampleCollision (NuclearData.cc:52-88).  Returns true to keep tracking.
-// SENS: the selected reaction adds d log Sigma_r / dtheta to the history's
-// scores S (stride `ss`), and fission products carry the scores along.
+// CollisionEvent (CollisionEvent.cc:48-148) with NuclearDataReaction::
+// sampleCollision (NuclearData.cc:52-88), split in two so that a warp runs the
+// expensive part (trajectory update: log, sincos, square roots, rotation) for
+// many lanes at once.  A particle's own random stream is consumed in the
+// reference's order either way, so the results are unchanged.
+enum CollisionKind { COLL_ENDS = 0, COLL_SCATTER = 1, COLL_FISSION = 2 };
+
+// First part, right after the segment: reaction selection, the scatter's
+// outgoing energy and direction cosine, the counters.  Returns COLL_ENDS when
+// the history ends here (absorption), otherwise the kind of the pending
+// second part.  SENS: the selected reaction adds d log Sigma_r / dtheta to the
+// history's scores S (stride `ss`).
 template <bool SENS>
-__device__ __forceinline__ bool collision_event(const DevTables& t, const DevTally& tally, Particle& p, int cls,
-                                                const DevStore& extra, uint32_t* cnt, const DevSens& sens,
-                                                double* S, int ss)
+__device__ __forceinline__ int collision_select(const DevTables& t, const DevTally& tally, Particle& p, int cls,
+                                                uint32_t* cnt, const DevSens& sens, double* S, int ss)
 {
     const int G = t.num_groups;
     const int K = t.max_reactions;
@@ -438,36 +447,53 @@ __device__ __forceinline__ bool collision_event(const DevTables& t, const DevTal
         const int k = __ldg(sens.param_of + ((int64_t)cls * G + p.group) * 3 + (type - 1));
         if (k >= 0) S[k * ss] += __ldg(sens.inv_theta + k);
     }
-    // 1.0 / mass of NuclearData.cc:64, divided once on the host (same bits)
-    const double inv_mass = __ldg(t.material_inv_mass + __ldg(t.class_material + cls));
-    double e_out[4], a_out[4];
-    int n_out = 0;
-    if (type == QSG_REACT_SCATTER) {
-        n_out = 1;
-        double rn = rng_sample(p.seed);
-        e_out[0] = p.kinetic_energy * (1.0 - (rn * inv_mass));
-        rn = rng_sample(p.seed) * 2.0 - 1.0;
-        a_out[0] = rn;
-    } else if (type == QSG_REACT_FISSION) {
-        int num = (int)(__ldg(t.class_reaction_nubar + cls * K + sel) + rng_sample(p.seed));
-        if (num > 4) num = 4;  // nuBar < 4 is checked at qsg_create
-        n_out = num;
-        for (int o = 0; o < num; o++) {
-            double rn = rng_sample(p.seed) / 2.0 + 0.5;
-            e_out[o] = (20 * rn * rn);
-            rn = rng_sample(p.seed) * 2.0 - 1.0;
-            a_out[o] = rn;
-        }
-    }
     cnt[LC_COLL]++;
-    if (type == QSG_REACT_SCATTER) cnt[LC_SCAT]++;
-    else if (type == QSG_REACT_ABSORPTION) cnt[LC_ABS]++;
-    else if (type == QSG_REACT_FISSION) {
-        cnt[LC_FIS]++;
-        cnt[LC_PROD] += (uint32_t)n_out;
+    if (type == QSG_REACT_SCATTER) {
+        cnt[LC_SCAT]++;
+        // 1.0 / mass of NuclearData.cc:64, divided once on the host (same bits)
+        const double inv_mass = __ldg(t.material_inv_mass + __ldg(t.class_material + cls));
+        double rn = rng_sample(p.seed);
+        p.pend_e = p.kinetic_energy * (1.0 - (rn * inv_mass));
+        rn = rng_sample(p.seed) * 2.0 - 1.0;
+        p.pend_a = rn;
+        return COLL_SCATTER;
     }
-    if (n_out == 0) return false;
-    for (int s = 1; s < n_out; s++) {
+    if (type == QSG_REACT_FISSION) {
+        cnt[LC_FIS]++;
+        p.pend_e = __ldg(t.class_reaction_nubar + cls * K + sel);
+        return COLL_FISSION;
+    }
+    if (type == QSG_REACT_ABSORPTION) cnt[LC_ABS]++;
+    return COLL_ENDS;
+}
+
+// Second part, run by the warp for its parked lanes together: fission
+// products (CollisionEvent.cc:125-142; products 1.. to the extra store, and
+// the particle itself too when there is more than one), the trajectory update
+// and the new energy group.  Returns true to keep tracking.  SENS: fission
+// products carry the scores along.
+template <bool SENS>
+__device__ __forceinline__ bool collision_finish(const DevTables& t, const DevTally& tally, Particle& p, int kind,
+                                                 const DevStore& extra, uint32_t* cnt, const DevSens& sens,
+                                                 double* S, int ss)
+{
+    if (kind == COLL_SCATTER) {
+        update_trajectory(p.pend_e, p.pend_a, p);
+        p.group = energy_group(t, p.kinetic_energy);
+        return true;
+    }
+    double e_out[4], a_out[4];
+    int num = (int)(p.pend_e + rng_sample(p.seed));
+    if (num > 4) num = 4;  // nuBar < 4 is checked at qsg_create
+    for (int o = 0; o < num; o++) {
+        double rn = rng_sample(p.seed) / 2.0 + 0.5;
+        e_out[o] = (20 * rn * rn);
+        rn = rng_sample(p.seed) * 2.0 - 1.0;
+        a_out[o] = rn;
+    }
+    cnt[LC_PROD] += (uint32_t)num;
+    if (num == 0) return false;
+    for (int s = 1; s < num; s++) {
         Particle sec = p;
         sec.seed = rng_spawn(p.seed);
         sec.identifier = sec.seed;
@@ -481,7 +507,7 @@ __device__ __forceinline__ bool collision_event(const DevTables& t, const DevTal
         }
     }
     update_trajectory(e_out[0], a_out[0], p);
-    if (n_out > 1) {
+    if (num > 1) {
         uint64_t slot = append_slot(extra);
         if (slot < extra.capacity) {
             store_particle(extra, slot, p);
@@ -491,7 +517,7 @@ __device__ __forceinline__ bool collision_event(const DevTables& t, const DevTal
         }
     }
     p.group = energy_group(t, p.kinetic_energy);
-    return n_out == 1;
+    return num == 1;
 }
 
 // MCT_Reflect_Particle, MCT.cc:400-430.
@@ -656,7 +682,11 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
     int cur_prob = -1;
     const uint64_t n = *in.count;
     Particle p;
-    bool active = false, exhausted = false, pending = false;
+    bool active = false, exhausted = false;
+    // collision stage of a parked lane: 0 none, 1 reaction selection pending,
+    // 2 trajectory update pending (kind in pend_kind)
+    int stage = 0;
+    int pend_kind = COLL_ENDS;
     double* flux_row = tally.flux;
     uint64_t segs_this_history = 0;
     uint64_t next = 0, end = 0;   // this lane's claimed run of queue positions
@@ -691,20 +721,49 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
         }
         if (__all_sync(0xffffffffu, !active)) break;
         // Deferred collisions: a lane whose segment ends in a collision parks
-        // its particle; the warp runs the collision code (log, sincos,
-        // rotation -- most of the FP64 work) once enough lanes are parked, or
-        // when nothing else can run.  A particle's own state and random stream
-        // are untouched while it waits, so the results are unchanged.
-        const unsigned pend_mask = __ballot_sync(0xffffffffu, active && pending);
-        const unsigned run_mask = __ballot_sync(0xffffffffu, active && !pending);
-        if (pend_mask != 0u && (__popc(pend_mask) >= tally.collision_batch || run_mask == 0u)) {
-            if (pending) {
-                pending = false;
-                active = collision_event<SENS>(t, tally, p, __ldg(t.cell_class + p.cell), extra, cnt, sens, S, BLOCK);
+        // its particle; the warp runs the collision work for its parked lanes
+        // together once enough of them wait, or when nothing else can run.  A
+        // particle's own state and random stream are untouched while it waits,
+        // so the results are unchanged.
+#if QSG_COLL_MODE == 2
+        // two levels: the reaction selection for parked lanes, then (only for
+        // scatter / fission, an absorption ends the history there) the
+        // trajectory update -- log, sincos, rotation, most of the FP64 work --
+        // so that absorbed lanes do not idle through it
+        const unsigned fin_mask = __ballot_sync(0xffffffffu, active && stage == 2);
+        const unsigned sel_mask = __ballot_sync(0xffffffffu, active && stage == 1);
+        const unsigned run_mask = __ballot_sync(0xffffffffu, active && stage == 0);
+        if (fin_mask != 0u && (__popc(fin_mask) >= tally.collision_batch || (run_mask | sel_mask) == 0u)) {
+            if (stage == 2) {
+                stage = 0;
+                active = collision_finish<SENS>(t, tally, p, pend_kind, extra, cnt, sens, S, BLOCK);
             }
             continue;
         }
-        if (active && !pending) {
+        if (sel_mask != 0u && (__popc(sel_mask) >= tally.collision_batch || run_mask == 0u)) {
+            if (stage == 1) {
+                pend_kind = collision_select<SENS>(t, tally, p, __ldg(t.cell_class + p.cell), cnt, sens, S, BLOCK);
+                stage = (pend_kind == COLL_ENDS) ? 0 : 2;
+                active = pend_kind != COLL_ENDS;
+            }
+            continue;
+        }
+#else
+        const unsigned pend_mask = __ballot_sync(0xffffffffu, active && stage != 0);
+        const unsigned run_mask = __ballot_sync(0xffffffffu, active && stage == 0);
+        if (pend_mask != 0u && (__popc(pend_mask) >= tally.collision_batch || run_mask == 0u)) {
+            if (stage != 0) {
+#if QSG_COLL_MODE == 0
+                pend_kind = collision_select<SENS>(t, tally, p, __ldg(t.cell_class + p.cell), cnt, sens, S, BLOCK);
+#endif
+                stage = 0;
+                active = (pend_kind != COLL_ENDS) &&
+                         collision_finish<SENS>(t, tally, p, pend_kind, extra, cnt, sens, S, BLOCK);
+            }
+            continue;
+        }
+#endif
+        if (active && stage == 0) {
             bool keep;
             const int cls = __ldg(t.cell_class + p.cell);
             int outcome = segment_outcome(t, tally, p, cls, flux_row);
@@ -712,8 +771,15 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
             cnt[LC_SEG]++;
             p.num_segments += 1.;
             if (outcome == OUT_COLLISION) {
-                pending = true;
+#if QSG_COLL_MODE == 1
+                // reaction selection right away: an absorption ends the history now
+                pend_kind = collision_select<SENS>(t, tally, p, cls, cnt, sens, S, BLOCK);
+                keep = pend_kind != COLL_ENDS;
+                stage = keep ? 2 : 0;
+#else
+                stage = 1;
                 keep = true;
+#endif
             } else if (outcome == OUT_FACET) {
                 // MC_Facet_Crossing_Event, MC_Facet_Crossing_Event.cc:23-70
                 const int64_t fi = (int64_t)p.cell * kFacets + p.facet;
@@ -760,10 +826,283 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
             if (keep && ++segs_this_history >= tally.max_segments) {
                 raise_flag(tally, QSG_DEV_SEGMENT_LIMIT);
                 keep = false;
-                pending = false;
+                stage = 0;
             }
             active = keep;
         }
+    }
+    bc.add_final(cur_prob, cnt);
+    bc.flush_block<BLOCK>();
+}
+
+// ------------------------------------------------------------------------
+// Particle-pool variant of the tracking pass.
+//
+// The lane-resident kernel above keeps one history per lane, so a warp's steps
+// run with the lanes whose particle happens to need that step (on config2
+// about 21 of 32 lanes in segment steps and 18 in collision steps), and an
+// FP64 warp instruction costs the FP64 pipe the same whatever its active
+// lanes.  Here each warp owns a pool of kPool particles in shared memory;
+// every step picks one kind of work -- a segment for particles ready to move,
+// or the collision (reaction selection + trajectory update) for particles
+// parked at a collision -- and hands up to 32 such particles to the lanes, so
+// steps run full while the pool holds enough of one kind.  Every particle
+// still follows its own history with its own random stream, in the
+// reference's order, so the results are those of the lane-resident kernel.
+constexpr int kPool = 64;                      // particles per warp
+constexpr int kPoolD = 20, kPoolU = 2, kPoolI = 12;
+constexpr size_t kPoolBytesPerWarp = (size_t)(kPoolD * 8 + kPoolU * 8 + kPoolI * 4) * kPool;
+enum { PD_X, PD_Y, PD_Z, PD_VX, PD_VY, PD_VZ, PD_A, PD_B, PD_G, PD_E, PD_W, PD_TTC, PD_AGE, PD_NMFP, PD_NSEG,
+       PD_SPEED, PD_SIG, PD_MFP, PD_PE, PD_PA };
+enum { PI_LAST, PI_NCOLL, PI_BREED, PI_SPECIES, PI_DOMAIN, PI_CELL, PI_FACET, PI_GROUP, PI_KEY, PI_PROB, PI_REP,
+       PI_SEGS };
+
+struct PoolView {
+    double* d;      // [kPoolD][kPool]
+    uint64_t* u;    // [2][kPool]: seed, identifier
+    int32_t* i;     // [kPoolI][kPool]
+};
+
+// Extra per-slot state the pool keeps beside the particle record.
+struct SlotState {
+    int prob, rep;
+    uint32_t segs;
+};
+
+__device__ __forceinline__ void pool_get(const PoolView& v, int s, Particle& p, SlotState& st)
+{
+    const double* d = v.d + s;
+    p.x = d[PD_X * kPool]; p.y = d[PD_Y * kPool]; p.z = d[PD_Z * kPool];
+    p.vx = d[PD_VX * kPool]; p.vy = d[PD_VY * kPool]; p.vz = d[PD_VZ * kPool];
+    p.alpha = d[PD_A * kPool]; p.beta = d[PD_B * kPool]; p.gamma = d[PD_G * kPool];
+    p.kinetic_energy = d[PD_E * kPool]; p.weight = d[PD_W * kPool];
+    p.time_to_census = d[PD_TTC * kPool]; p.age = d[PD_AGE * kPool];
+    p.num_mean_free_paths = d[PD_NMFP * kPool]; p.num_segments = d[PD_NSEG * kPool];
+    p.speed = d[PD_SPEED * kPool]; p.total_xs = d[PD_SIG * kPool]; p.mean_free_path = d[PD_MFP * kPool];
+    p.pend_e = d[PD_PE * kPool]; p.pend_a = d[PD_PA * kPool];
+    p.seed = v.u[s]; p.identifier = v.u[kPool + s];
+    const int32_t* i = v.i + s;
+    p.last_event = i[PI_LAST * kPool]; p.num_collisions = i[PI_NCOLL * kPool]; p.breed = i[PI_BREED * kPool];
+    p.species = i[PI_SPECIES * kPool]; p.domain = i[PI_DOMAIN * kPool]; p.cell = i[PI_CELL * kPool];
+    p.facet = i[PI_FACET * kPool]; p.group = i[PI_GROUP * kPool]; p.xs_key = i[PI_KEY * kPool];
+    st.prob = i[PI_PROB * kPool]; st.rep = i[PI_REP * kPool]; st.segs = (uint32_t)i[PI_SEGS * kPool];
+}
+
+__device__ __forceinline__ void pool_put(const PoolView& v, int s, const Particle& p, const SlotState& st)
+{
+    double* d = v.d + s;
+    d[PD_X * kPool] = p.x; d[PD_Y * kPool] = p.y; d[PD_Z * kPool] = p.z;
+    d[PD_VX * kPool] = p.vx; d[PD_VY * kPool] = p.vy; d[PD_VZ * kPool] = p.vz;
+    d[PD_A * kPool] = p.alpha; d[PD_B * kPool] = p.beta; d[PD_G * kPool] = p.gamma;
+    d[PD_E * kPool] = p.kinetic_energy; d[PD_W * kPool] = p.weight;
+    d[PD_TTC * kPool] = p.time_to_census; d[PD_AGE * kPool] = p.age;
+    d[PD_NMFP * kPool] = p.num_mean_free_paths; d[PD_NSEG * kPool] = p.num_segments;
+    d[PD_SPEED * kPool] = p.speed; d[PD_SIG * kPool] = p.total_xs; d[PD_MFP * kPool] = p.mean_free_path;
+    d[PD_PE * kPool] = p.pend_e; d[PD_PA * kPool] = p.pend_a;
+    v.u[s] = p.seed; v.u[kPool + s] = p.identifier;
+    int32_t* i = v.i + s;
+    i[PI_LAST * kPool] = p.last_event; i[PI_NCOLL * kPool] = p.num_collisions; i[PI_BREED * kPool] = p.breed;
+    i[PI_SPECIES * kPool] = p.species; i[PI_DOMAIN * kPool] = p.domain; i[PI_CELL * kPool] = p.cell;
+    i[PI_FACET * kPool] = p.facet; i[PI_GROUP * kPool] = p.group; i[PI_KEY * kPool] = p.xs_key;
+    i[PI_PROB * kPool] = st.prob; i[PI_REP * kPool] = st.rep; i[PI_SEGS * kPool] = (int32_t)st.segs;
+}
+
+// Position of the n-th (0-based) set bit of m; n < popcount(m).
+__device__ __forceinline__ int nth_set_bit(uint64_t m, int n)
+{
+    const uint32_t lo = (uint32_t)m;
+    const int c = __popc(lo);
+    uint32_t w32 = lo;
+    int base = 0;
+    if (n >= c) {
+        n -= c;
+        w32 = (uint32_t)(m >> 32);
+        base = 32;
+    }
+#pragma unroll
+    for (int w = 16; w > 0; w >>= 1) {
+        const uint32_t low = w32 & ((1u << w) - 1u);
+        const int cl = __popc(low);
+        if (n >= cl) {
+            n -= cl;
+            w32 >>= w;
+            base += w;
+        } else {
+            w32 = low;
+        }
+    }
+    return base;
+}
+
+// 64-bit OR of one bit per lane (bit < 0: none) over the warp.
+__device__ __forceinline__ uint64_t warp_bits(int bit)
+{
+    const uint32_t lo = __reduce_or_sync(0xffffffffu, (bit >= 0 && bit < 32) ? (1u << bit) : 0u);
+    const uint32_t hi = __reduce_or_sync(0xffffffffu, (bit >= 32) ? (1u << (bit - 32)) : 0u);
+    return ((uint64_t)hi << 32) | lo;
+}
+
+size_t track_pool_smem_bytes_per_block(int block, int num_problems, int K)
+{
+    const size_t counts = num_problems <= kSmemProblems ? (size_t)num_problems * LC_N * 8 : 0;
+    const int warps = block / 32;
+    return counts + (size_t)warps * kPoolBytesPerWarp + (size_t)warps * K * kPool * sizeof(double);
+}
+
+template <int BLOCK, bool SENS>
+__global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / BLOCK)
+    track_pool_kernel(DevTables t, DevTally tally, DevStore in, DevStore census, DevStore extra,
+                      unsigned long long* cursor, DevSens sens)
+{
+    extern __shared__ unsigned long long s_counts[];
+    BlockCounters bc;
+    const bool counts_in_smem = tally.num_problems <= kSmemProblems;
+    bc.smem = counts_in_smem ? s_counts : nullptr;
+    bc.tally = &tally;
+    bc.replica = (int)(blockIdx.x % (unsigned)tally.balance_replicas);
+    if (bc.smem)
+        for (int k = threadIdx.x; k < tally.num_problems * LC_N; k += BLOCK) s_counts[k] = 0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    char* pool_base = reinterpret_cast<char*>(s_counts + (counts_in_smem ? tally.num_problems * LC_N : 0));
+    char* mine = pool_base + (size_t)warp * kPoolBytesPerWarp;
+    PoolView v;
+    v.d = reinterpret_cast<double*>(mine);
+    v.u = reinterpret_cast<uint64_t*>(mine + (size_t)kPoolD * 8 * kPool);
+    v.i = reinterpret_cast<int32_t*>(mine + (size_t)(kPoolD + kPoolU) * 8 * kPool);
+    double* s_scores = nullptr;   // [K][kPool] of this warp
+    if (SENS)
+        s_scores = reinterpret_cast<double*>(pool_base + (size_t)(BLOCK / 32) * kPoolBytesPerWarp) +
+                   (size_t)warp * sens.K * kPool;
+    __syncthreads();
+    uint32_t cnt[LC_N];
+#pragma unroll
+    for (int k = 0; k < LC_N; k++) cnt[k] = 0;
+    int cur_prob = -1;
+    const uint64_t n = *in.count;
+    uint64_t ready = 0, coll = 0;   // warp-uniform slot masks
+    bool exhausted = false;
+    for (;;) {
+        // refill empty slots from the work queue (warp-aggregated claim)
+        const uint64_t empty = ~(ready | coll);
+        const int n_empty = __popcll(empty);
+        if (!exhausted && n_empty > 0 &&
+            (n_empty >= 16 || (__popcll(ready) < 32 && __popcll(coll) < 32))) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(cursor, (unsigned long long)n_empty);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base + (unsigned long long)n_empty >= n) exhausted = true;
+            int filled = -1, filled2 = -1;
+            for (int k = lane; k < n_empty; k += 32) {
+                const uint64_t i = base + (uint64_t)k;
+                if (i >= n) break;
+                const int slot = nth_set_bit(empty, k);
+                Particle p;
+                load_particle(t, in, i, p);
+                if (!(p.speed > 0.0)) raise_flag(tally, QSG_DEV_BAD_FACET);
+                SlotState st;
+                st.prob = tally.cell_problem ? __ldg(tally.cell_problem + p.cell) : 0;
+                // CycleTracking.cc:37-39 replica selection by particle index
+                st.rep = (int)(i % (uint64_t)tally.flux_replicas);
+                st.segs = 0;
+                p.pend_e = 0.0;
+                p.pend_a = 0.0;
+                pool_put(v, slot, p, st);
+                if (SENS) load_scores(in, i, s_scores + slot, kPool, sens.K);
+                if (k < 32) filled = slot;
+                else filled2 = slot;
+            }
+            ready |= warp_bits(filled) | warp_bits(filled2);
+        }
+        const int nr = __popcll(ready), nc = __popcll(coll);
+        if (nr == 0 && nc == 0) {
+            if (exhausted) break;
+            continue;
+        }
+        const bool do_coll = (nc >= 32) || (nc > nr);
+        const uint64_t sel = do_coll ? coll : ready;
+        const int nsel = do_coll ? nc : nr;
+        int slot = -1, next_state = 0;   // 0 empty, 1 ready, 2 collision pending
+        if (lane < nsel) {
+            slot = nth_set_bit(sel, lane);
+            Particle p;
+            SlotState st;
+            pool_get(v, slot, p, st);
+            if (st.prob != cur_prob) {
+                if (cur_prob >= 0) bc.add(cur_prob, cnt);
+                cur_prob = st.prob;
+            }
+            double* S = SENS ? s_scores + slot : nullptr;
+            const int cls = __ldg(t.cell_class + p.cell);
+            if (do_coll) {
+                // CollisionEvent, both parts (see collision_select / collision_finish)
+                const int kind = collision_select<SENS>(t, tally, p, cls, cnt, sens, S, kPool);
+                const bool alive = (kind != COLL_ENDS) &&
+                                   collision_finish<SENS>(t, tally, p, kind, extra, cnt, sens, S, kPool);
+                next_state = alive ? 1 : 0;
+            } else {
+                double* flux_row = tally.flux + (int64_t)st.rep * t.num_cells * t.num_groups;
+                const int outcome = segment_outcome(t, tally, p, cls, flux_row);
+                if (SENS) sens_segment(t, sens, p, cls, outcome == OUT_COLLISION, S, kPool);
+                cnt[LC_SEG]++;
+                p.num_segments += 1.;
+                if (outcome == OUT_COLLISION) {
+                    next_state = 2;
+                } else if (outcome == OUT_FACET) {
+                    // MC_Facet_Crossing_Event, MC_Facet_Crossing_Event.cc:23-70
+                    const int64_t fi = (int64_t)p.cell * kFacets + p.facet;
+                    const uint8_t fe = __ldg(t.adj_facet_event + fi);
+                    const int ev = fe >> 5;
+                    if (ev == QSG_ADJ_TRANSIT_ON_PROCESSOR) {
+                        p.cell = __ldg(t.adj_cell + fi);
+                        p.facet = fe & 31;
+                        p.last_event = QSG_EVENT_FACET_TRANSIT_EXIT;
+                        next_state = 1;
+                    } else if (ev == QSG_ADJ_BOUNDARY_ESCAPE) {
+                        cnt[LC_ESC]++;
+                        if (SENS) {
+                            atomicAdd(sens.leak + st.prob, p.weight);
+                            for (int k = 0; k < sens.K; k++) {
+                                const double sv = S[k * kPool];
+                                if (sv != 0.0) atomicAdd(sens.dleak + (int64_t)st.prob * sens.K + k, p.weight * sv);
+                            }
+                        }
+                        p.last_event = QSG_EVENT_FACET_ESCAPE;
+                        p.species = -1;
+                        next_state = 0;
+                    } else if (ev == QSG_ADJ_BOUNDARY_REFLECTION) {
+                        p.last_event = QSG_EVENT_FACET_REFLECTION;
+                        reflect_particle(t, p);
+                        next_state = 1;
+                    } else {
+                        raise_flag(tally, QSG_DEV_OFF_PROCESSOR);
+                        next_state = 0;
+                    }
+                } else {
+                    // census: ParticleVault::pushParticle (ParticleVault.hh:86-93)
+                    uint64_t cs = append_slot(census);
+                    if (cs < census.capacity) {
+                        store_particle(census, cs, p);
+                        if (SENS) store_scores(census, cs, S, kPool, sens.K);
+                    } else {
+                        raise_flag(tally, QSG_DEV_STORE_OVERFLOW);
+                    }
+                    cnt[LC_CEN]++;
+                    next_state = 0;
+                }
+                if (next_state != 0 && (uint64_t)(++st.segs) >= tally.max_segments) {
+                    raise_flag(tally, QSG_DEV_SEGMENT_LIMIT);
+                    next_state = 0;
+                }
+            }
+            if (next_state != 0) pool_put(v, slot, p, st);
+        }
+        const uint64_t taken = warp_bits(slot);
+        const uint64_t now_ready = warp_bits(next_state == 1 ? slot : -1);
+        const uint64_t now_coll = warp_bits(next_state == 2 ? slot : -1);
+        if (do_coll) coll &= ~taken;
+        else ready &= ~taken;
+        ready |= now_ready;
+        coll |= now_coll;
     }
     bc.add_final(cur_prob, cnt);
     bc.flush_block<BLOCK>();
@@ -809,6 +1148,8 @@ size_t track_smem_bytes_sens(const QsgHandle* h)
     return track_smem_bytes(h) + (size_t)h->sens.K * h->block_size * sizeof(double);
 }
 
+size_t track_pool_smem_bytes_per_block(int block, int num_problems, int K);
+
 // Persistent grid for the current block size: SMs x resident blocks.
 int configure_track_grid(QsgHandle* h)
 {
@@ -831,6 +1172,18 @@ int configure_track_grid(QsgHandle* h)
             QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel<128, true>, 128, ss));
         }
         h->sens_track_blocks = h->num_sms * (per_sm > 0 ? per_sm : 1);
+    }
+    // particle-pool kernels (their pools live in dynamic shared memory)
+    for (int sens = 0; sens < 2; sens++) {
+        if (sens && h->sens.K == 0) continue;
+        const size_t ps = track_pool_smem_bytes_per_block(h->block_size, h->num_problems, sens ? h->sens.K : 0);
+        const void* fn = h->block_size == 256
+                             ? (sens ? (const void*)track_pool_kernel<256, true> : (const void*)track_pool_kernel<256, false>)
+                             : (sens ? (const void*)track_pool_kernel<128, true> : (const void*)track_pool_kernel<128, false>);
+        QSG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps));
+        per_sm = 0;
+        QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, h->block_size, ps));
+        (sens ? h->pool_sens_blocks : h->pool_blocks) = h->num_sms * (per_sm > 0 ? per_sm : 1);
     }
     return QSG_OK;
 }
@@ -1117,7 +1470,27 @@ int launch_pass(QsgHandle* h, cudaStream_t s)
     QSG_CUDA(cudaMemsetAsync(h->extra.count, 0, sizeof(unsigned long long), s));
     QSG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s));
     const DevTally tv = tally_view(h);
-    if (h->sens.K > 0) {
+    if (h->kernel_kind == 1) {
+        const bool sens = h->sens.K > 0;
+        const size_t ps = track_pool_smem_bytes_per_block(h->block_size, h->num_problems, h->sens.K);
+        const int grid = sens ? h->pool_sens_blocks : h->pool_blocks;
+        const DevSens ds = sens ? h->sens : DevSens{};
+        if (h->block_size == 256) {
+            if (sens)
+                track_pool_kernel<256, true><<<grid, 256, ps, s>>>(h->tables, tv, h->processing.view, h->processed.view,
+                                                                   h->extra.view, cursor, ds);
+            else
+                track_pool_kernel<256, false><<<grid, 256, ps, s>>>(h->tables, tv, h->processing.view,
+                                                                    h->processed.view, h->extra.view, cursor, ds);
+        } else {
+            if (sens)
+                track_pool_kernel<128, true><<<grid, 128, ps, s>>>(h->tables, tv, h->processing.view, h->processed.view,
+                                                                   h->extra.view, cursor, ds);
+            else
+                track_pool_kernel<128, false><<<grid, 128, ps, s>>>(h->tables, tv, h->processing.view,
+                                                                    h->processed.view, h->extra.view, cursor, ds);
+        }
+    } else if (h->sens.K > 0) {
         const size_t smem = track_smem_bytes_sens(h);
         if (h->block_size == 256)
             track_kernel<256, true><<<h->sens_track_blocks, 256, smem, s>>>(
@@ -1312,6 +1685,15 @@ extern "C" int qsg_set_tuning(QsgHandle* h, int32_t block_size, int32_t collisio
     if (queue_chunk > 0) h->queue_chunk = std::min<int>(queue_chunk, 1024);
     h->clear_graphs();   // captured launches carry the old shape
     return configure_track_grid(h);
+}
+
+extern "C" int qsg_set_track_kernel(QsgHandle* h, int32_t kind)
+{
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_set_track_kernel: null handle");
+    if (kind != 0 && kind != 1) return fail(QSG_ERR_INVALID, "qsg_set_track_kernel: kind must be 0 or 1");
+    h->kernel_kind = kind;
+    h->clear_graphs();   // captured launches carry the old kernel
+    return QSG_OK;
 }
 
 extern "C" int qsg_destroy(QsgHandle* h)

@@ -27,6 +27,12 @@ constexpr int kFacets = 24;
 #ifndef QSG_MIN_BLOCKS
 #define QSG_MIN_BLOCKS 3
 #endif
+// How a warp batches its collisions: 0 = selection and trajectory update in
+// one batched step; 1 = selection right after the segment, trajectory update
+// batched; 2 = both batched, in two levels.
+#ifndef QSG_COLL_MODE
+#define QSG_COLL_MODE 0
+#endif
 #ifndef QSG_COLLISION_BATCH
 #define QSG_COLLISION_BATCH 16
 #endif
@@ -198,6 +204,9 @@ struct Particle {
     double speed;                  // < 0: stale
     int32_t xs_key;                // -1: stale
     double seg_len;                // length of the last segment (MC_Particle::segment_path_length)
+    // a collision waiting for its warp's batched trajectory update: scatter's
+    // outgoing energy and direction cosine, or the fission reaction's nuBar
+    double pend_e, pend_a;
 };
 
 __device__ __forceinline__ void load_particle(const DevTables& t, const DevStore& s, uint64_t i, Particle& p)
