@@ -320,9 +320,8 @@ __device__ __forceinline__ int segment_outcome(const DevTables& t, const DevTall
     }
     const int key = cls * t.num_groups + p.group;
     if (key != p.xs_key) {
-        const double sigma = __ldg(t.sigma_total + key);
-        p.total_xs = sigma;
-        p.mean_free_path = (sigma == 0.0) ? kHugeDouble : 1.0 / sigma;
+        p.total_xs = __ldg(t.sigma_total + key);
+        p.mean_free_path = __ldg(t.mfp_table + key);   // same bits as the reference's 1.0 / sigma
         p.xs_key = key;
     }
     if (p.num_mean_free_paths == 0.0) {
@@ -849,7 +848,12 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
 // steps run full while the pool holds enough of one kind.  Every particle
 // still follows its own history with its own random stream, in the
 // reference's order, so the results are those of the lane-resident kernel.
-constexpr int kPool = 64;                      // particles per warp
+#ifndef QSG_POOL
+#define QSG_POOL 64
+#endif
+constexpr int kPool = QSG_POOL;                // particles per warp (at most 64: one bit each in a mask)
+static_assert(kPool >= 32 && kPool <= 64, "pool size");
+constexpr uint64_t kPoolMask = kPool == 64 ? ~0ull : ((1ull << kPool) - 1ull);
 constexpr int kPoolD = 20, kPoolU = 2, kPoolI = 12;
 constexpr size_t kPoolBytesPerWarp = (size_t)(kPoolD * 8 + kPoolU * 8 + kPoolI * 4) * kPool;
 enum { PD_X, PD_Y, PD_Z, PD_VX, PD_VY, PD_VZ, PD_A, PD_B, PD_G, PD_E, PD_W, PD_TTC, PD_AGE, PD_NMFP, PD_NSEG,
@@ -983,7 +987,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
     bool exhausted = false;
     for (;;) {
         // refill empty slots from the work queue (warp-aggregated claim)
-        const uint64_t empty = ~(ready | coll);
+        const uint64_t empty = ~(ready | coll) & kPoolMask;
         const int n_empty = __popcll(empty);
         if (!exhausted && n_empty > 0 &&
             (n_empty >= 16 || (__popcll(ready) < 32 && __popcll(coll) < 32))) {
@@ -1352,6 +1356,11 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
     std::vector<double> mass(p->num_materials);
     for (int m = 0; m < p->num_materials; m++) mass[m] = 1.0 / p->material_mass[m];
     int st;
+    // mean free path per (class, group): the reference's 1.0 / sigma, an IEEE
+    // division whose bits the host reproduces
+    std::vector<double> mfp(sigma_total.size());
+    for (size_t k = 0; k < mfp.size(); k++) mfp[k] = (sigma_total[k] == 0.0) ? kHugeDouble : 1.0 / sigma_total[k];
+    if ((st = h->mfp_table.upload(mfp))) return st;
     if ((st = h->energies.upload(energies)) || (st = h->sigma_total.upload(sigma_total)) ||
         (st = h->macro_xs.upload(macro)) || (st = h->class_nubar.upload(nubar)) ||
         (st = h->material_mass.upload(mass)) || (st = h->cell_nodes.upload(nodes)) ||
@@ -1372,6 +1381,21 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
     t.max_reactions = K;
     t.energies = h->energies.ptr;
     t.sigma_total = h->sigma_total.ptr;
+    t.mfp_table = h->mfp_table.ptr;
+    // group hint: accepted when every edge but the last lies within a quarter
+    // group of the log-linear fit through the first two
+    t.group_hint_ln0 = 0.0f;
+    t.group_hint_scale = 0.0f;
+    if (G >= 2 && energies[0] > 0.0 && energies[1] > energies[0]) {
+        const double ln0 = std::log(energies[0]), delta = std::log(energies[1]) - ln0;
+        bool ok = delta > 0.0;
+        for (int k = 0; ok && k <= G - 1; k++)
+            ok = energies[k] > 0.0 && std::fabs(std::log(energies[k]) - (ln0 + k * delta)) < 0.25 * delta;
+        if (ok) {
+            t.group_hint_ln0 = (float)ln0;
+            t.group_hint_scale = (float)(1.0 / delta);
+        }
+    }
     t.macro_xs = h->macro_xs.ptr;
     t.class_num_reactions = h->class_num_reactions.ptr;
     t.class_material = h->class_material.ptr;
@@ -1700,7 +1724,7 @@ extern "C" int qsg_destroy(QsgHandle* h)
 {
     if (!h) return QSG_OK;
     cudaSetDevice(h->device);
-    h->energies.free(); h->sigma_total.free(); h->macro_xs.free(); h->class_nubar.free();
+    h->energies.free(); h->sigma_total.free(); h->mfp_table.free(); h->macro_xs.free(); h->class_nubar.free();
     h->material_mass.free(); h->cell_nodes.free(); h->cell_center.free(); h->planes.free();
     h->class_num_reactions.free(); h->class_material.free(); h->cell_class.free(); h->adj_cell.free();
     h->class_type.free(); h->adj_facet_event.free();

@@ -87,6 +87,10 @@ struct DevTables {
     int32_t max_reactions;         // K: reactions per cross-section class row
     const double* energies;        // [G+1]
     const double* sigma_total;     // [classes][G]  weightedMacroscopicCrossSection values
+    const double* mfp_table;       // [classes][G]  1/Sigma_t, or _hugeDouble when Sigma_t = 0 (MC_Segment_Outcome.cc:129-131)
+    // energy-group hint for log-spaced grids: group ~ (ln E - ln E_0) * scale
+    // (scale = 0: no hint); the exact search below confirms it
+    float group_hint_ln0, group_hint_scale;
     const double* macro_xs;        // [classes][G][K] macroscopicCrossSection per (iso, reaction)
     const int32_t* class_num_reactions;  // [classes]
     const int32_t* class_material;       // [classes]
@@ -182,6 +186,20 @@ __device__ __forceinline__ int energy_group(const DevTables& t, double e)
     const double* en = t.energies;
     if (e <= __ldg(en)) return 0;
     if (e > __ldg(en + n - 1)) return n - 1;
+    // The binary search below returns the largest k <= n-2 with en[k] <= e.
+    // On a log-spaced grid a float estimate lands within a group of it; two
+    // exact comparisons on each side confirm it, else the search runs.
+    if (t.group_hint_scale > 0.0f) {
+        int g = (int)((__logf((float)e) - t.group_hint_ln0) * t.group_hint_scale);
+        g = max(0, min(g, n - 2));
+        if (__ldg(en + g) <= e) {
+            if (g + 1 > n - 2 || e < __ldg(en + g + 1)) return g;
+            if (g + 2 > n - 2 || e < __ldg(en + g + 2)) return g + 1;
+        } else {
+            if (g >= 1 && __ldg(en + g - 1) <= e) return g - 1;
+            if (g >= 2 && __ldg(en + g - 2) <= e) return g - 2;
+        }
+    }
     int high = n - 1, low = 0;
     while (high != low + 1) {
         int mid = (high + low) / 2;
