@@ -46,7 +46,7 @@ WORKLOAD = ("config2: 40^3-cell 40 cm cube, 3 materials in spherical shells (r=8
             "3 reactions each, polynomial cross sections, 230 groups, 1e6 particles, FP64")
 METRIC = "segments/s per cycle on 1 GB300; batched+adjoint vs plain at matched tally error"
 B_ALG_PER_SEGMENT = 288          # algorithmic HBM bytes per segment (136-B record read+write + 16-B flux RMW)
-PROFILE_SUMMARY = ROOT / "profiles" / "track_kernel_config2.md"
+PROFILE_SUMMARY = ROOT / "profiles" / "track_pool_kernel_config2.md"
 
 
 def dist_env():

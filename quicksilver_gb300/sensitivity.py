@@ -163,5 +163,31 @@ def tallies(theta, deck: Deck, params, n_steps: int | None = None, seed_offset: 
     return _TALLY_FUNCTION.apply(theta, deck, list(params), n_steps, seed_offset, options)
 
 
+def main(argv=None) -> None:
+    """``python -m quicksilver_gb300.sensitivity DECK [--steps N] [--split-mev E]``:
+    run the deck with one parameter per (material, {scatter, absorption},
+    energy band) and print the total flux, the leakage and their derivatives."""
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("deck")
+    ap.add_argument("--steps", type=int, default=None, help="cycles (default: the deck's nSteps)")
+    ap.add_argument("--split-mev", type=float, default=1.0)
+    args = ap.parse_args(argv)
+    deck = Deck.from_file(args.deck)
+    hp = deck.build()
+    params = band_params(hp.array("energies"), hp.num_materials, split_mev=args.split_mev)
+    hp.close()
+    res = run_sensitivity(deck, params, args.steps)
+    print(json.dumps({"segments": res["segments"], "flux_total": float(res["flux_cell"].sum()),
+                      "leak": float(res["leak"].sum()),
+                      "dflux_total": res["dflux"].sum(axis=0).tolist(), "dleak": res["dleak"].sum(axis=0).tolist(),
+                      "params": [[p.material, p.reaction, p.group_lo, p.group_hi] for p in params]}))
+
+
+if __name__ == "__main__":
+    main()
+
+
 __all__ = ["Param", "SCATTER", "ABSORPTION", "FISSION", "band_params", "with_theta", "scaled_problem",
            "tie_across_problems", "run_sensitivity", "tallies"]
