@@ -311,6 +311,87 @@ def measure_adjoint(replicas=6):
             "timing": "wall clock of MonteCarlo.run (20 whole cycles), synchronised; handle set-up excluded"}
 
 
+def run_config5(args):
+    """--workload config5: the large batched + differentiated run -- 8 replicas
+    of a 5-slab 64^3-cell problem (1e7 particles each, distinct seeds, escape
+    boundaries, 230 groups), 20 parameters (5 materials x {scatter,
+    absorption} x 2 bands) tied across the replicas, every cycle one CUDA
+    graph whose tracking pass is one persistent launch over all replicas with
+    forward tallies and sensitivities.  20 timed cycles after 1 warm-up cycle;
+    then 5 cycles with the sensitivities switched off give the forward-only
+    rate of the same batch.  The replicas' spread gives the standard error of
+    each derivative."""
+    import torch
+    from quicksilver_gb300 import Deck
+    from quicksilver_gb300.decks.make_decks import config5
+    from quicksilver_gb300.monte_carlo import BatchMonteCarlo, seed_offset
+    from quicksilver_gb300.sensitivity import band_params, tie_across_problems
+    from quicksilver_gb300 import _native as N
+    n_part = int(round(1e7 * args.config5_scale))
+    decks = [Deck.from_string(t) for t in config5(n_particles=n_part)]
+    t0 = time.perf_counter()
+    problems = [d.build() for d in decks]
+    build_s = time.perf_counter() - t0
+    offs = [seed_offset(d.simulation.seed) for d in decks]
+    cap = int(1.3 * (n_part + n_part // 10)) + 1024
+    cycles = decks[0].simulation.n_steps
+    base = band_params(problems[0].array("energies"), problems[0].num_materials)
+    t0 = time.perf_counter()
+    bmc = BatchMonteCarlo(decks, problems=problems, seed_offsets=offs, store_capacity=cap, max_passes=2)
+    params = tie_across_problems(base, bmc.tracker.material_offsets())
+    bmc.tracker.enable_sensitivity(params)
+    setup_s = time.perf_counter() - t0
+    bmc.run(1, use_graph=True)
+    bmc.tracker.reset_sensitivity()
+    first = bmc.cycles
+    with ClockSampler(0) as clocks:
+        _sync()
+        t0 = time.perf_counter()
+        bmc.run_cycles(cycles, use_graph=True)
+        _sync()
+        t_sens = time.perf_counter() - t0
+    hist = bmc.history(first, cycles)
+    seg = hist.segments()
+    sens = bmc.tracker.read_sensitivity()
+    flags = bmc.device_status()
+    # forward-only rate of the same batch
+    N.check(N.lib().qsg_enable_sensitivity(bmc.tracker.handle, C.byref(N.QsgSensitivity())))
+    bmc.run(1, use_graph=True)
+    first2 = bmc.cycles
+    _sync()
+    t0 = time.perf_counter()
+    bmc.run_cycles(5, use_graph=True)
+    _sync()
+    t_plain = time.perf_counter() - t0
+    seg_plain = bmc.history(first2, 5).segments()
+    flags |= bmc.device_status()
+    coff = bmc.tracker.cell_offsets
+    bmc.close()
+    P, K = len(decks), len(params)
+    dflux_p = np.array([sens["dflux"][int(coff[q]):int(coff[q + 1])].sum(axis=0) for q in range(P)])
+    se = lambda a: (a.std(axis=0, ddof=1) / np.sqrt(P)).tolist()
+    line = {
+        "metric": METRIC, "value": seg / t_sens, "unit": "segments/s", "n_gpus": 1, "steps": cycles, "warmup": 1,
+        # (each cell sources floor(volume x rate x dt / particle weight) particles, so the
+        # 64^3 mesh needs >= 3e6 particles per replica for any source at all)
+        "ms_per_step": 1e3 * t_sens / cycles, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded decks make_decks.config5)",
+        "config": {"workload": f"config5: 8 replicas x 64^3-cell 64 cm cube, 5 slabs along z, 5 materials, escape "
+                               f"boundaries, 230 groups, {n_part:.0e} particles each, 20 cycles, {K} parameters tied "
+                               f"across replicas", "step": "one whole cycle (CUDA graph) with sensitivities",
+                   "timing": "wall clock of 20 graph replays, synchronised", "build_s": build_s, "setup_s": setup_s},
+        "forms": {"batched_adjoint_segments_per_s": seg / t_sens, "batched_forward_segments_per_s": seg_plain / t_plain,
+                  "adjoint_time_over_forward": (t_sens / seg) / (t_plain / seg_plain) if seg and seg_plain else None,
+                  "segments": seg, "leak_mean": float(sens["leak"].mean()),
+                  "dflux_total_mean": dflux_p.mean(axis=0).tolist(), "dflux_total_se": se(dflux_p),
+                  "dleak_mean": sens["dleak"].mean(axis=0).tolist(), "dleak_se": se(sens["dleak"])},
+        "gpu_launches": cycles * 9, "device_flags": flags, "clocks": clocks.summary(),
+    }
+    for hp in problems:
+        hp.close()
+    print(json.dumps(line), flush=True)
+
+
 def run_reference_arm(args, world, rank):
     """--impl reference: the CPU port of the reference algorithm on the host cores."""
     if rank != 0:
@@ -359,6 +440,10 @@ def main():
     ap.add_argument("--flux-replicas", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and differentiated forms")
+    ap.add_argument("--workload", default="config2", choices=["config2", "config5"],
+                    help="config5: the large batched + differentiated run (its own JSON line)")
+    ap.add_argument("--config5-scale", type=float, default=1.0,
+                    help="particle-count scale of config5 (>= 0.3: below that no cell sources a particle)")
     ap.add_argument("--kernel", type=int, default=1, choices=[0, 1],
                     help="tracking kernel: 1 warp particle pool (default), 0 one history per lane")
     args = ap.parse_args()
@@ -367,6 +452,10 @@ def main():
 
     if args.impl == "reference":
         run_reference_arm(args, world, rank)
+        return
+    if args.workload == "config5":
+        if rank == 0:
+            run_config5(args)
         return
 
     import torch

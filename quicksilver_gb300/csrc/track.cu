@@ -848,14 +848,20 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
 // steps run full while the pool holds enough of one kind.  Every particle
 // still follows its own history with its own random stream, in the
 // reference's order, so the results are those of the lane-resident kernel.
+// Particles per warp (one bit each in a 64-bit mask): 64 for the plain
+// kernel; 48 with sensitivity scores, whose shared memory would otherwise
+// leave room for only 2 blocks per SM.
 #ifndef QSG_POOL
 #define QSG_POOL 64
 #endif
-constexpr int kPool = QSG_POOL;                // particles per warp (at most 64: one bit each in a mask)
-static_assert(kPool >= 32 && kPool <= 64, "pool size");
-constexpr uint64_t kPoolMask = kPool == 64 ? ~0ull : ((1ull << kPool) - 1ull);
+#ifndef QSG_POOL_SENS
+#define QSG_POOL_SENS 48
+#endif
+constexpr int kPoolPlain = QSG_POOL, kPoolSens = QSG_POOL_SENS;
+static_assert(kPoolPlain >= 32 && kPoolPlain <= 64 && kPoolSens >= 32 && kPoolSens <= 64, "pool size");
 constexpr int kPoolD = 20, kPoolU = 2, kPoolI = 12;
-constexpr size_t kPoolBytesPerWarp = (size_t)(kPoolD * 8 + kPoolU * 8 + kPoolI * 4) * kPool;
+__host__ __device__ constexpr size_t pool_bytes_per_warp(int pool) { return (size_t)(kPoolD * 8 + kPoolU * 8 + kPoolI * 4) * pool; }
+__host__ __device__ constexpr uint64_t pool_mask(int pool) { return pool == 64 ? ~0ull : ((1ull << pool) - 1ull); }
 enum { PD_X, PD_Y, PD_Z, PD_VX, PD_VY, PD_VZ, PD_A, PD_B, PD_G, PD_E, PD_W, PD_TTC, PD_AGE, PD_NMFP, PD_NSEG,
        PD_SPEED, PD_SIG, PD_MFP, PD_PE, PD_PA };
 enum { PI_LAST, PI_NCOLL, PI_BREED, PI_SPECIES, PI_DOMAIN, PI_CELL, PI_FACET, PI_GROUP, PI_KEY, PI_PROB, PI_REP,
@@ -873,6 +879,7 @@ struct SlotState {
     uint32_t segs;
 };
 
+template <int kPool>
 __device__ __forceinline__ void pool_get(const PoolView& v, int s, Particle& p, SlotState& st)
 {
     const double* d = v.d + s;
@@ -892,6 +899,7 @@ __device__ __forceinline__ void pool_get(const PoolView& v, int s, Particle& p, 
     st.prob = i[PI_PROB * kPool]; st.rep = i[PI_REP * kPool]; st.segs = (uint32_t)i[PI_SEGS * kPool];
 }
 
+template <int kPool>
 __device__ __forceinline__ void pool_put(const PoolView& v, int s, const Particle& p, const SlotState& st)
 {
     double* d = v.d + s;
@@ -950,7 +958,8 @@ size_t track_pool_smem_bytes_per_block(int block, int num_problems, int K)
 {
     const size_t counts = num_problems <= kSmemProblems ? (size_t)num_problems * LC_N * 8 : 0;
     const int warps = block / 32;
-    return counts + (size_t)warps * kPoolBytesPerWarp + (size_t)warps * K * kPool * sizeof(double);
+    const int pool = K > 0 ? kPoolSens : kPoolPlain;
+    return counts + (size_t)warps * pool_bytes_per_warp(pool) + (size_t)warps * K * pool * sizeof(double);
 }
 
 template <int BLOCK, bool SENS>
@@ -958,6 +967,9 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
     track_pool_kernel(DevTables t, DevTally tally, DevStore in, DevStore census, DevStore extra,
                       unsigned long long* cursor, DevSens sens)
 {
+    constexpr int kPool = SENS ? kPoolSens : kPoolPlain;
+    constexpr size_t kPoolBytesPerWarp = pool_bytes_per_warp(kPool);
+    constexpr uint64_t kPoolMask = pool_mask(kPool);
     extern __shared__ unsigned long long s_counts[];
     BlockCounters bc;
     const bool counts_in_smem = tally.num_problems <= kSmemProblems;
@@ -1010,7 +1022,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
                 st.segs = 0;
                 p.pend_e = 0.0;
                 p.pend_a = 0.0;
-                pool_put(v, slot, p, st);
+                pool_put<kPool>(v, slot, p, st);
                 if (SENS) load_scores(in, i, s_scores + slot, kPool, sens.K);
                 if (k < 32) filled = slot;
                 else filled2 = slot;
@@ -1030,7 +1042,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
             slot = nth_set_bit(sel, lane);
             Particle p;
             SlotState st;
-            pool_get(v, slot, p, st);
+            pool_get<kPool>(v, slot, p, st);
             if (st.prob != cur_prob) {
                 if (cur_prob >= 0) bc.add(cur_prob, cnt);
                 cur_prob = st.prob;
@@ -1098,7 +1110,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
                     next_state = 0;
                 }
             }
-            if (next_state != 0) pool_put(v, slot, p, st);
+            if (next_state != 0) pool_put<kPool>(v, slot, p, st);
         }
         const uint64_t taken = warp_bits(slot);
         const uint64_t now_ready = warp_bits(next_state == 1 ? slot : -1);

@@ -17,6 +17,8 @@ fixed numpy seed, so the decks are reproducible.  Benchmark workloads:
 * ``config4.inp``  config-1 box and mesh with 3 materials (spheres of radius
   2 and 4 cm about the centre), escape boundaries, 1e6 particles, 20 cycles;
   numpy default_rng(4).
+* ``config3()`` / ``config5()`` return deck strings (64 uneven problems; 8
+  replicas of a 5-slab 64^3 problem) instead of writing files.
 
 Test decks (small, seconds on one CPU core): limit cases mirroring the
 reference's example physics (all-absorb, all-escape, no-collision,
@@ -124,6 +126,23 @@ def config3(n_problems: int = 64, seed: int = 3) -> list:
                 geo + drawn_materials(rng, names))
         decks.append(text)
     return decks
+
+
+def config5(n_replicas: int = 8, seed: int = 5, n_particles: int = 10_000_000) -> list:
+    """The large batched + differentiated run: n_replicas copies of a 64^3-cell
+    64 cm cube made of 5 slabs along z (thicknesses 64 x a Dirichlet(1,...,1)
+    draw), 5 materials with config-2-style cross sections, 230 groups, escape
+    boundaries, 1e7 particles, 20 cycles; replica r carries deck seed 5 + r
+    (numpy default_rng(seed) draws the geometry and the materials once)."""
+    rng = np.random.default_rng(seed)
+    z = np.concatenate([[0.0], np.cumsum(rng.dirichlet(np.ones(5)) * 64.0)])
+    z[-1] = 64.0
+    names = [f"slab{k}" for k in range(5)]
+    geo = "".join(brick(names[k], 0, 64, 0, 64, repr(float(z[k])), repr(float(z[k + 1]))) for k in range(5))
+    mats = drawn_materials(rng, names)
+    return [simulation(boundaryCondition="escape", lx=64, ly=64, lz=64, nx=64, ny=64, nz=64,
+                       nParticles=n_particles, nSteps=20, seed=seed + r) + geo + mats
+            for r in range(n_replicas)]
 
 
 def small(**kw) -> str:
