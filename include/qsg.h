@@ -237,6 +237,22 @@ int qsg_cycle_history(QsgHandle* h, uint64_t first, uint64_t n, uint64_t* balanc
 /* Copy the processing store (e.g. after qsg_cycle_init) to host arrays. */
 int qsg_get_processing(QsgHandle* h, QsgParticleSoA* host, uint64_t cap, uint64_t* n_out);
 
+/* ---- observability: fluence and census energy spectrum ----------------- */
+/* Tallies kept across cycles by qsg_cycle_finalize when switched on:
+ *   QSG_OBSERVE_FLUENCE   per-cell fluence, the replica-summed scalar flux of
+ *     every cycle added group by group to the cell's running total
+ *     (Fluence::compute, Tallies.cc:92,100-118; the reference keeps it for the
+ *     CORAL2 decks' FluenceTest, CoralBenchmark.cc:177-228);
+ *   QSG_OBSERVE_SPECTRUM  per-problem histogram [G+1] of the energy groups of
+ *     the particles left in the stores at the end of each cycle (the census;
+ *     EnergySpectrum::UpdateSpectrum, EnergySpectrum.cc:12-36). */
+enum { QSG_OBSERVE_FLUENCE = 1, QSG_OBSERVE_SPECTRUM = 2 };
+/* Switch the tallies in `flags` on (others off); the ones switched on start
+ * from zero. */
+int qsg_set_observers(QsgHandle* h, int32_t flags);
+/* fluence [num_cells], spectrum [problems][G+1] (either may be NULL). */
+int qsg_read_observers(QsgHandle* h, double* fluence, uint64_t* spectrum);
+
 /* ---- sensitivities (adjoint / differential-operator tallies) ------------- */
 #define QSG_MAX_PARAMS 32
 /* K scale parameters theta_k.  Entry e says that theta[param[e]] multiplies
@@ -373,6 +389,9 @@ typedef struct QsgSimulation {
     int32_t boundary_condition; /* 0 reflect, 1 escape, 2 octant */
 } QsgSimulation;
 int qsg_deck_simulation(const QsgDeck* deck, QsgSimulation* out);
+/* The Simulation block's energySpectrum value (output file stem, "" when
+ * absent; EnergySpectrum.cc:38-59 appends ".dat"). */
+int qsg_deck_energy_spectrum(const QsgDeck* deck, char* buf, size_t len);
 
 /* Host-built problem tables (initNuclearData / initMesh restated,
  * initMC.cc:130-320, NuclearData.cc:12-187, MC_Domain.cc:77-394,

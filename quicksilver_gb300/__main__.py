@@ -1,0 +1,90 @@
+"""``python -m quicksilver_gb300 DECK [--nSteps N] [--key value ...]``
+
+Runs a Quicksilver input deck with every cycle on the GPU, the way the
+reference's driver does (main.cc:38-85): nSteps cycles of cycleInit /
+cycleTracking / cycleFinalize, one summary line per cycle with the balance
+counters, the scalar-flux total and the three phase times (the columns of
+Tallies::PrintSummary, Tallies.cc:122-144, Tallies.hh:60-76), then the
+figure of merit (segments per second of tracking), the census energy
+spectrum file when the deck names one (EnergySpectrum.cc:38-59) and the
+CORAL2 checks when the deck sets coralBenchmark (CoralBenchmark.cc:17-44).
+Simulation keys may be overridden on the command line (``--nParticles 1e5``),
+as the reference's flags do (Parameters.cc:230-255).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import sys
+import time
+
+from . import _native as N
+from .monte_carlo import MonteCarlo
+from .observe import coral_benchmark_correctness, cumulative_balance, write_energy_spectrum
+from .problem import Deck
+
+COLUMNS = ["start", "source", "rr", "split", "absorb", "scatter", "fission", "produce", "collision", "escape",
+           "census", "num_segments"]
+HEADER = ["start", "source", "rr", "split", "absorb", "scatter", "fission", "produce", "collisn", "escape",
+          "census", "num_seg"]
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(prog="python -m quicksilver_gb300", description=__doc__.split("\n\n")[1])
+    ap.add_argument("deck")
+    args, extra = ap.parse_known_args(argv)
+    deck = Deck.from_file(args.deck)
+    it = iter(extra)
+    for flag in it:
+        if not flag.startswith("--"):
+            ap.error(f"unexpected argument {flag!r}")
+        deck.set(flag[2:], next(it))
+    sim = deck.simulation
+    mc = MonteCarlo(deck)
+    spectrum_stem = deck.energy_spectrum
+    mc.observe(fluence=bool(sim.coral_benchmark), spectrum=bool(spectrum_stem))
+    out = sys.stdout
+    out.write("%-8s " % "cycle" + " ".join("%12s" % h for h in HEADER) +
+              " %14s %14s %14s %14s\n" % ("scalar_flux", "cycleInit", "cycleTracking", "cycleFinalize"))
+    track_s = 0.0
+    for cycle in range(sim.n_steps):
+        t0 = time.perf_counter()
+        mc.cycle_init()
+        h = mc.tracker
+        mc_sync(h)
+        t1 = time.perf_counter()
+        mc.cycle_tracking()
+        mc_sync(h)
+        t2 = time.perf_counter()
+        mc.cycle_finalize()
+        row = mc.history(cycle, 1)
+        t3 = time.perf_counter()
+        track_s += t2 - t1
+        bal = row.balance[0]
+        out.write("%8d " % cycle + " ".join("%12d" % int(bal[N.BAL[c]]) for c in COLUMNS) +
+                  " %14e %14e %14e %14e\n" % (row.flux_total[0], t1 - t0, t2 - t1, t3 - t2))
+    flags = mc.device_status()
+    if flags:
+        raise N.QsgError(N.QSG_ERR_DEVICE, f"device flags 0x{flags:x} raised during the run")
+    hist = mc.history(0, sim.n_steps)
+    cum = cumulative_balance(hist.balance)
+    out.write(f"\nFigure of merit: {cum['num_segments'] / track_s:.4e} segments/s "
+              f"({cum['num_segments']} segments, {track_s:.3f} s of tracking)\n")
+    if spectrum_stem:
+        path = write_energy_spectrum(spectrum_stem, mc.problem.array("energies"), mc.energy_spectrum()[0])
+        out.write(f"energy spectrum written to {path}\n")
+    if sim.coral_benchmark:
+        coral_benchmark_correctness(cum, mc.fluence(), sim.coral_benchmark, out)
+    mc.close()
+    return 0
+
+
+def mc_sync(tracker) -> None:
+    """Wait for the work enqueued so far (phase timing): qsg_sizes reads the
+    stores' device counters, which waits for the device."""
+    a, b = C.c_uint64(), C.c_uint64()
+    N.check(N.lib().qsg_sizes(tracker.handle, C.byref(a), C.byref(b)))
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -26,6 +26,8 @@ QSG_ERR_DEVICE = 4
 QSG_ERR_UNSUPPORTED = 5
 QSG_ERR_IO = 6
 QSG_ERR_NO_DEVICE = 7
+QSG_OBSERVE_FLUENCE = 1
+QSG_OBSERVE_SPECTRUM = 2
 
 BALANCE_FIELDS = ("absorb", "census", "escape", "collision", "end", "fission", "produce",
                   "scatter", "start", "source", "rr", "split", "num_segments")
@@ -149,6 +151,9 @@ _SIGNATURES = {
     "qsg_deck_set": ([_VP, C.c_char_p, C.c_char_p], C.c_int),
     "qsg_deck_free": ([_VP], C.c_int),
     "qsg_deck_simulation": ([_VP, C.POINTER(QsgSimulation)], C.c_int),
+    "qsg_deck_energy_spectrum": ([_VP, C.c_char_p, C.c_size_t], C.c_int),
+    "qsg_set_observers": ([_VP, C.c_int32], C.c_int),
+    "qsg_read_observers": ([_VP, _dp, _up], C.c_int),
     "qsg_deck_build": ([_VP, C.POINTER(_VP)], C.c_int),
     "qsg_host_problem_view": ([_VP, C.POINTER(QsgProblem)], C.c_int),
     "qsg_host_problem_source_rates": ([_VP, _dp, C.c_int32], C.c_int),

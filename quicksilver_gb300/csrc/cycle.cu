@@ -354,6 +354,38 @@ __global__ void __launch_bounds__(256) flux_partial_kernel(const double* flux, c
     if (threadIdx.x == 0) partial[(int64_t)prob * gridDim.x + blockIdx.x] = s[0];
 }
 
+// Fluence::compute (Tallies.cc:100-118) after the replica sum of
+// Tallies.cc:84-89: each cell's scalar flux summed over replicas in replica
+// order, then added group by group, in group order, to the cell's fluence.
+__global__ void fluence_kernel(const double* flux, int64_t cells, int groups, int replicas, int64_t replica_stride,
+                               double* fluence)
+{
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < cells; c += (int64_t)gridDim.x * blockDim.x) {
+        const double* row = flux + c * groups;
+        double f = fluence[c];
+        for (int g = 0; g < groups; g++) {
+            double v = row[g];
+            for (int r = 1; r < replicas; r++) v += row[r * replica_stride + g];
+            f += v;
+        }
+        fluence[c] = f;
+    }
+}
+
+// EnergySpectrum::UpdateSpectrum (EnergySpectrum.cc:12-36): the energy group
+// (NuclearData::getEnergyGroup, as MC_Load_Particle computes it) of every
+// particle of a store, counted per problem into [problems][G+1].
+__global__ void spectrum_kernel(DevTables t, DevStore s, const int32_t* cell_problem, unsigned long long* spectrum)
+{
+    const uint64_t n = min((uint64_t)*s.count, s.capacity);
+    const int width = t.num_groups + 1;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const int g = energy_group(t, s.kinetic_energy[i]);
+        const int prob = cell_problem ? cell_problem[s.cell[i]] : 0;
+        atomicAdd(spectrum + (int64_t)prob * width + g, 1ull);
+    }
+}
+
 // Block p records problem p's cycle: counters summed over replicas, END = its
 // census count (main.cc:314), the flux total; carries the census count into
 // the next cycle and clears the counters.
@@ -461,6 +493,17 @@ int cycle_finalize_enqueue(QsgHandle* h, cudaStream_t s)
 {
     CycleArgs ca = cycle_args(h);
     const int64_t stride = (int64_t)h->num_cells * h->num_groups;
+    if (h->observe_flags & QSG_OBSERVE_FLUENCE) {
+        fluence_kernel<<<h->num_sms * 4, 128, 0, s>>>(h->flux.ptr, h->num_cells, h->num_groups, h->flux_replicas,
+                                                      stride, h->fluence.ptr);
+        QSG_CUDA(cudaGetLastError());
+    }
+    if (h->observe_flags & QSG_OBSERVE_SPECTRUM) {
+        const int32_t* cp = h->num_problems > 1 ? h->cell_problem.ptr : nullptr;
+        spectrum_kernel<<<h->num_sms * 4, 256, 0, s>>>(h->tables, h->processed.view, cp, h->spectrum.ptr);
+        spectrum_kernel<<<h->num_sms, 256, 0, s>>>(h->tables, h->processing.view, cp, h->spectrum.ptr);
+        QSG_CUDA(cudaGetLastError());
+    }
     flux_partial_kernel<<<dim3(kFluxPartials, h->num_problems), 256, 0, s>>>(
         h->flux.ptr, h->prob_cell_offset.ptr, h->num_groups, h->flux_replicas, stride, h->flux_partial.ptr);
     QSG_CUDA(cudaGetLastError());
@@ -478,6 +521,48 @@ int cycle_finalize_enqueue(QsgHandle* h, cudaStream_t s)
 }  // namespace qsg
 
 using namespace qsg;
+
+extern "C" int qsg_set_observers(QsgHandle* h, int32_t flags)
+{
+    QSG_API_BEGIN
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_set_observers: null handle");
+    if (flags & ~(QSG_OBSERVE_FLUENCE | QSG_OBSERVE_SPECTRUM))
+        return fail(QSG_ERR_INVALID, "qsg_set_observers: unknown flag bits 0x%x", (unsigned)flags);
+    int st = set_device(h);
+    if (st) return st;
+    QSG_CUDA(cudaDeviceSynchronize());
+    if (flags & QSG_OBSERVE_FLUENCE) {
+        if ((st = h->fluence.alloc((size_t)h->num_cells))) return st;
+        QSG_CUDA(cudaMemset(h->fluence.ptr, 0, h->fluence.n * sizeof(double)));
+    }
+    if (flags & QSG_OBSERVE_SPECTRUM) {
+        if ((st = h->spectrum.alloc((size_t)h->num_problems * (h->num_groups + 1)))) return st;
+        QSG_CUDA(cudaMemset(h->spectrum.ptr, 0, h->spectrum.n * sizeof(unsigned long long)));
+    }
+    h->observe_flags = flags;
+    h->clear_graphs();   // captured cycles carry the old finalize sequence
+    return QSG_OK;
+    QSG_API_END
+}
+
+extern "C" int qsg_read_observers(QsgHandle* h, double* fluence, uint64_t* spectrum)
+{
+    QSG_API_BEGIN
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_read_observers: null handle");
+    int st = set_device(h);
+    if (st) return st;
+    QSG_CUDA(cudaDeviceSynchronize());
+    if (fluence) {
+        if (!(h->observe_flags & QSG_OBSERVE_FLUENCE)) return fail(QSG_ERR_INVALID, "qsg_read_observers: fluence is off");
+        QSG_CUDA(cudaMemcpy(fluence, h->fluence.ptr, h->fluence.n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    if (spectrum) {
+        if (!(h->observe_flags & QSG_OBSERVE_SPECTRUM)) return fail(QSG_ERR_INVALID, "qsg_read_observers: spectrum is off");
+        QSG_CUDA(cudaMemcpy(spectrum, h->spectrum.ptr, h->spectrum.n * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    }
+    return QSG_OK;
+    QSG_API_END
+}
 
 extern "C" int qsg_configure_cycle_batch(QsgHandle* h, const QsgCycleConfig* cfgs, const uint64_t* seed_offsets)
 {

@@ -255,6 +255,10 @@ struct QsgHandle {
     std::vector<uint8_t> h_class_const;           // [classes][max_reactions] 1: the 1e-20 placeholder entry
     std::vector<double> h_class_macro;            // [classes][G][max_reactions]
     int32_t num_classes = 0, max_reactions = 0;
+    // observability tallies (qsg_set_observers)
+    int observe_flags = 0;
+    qsg::DevBuf<double> fluence;                  // [C]
+    qsg::DevBuf<unsigned long long> spectrum;     // [problems][G+1]
     // sensitivities (qsg_enable_sensitivity); sens.K == 0: off
     qsg::DevSens sens{};
     int sens_track_blocks = 0;

@@ -10,6 +10,7 @@
 #include "deck.h"
 
 #include <cctype>
+#include <cstring>
 #include <fstream>
 #include <sstream>
 #include <stdexcept>
@@ -138,6 +139,7 @@ void scan_simulation(const Block& b, SimulationSpec& s)
     b.get("fTally", s.flux_replications);
     b.get("cTally", s.cell_replications);
     b.get("coralBenchmark", s.coral_benchmark);
+    b.get("energySpectrum", s.energy_spectrum);
 }
 
 void scan_geometry(const Block& b, Deck& d)
@@ -249,7 +251,8 @@ void set_simulation_key(Deck& deck, const std::string& key, const std::string& v
     static const char* known[] = {"boundaryCondition", "dt", "fMax", "loadBalance", "lx", "ly", "lz",
                                   "nParticles", "batchSize", "nBatches", "nSteps", "nx", "ny", "nz",
                                   "seed", "xDom", "yDom", "zDom", "eMax", "eMin", "nGroups",
-                                  "lowWeightCutoff", "bTally", "fTally", "cTally", "coralBenchmark"};
+                                  "lowWeightCutoff", "bTally", "fTally", "cTally", "coralBenchmark",
+                                  "energySpectrum"};
     bool ok = false;
     for (const char* k : known) ok = ok || key == k;
     if (!ok) throw std::runtime_error("deck: unknown Simulation key '" + key + "'");
@@ -317,6 +320,17 @@ extern "C" int qsg_deck_free(QsgDeck* deck)
 {
     delete deck;
     return QSG_OK;
+}
+
+extern "C" int qsg_deck_energy_spectrum(const QsgDeck* deck, char* buf, size_t len)
+{
+    QSG_API_BEGIN
+    if (!deck || !buf || len == 0) return qsg::fail(QSG_ERR_INVALID, "qsg_deck_energy_spectrum: null argument");
+    const std::string& name = deck->deck.sim.energy_spectrum;
+    if (name.size() + 1 > len) return qsg::fail(QSG_ERR_CAPACITY, "qsg_deck_energy_spectrum: buffer too small");
+    std::memcpy(buf, name.c_str(), name.size() + 1);
+    return QSG_OK;
+    QSG_API_END
 }
 
 extern "C" int qsg_deck_simulation(const QsgDeck* deck, QsgSimulation* out)

@@ -38,6 +38,7 @@ struct CrossSectionSpec {      // CrossSectionParameters, Parameters.hh:76-95
 
 struct SimulationSpec {        // SimulationParameters, Parameters.hh:97-167
     std::string boundary_condition = "reflect";
+    std::string energy_spectrum;   // output file stem of the census energy spectrum ("" = none)
     int load_balance = 0;
     uint64_t n_particles = 1000000;
     uint64_t batch_size = 0;

@@ -1749,6 +1749,7 @@ extern "C" int qsg_destroy(QsgHandle* h)
     h->prob_load_balance.free(); h->prob_cell_offset.free(); h->prob_carry.free();
     h->sens_param.free(); h->sens_dsig.free(); h->sens_inv_theta.free(); h->sens_flux_cell.free();
     h->sens_dflux.free(); h->sens_leak.free(); h->sens_dleak.free();
+    h->fluence.free(); h->spectrum.free();
     h->clear_graphs();
     if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
     h->processing.release(); h->processed.release(); h->extra.release();

@@ -186,6 +186,13 @@ def test_decks() -> dict:
     d["t_sens.inp"] = (small(boundaryCondition="escape", nx=6, ny=6, nz=6, lx=6, ly=6, lz=6, nGroups=40) +
                        brick("matA", 0, 6, 0, 6, 0, 6) + sphere("matB", "2.4", 3, 3, 3) +
                        sphere("matC", "1.2", 3, 3, 3) + drawn_materials(rng, ["matA", "matB", "matC"]))
+    # CORAL2-style problem 1 setup (the proportions CoralBenchmark.cc:60-65
+    # expects: absorption 0.04, fission 0.05, scatter 1) with its checks on
+    d["t_coral1.inp"] = (small(nx=6, ny=6, nz=6, lx=6, ly=6, lz=6, dt="2e-09", nParticles=8000, nSteps=5,
+                               coralBenchmark=1) +
+                         brick("src", 0, 6, 0, 6, 0, 6) +
+                         material("src", total="1.5", scatter=1, absorb="0.04", fission="0.05", n_iso=4,
+                                  n_react=9, mass="12.011") + cross_section("flat"))
     # no Geometry block: supplyDefaults problem (Parameters.cc:350-379)
     d["t_default.inp"] = small(nParticles=3000, nSteps=2, lx=10, ly=10, lz=10)
     return d

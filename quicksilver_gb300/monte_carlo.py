@@ -99,6 +99,25 @@ class _Driver:
     def device_status(self, clear: bool = True) -> int:
         return self.tracker.device_status(clear)
 
+    # ---- observability (quicksilver_gb300.observe) ----
+    def observe(self, fluence: bool = False, spectrum: bool = False) -> None:
+        """Keep the per-cell fluence and / or the census energy spectrum on
+        the device from the next finalised cycle on (both start at zero)."""
+        flags = (N.QSG_OBSERVE_FLUENCE if fluence else 0) | (N.QSG_OBSERVE_SPECTRUM if spectrum else 0)
+        N.check(N.lib().qsg_set_observers(self.tracker.handle, flags))
+        self._observe_flags = flags
+
+    def fluence(self) -> np.ndarray:
+        out = np.zeros(self.tracker.num_cells, dtype=np.float64)
+        N.check(N.lib().qsg_read_observers(self.tracker.handle, out.ctypes.data_as(C.POINTER(C.c_double)), None))
+        return out
+
+    def energy_spectrum(self) -> np.ndarray:
+        """[problems, G+1] census energy-group counts (summed over cycles)."""
+        out = np.zeros((len(self.tracker.problems), self.tracker.num_groups + 1), dtype=np.uint64)
+        N.check(N.lib().qsg_read_observers(self.tracker.handle, None, out.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return out
+
     def run_cycles(self, n_cycles: int, use_graph: bool = False, stream=None) -> None:
         """n whole cycles enqueued without host synchronisation: each cycle is
         init + QsgOptions.max_passes tracking passes + finalize, replayed from a

@@ -1,0 +1,122 @@
+"""Observability outputs of a run: cumulative balance, fluence, census energy
+spectrum and the CORAL2 correctness checks.
+
+* ``cumulative_balance`` -- Tallies::_balanceCumulative (Tallies.cc:65), the
+  sum of every finished cycle's 13 counters;
+* fluence -- Fluence::compute (Tallies.cc:100-118), kept on the device by
+  qsg_set_observers(QSG_OBSERVE_FLUENCE);
+* energy spectrum -- EnergySpectrum::UpdateSpectrum / PrintSpectrum
+  (EnergySpectrum.cc:12-59), kept on the device by
+  qsg_set_observers(QSG_OBSERVE_SPECTRUM), written as ``<stem>.dat`` with one
+  ``index<TAB>lower edge<TAB>count`` line per group edge;
+* ``coral_benchmark_correctness`` -- the four checks of CoralBenchmark.cc:17-228
+  with the reference's tolerances and messages.
+"""
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+
+from . import _native as N
+
+B = N.BAL
+
+# CoralBenchmark.cc:60-79: expected absorption / fission / scatter proportions
+# of the two CORAL2 problems and the tolerance (percent) on their ratios
+CORAL_RATIOS = {1: (0.04, 0.05, 1.0, 1.0), 2: (0.094, 0.075, 0.830, 1.1)}
+
+
+def cumulative_balance(history_balance: np.ndarray) -> dict:
+    """Sum of per-cycle counters ([cycles, 13]) as a name -> int dict."""
+    tot = np.asarray(history_balance, dtype=np.uint64).reshape(-1, 13).sum(axis=0, dtype=np.uint64)
+    return {name: int(tot[i]) for name, i in B.items()}
+
+
+def balance_ratio_test(bal: dict, coral_benchmark: int):
+    """BalanceRatioTest (CoralBenchmark.cc:46-118)."""
+    if coral_benchmark not in CORAL_RATIOS:
+        raise ValueError(f"coralBenchmark must be 1 or 2, not {coral_benchmark}")
+    absorb_r, fission_r, scatter_r, pct = CORAL_RATIOS[coral_benchmark]
+    tol = pct / 100.0
+    a, f, s = float(bal["absorb"]), float(bal["fission"]), float(bal["scatter"])
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rel = {
+            "Absorb to Scatter": abs((a / absorb_r) * (scatter_r / s) - 1) if s else np.inf,
+            "Absorb to Fission": abs((a / absorb_r) * (fission_r / f) - 1) if f else np.inf,
+            "Scatter to Absorb": abs((s / scatter_r) * (absorb_r / a) - 1) if a else np.inf,
+            "Scatter to Fission": abs((s / scatter_r) * (fission_r / f) - 1) if f else np.inf,
+            "Fission to Absorb": abs((f / fission_r) * (absorb_r / a) - 1) if a else np.inf,
+            "Fission to Scatter": abs((f / fission_r) * (scatter_r / s) - 1) if s else np.inf,
+        }
+    ok = all(v <= tol for v in rel.values())
+    msg = (f"PASS:: Absorption / Fission / Scatter Ratios maintained with {tol * 100:g}% tolerance" if ok else
+           f"FAIL:: Absorption / Fission / Scatter Ratios NOT maintained with {tol * 100:g}% tolerance\n" +
+           "\n".join(f"Relative {k}:  {v:g} < {tol:g}" for k, v in rel.items()))
+    return ok, msg, rel
+
+
+def balance_event_test(bal: dict):
+    """BalanceEventTest (CoralBenchmark.cc:120-152): facet crossings
+    (segments - census - collisions) within 1% of the collisions."""
+    facet = bal["num_segments"] - bal["census"] - bal["collision"]
+    ratio = abs(facet / bal["collision"] - 1) if bal["collision"] else np.inf
+    ok = ratio <= 0.01
+    msg = ("PASS:: Collision to Facet Crossing Ratio maintained even balanced within 1% tolerance" if ok else
+           f" FAIL:: Collision to Facet Crossing Ratio balanced NOT maintained within 1% tolerance\n"
+           f"\tFacet Crossing: {facet}\tCollision: {bal['collision']}\tRatio: {ratio:g}")
+    return ok, msg, ratio
+
+
+def missing_particle_test(bal: dict):
+    """MissingParticleTest (CoralBenchmark.cc:154-175): start + source +
+    produce + split == absorb + census + escape + rr + fission."""
+    gains = bal["start"] + bal["source"] + bal["produce"] + bal["split"]
+    losses = bal["absorb"] + bal["census"] + bal["escape"] + bal["rr"] + bal["fission"]
+    ok = gains == losses
+    msg = ("PASS:: No Particles Lost During Run" if ok else
+           "FAIL:: Particles Were Lost During Run, test for done should have failed")
+    return ok, msg, (gains, losses)
+
+
+def fluence_test(fluence: np.ndarray):
+    """FluenceTest (CoralBenchmark.cc:177-228): max over cells of
+    |cell - mean| / ((cell + mean) / 2) in percent, within 6%."""
+    f = np.asarray(fluence, dtype=np.float64)
+    avg = f.sum() / len(f)
+    diff = np.where(f > avg, f - avg, avg - f) / ((f + avg) / 2.0) * 100.0
+    max_diff = float(diff.max()) if len(f) else 0.0
+    ok = not (max_diff > 6.0)
+    msg = ("PASS:: Fluence is homogenous across cells with 6% tolerance" if ok else
+           "FAIL:: Fluence not homogenous across cells within 6% tolerance\n"
+           "\tTry running more particles or more cycles to see if Max Percent Difference goes down.\n"
+           f"\tCurrent Max Percent Diff: {max_diff:4.1f}%")
+    return ok, msg, max_diff
+
+
+def coral_benchmark_correctness(bal: dict, fluence: np.ndarray, coral_benchmark: int, out=sys.stdout) -> dict:
+    """coralBenchmarkCorrectness (CoralBenchmark.cc:17-44): prints the four
+    checks and returns {name: passed}."""
+    results = {}
+    for name, header, (ok, msg, _) in (
+            ("balance_ratio", "Testing Ratios for Absorbtion, Fission, and Scattering are maintained",
+             balance_ratio_test(bal, coral_benchmark)),
+            ("balance_event", "Testing balance between number of facet crossings and reactions",
+             balance_event_test(bal)),
+            ("missing_particle", "Test for lost / unaccounted for particles in this simulation",
+             missing_particle_test(bal)),
+            ("fluence", "Test Fluence for homogeneity across cells", fluence_test(fluence))):
+        if out is not None:
+            out.write(f"\n{header}\n{msg}\n")
+        results[name] = ok
+    return results
+
+
+def write_energy_spectrum(stem: str, energies: np.ndarray, counts: np.ndarray) -> str:
+    """PrintSpectrum (EnergySpectrum.cc:38-59): ``stem + ".dat"`` with
+    ``index<TAB>energy edge<TAB>count`` for each of the G+1 entries."""
+    path = stem + ".dat"
+    with open(path, "w") as fh:
+        for i, (e, c) in enumerate(zip(energies, counts)):
+            fh.write(f"{i}\t{float(e):g}\t{int(c)}\n")
+    return path

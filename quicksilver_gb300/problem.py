@@ -50,6 +50,13 @@ class Deck:
         N.check(N.lib().qsg_deck_simulation(self._h, C.byref(s)))
         return s
 
+    @property
+    def energy_spectrum(self) -> str:
+        """The Simulation block's energySpectrum file stem ("" when absent)."""
+        buf = C.create_string_buffer(4096)
+        N.check(N.lib().qsg_deck_energy_spectrum(self._h, buf, len(buf)))
+        return buf.value.decode()
+
     def build(self) -> "HostProblem":
         h = C.c_void_p()
         N.check(N.lib().qsg_deck_build(self._h, C.byref(h)))
