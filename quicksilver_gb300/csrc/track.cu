@@ -841,36 +841,54 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
 // run with the lanes whose particle happens to need that step (on config2
 // about 21 of 32 lanes in segment steps and 18 in collision steps), and an
 // FP64 warp instruction costs the FP64 pipe the same whatever its active
-// lanes.  Here each warp owns a pool of kPool particles in shared memory;
+// lanes.  Here each warp owns a pool of POOL particles in shared memory;
 // every step picks one kind of work -- a segment for particles ready to move,
 // or the collision (reaction selection + trajectory update) for particles
 // parked at a collision -- and hands up to 32 such particles to the lanes, so
 // steps run full while the pool holds enough of one kind.  Every particle
 // still follows its own history with its own random stream, in the
 // reference's order, so the results are those of the lane-resident kernel.
-// Particles per warp (one bit each in a 64-bit mask): 64 for the plain
-// kernel; 48 with sensitivity scores, whose shared memory would otherwise
-// leave room for only 2 blocks per SM.
+//
+// Pool sizes: 96 particles per warp for the plain kernel; with K sensitivity
+// scores per particle, 64, 48 or 32, the largest that still leaves room for
+// three 4-warp blocks per SM (pool_for_scores).
 #ifndef QSG_POOL
 #define QSG_POOL 64
 #endif
-#ifndef QSG_POOL_SENS
-#define QSG_POOL_SENS 48
+#ifndef QSG_POOL_SENS_MAX
+#define QSG_POOL_SENS_MAX 64
 #endif
-constexpr int kPoolPlain = QSG_POOL, kPoolSens = QSG_POOL_SENS;
-static_assert(kPoolPlain >= 32 && kPoolPlain <= 64 && kPoolSens >= 32 && kPoolSens <= 64, "pool size");
-constexpr int kPoolD = 20, kPoolU = 2, kPoolI = 12;
-__host__ __device__ constexpr size_t pool_bytes_per_warp(int pool) { return (size_t)(kPoolD * 8 + kPoolU * 8 + kPoolI * 4) * pool; }
-__host__ __device__ constexpr uint64_t pool_mask(int pool) { return pool == 64 ? ~0ull : ((1ull << pool) - 1ull); }
+constexpr int kPoolPlain = QSG_POOL;
+constexpr int kPoolD = 18, kPoolU = 2, kPoolI = 9;
+constexpr int kSlotBytes = kPoolD * 8 + kPoolU * 8 + kPoolI * 4;   // 196
+__host__ __device__ constexpr size_t pool_bytes_per_warp(int pool) { return (size_t)kSlotBytes * pool; }
 enum { PD_X, PD_Y, PD_Z, PD_VX, PD_VY, PD_VZ, PD_A, PD_B, PD_G, PD_E, PD_W, PD_TTC, PD_AGE, PD_NMFP, PD_NSEG,
-       PD_SPEED, PD_SIG, PD_MFP, PD_PE, PD_PA };
-enum { PI_LAST, PI_NCOLL, PI_BREED, PI_SPECIES, PI_DOMAIN, PI_CELL, PI_FACET, PI_GROUP, PI_KEY, PI_PROB, PI_REP,
-       PI_SEGS };
+       PD_SPEED, PD_SIG, PD_MFP };
+// PI_PACK = facet | flux replica << 8 | group << 16
+enum { PI_LAST, PI_NCOLL, PI_BREED, PI_SPECIES, PI_DOMAIN, PI_CELL, PI_PACK, PI_KEY, PI_SEGS };
+
+// Shared memory a block of the pool kernel needs (counters, pools, scores).
+size_t track_pool_smem_bytes(int block, int num_problems, int K, int pool)
+{
+    const size_t counts = num_problems <= kSmemProblems ? (size_t)num_problems * LC_N * 8 : 0;
+    const int warps = block / 32;
+    return counts + (size_t)warps * pool_bytes_per_warp(pool) + (size_t)warps * K * pool * sizeof(double);
+}
+
+// Pool size of the sensitivity kernel for K scores: the largest of 64, 48, 32
+// whose 4-warp block fits three times into an SM's 228 KB of shared memory.
+int pool_for_scores(int K, int num_problems)
+{
+    for (int pool : {64, 48, 32})
+        if (pool <= QSG_POOL_SENS_MAX && 3 * (track_pool_smem_bytes(128, num_problems, K, pool) + 1024) <= 228 * 1024)
+            return pool;
+    return 32;
+}
 
 struct PoolView {
-    double* d;      // [kPoolD][kPool]
-    uint64_t* u;    // [2][kPool]: seed, identifier
-    int32_t* i;     // [kPoolI][kPool]
+    double* d;      // [kPoolD][POOL]
+    uint64_t* u;    // [2][POOL]: seed, identifier
+    int32_t* i;     // [kPoolI][POOL]
 };
 
 // Extra per-slot state the pool keeps beside the particle record.
@@ -879,44 +897,48 @@ struct SlotState {
     uint32_t segs;
 };
 
-template <int kPool>
-__device__ __forceinline__ void pool_get(const PoolView& v, int s, Particle& p, SlotState& st)
+template <int POOL>
+__device__ __forceinline__ void pool_get(const PoolView& v, int s, const DevTally& tally, Particle& p, SlotState& st)
 {
     const double* d = v.d + s;
-    p.x = d[PD_X * kPool]; p.y = d[PD_Y * kPool]; p.z = d[PD_Z * kPool];
-    p.vx = d[PD_VX * kPool]; p.vy = d[PD_VY * kPool]; p.vz = d[PD_VZ * kPool];
-    p.alpha = d[PD_A * kPool]; p.beta = d[PD_B * kPool]; p.gamma = d[PD_G * kPool];
-    p.kinetic_energy = d[PD_E * kPool]; p.weight = d[PD_W * kPool];
-    p.time_to_census = d[PD_TTC * kPool]; p.age = d[PD_AGE * kPool];
-    p.num_mean_free_paths = d[PD_NMFP * kPool]; p.num_segments = d[PD_NSEG * kPool];
-    p.speed = d[PD_SPEED * kPool]; p.total_xs = d[PD_SIG * kPool]; p.mean_free_path = d[PD_MFP * kPool];
-    p.pend_e = d[PD_PE * kPool]; p.pend_a = d[PD_PA * kPool];
-    p.seed = v.u[s]; p.identifier = v.u[kPool + s];
+    p.x = d[PD_X * POOL]; p.y = d[PD_Y * POOL]; p.z = d[PD_Z * POOL];
+    p.vx = d[PD_VX * POOL]; p.vy = d[PD_VY * POOL]; p.vz = d[PD_VZ * POOL];
+    p.alpha = d[PD_A * POOL]; p.beta = d[PD_B * POOL]; p.gamma = d[PD_G * POOL];
+    p.kinetic_energy = d[PD_E * POOL]; p.weight = d[PD_W * POOL];
+    p.time_to_census = d[PD_TTC * POOL]; p.age = d[PD_AGE * POOL];
+    p.num_mean_free_paths = d[PD_NMFP * POOL]; p.num_segments = d[PD_NSEG * POOL];
+    p.speed = d[PD_SPEED * POOL]; p.total_xs = d[PD_SIG * POOL]; p.mean_free_path = d[PD_MFP * POOL];
+    p.seed = v.u[s]; p.identifier = v.u[POOL + s];
     const int32_t* i = v.i + s;
-    p.last_event = i[PI_LAST * kPool]; p.num_collisions = i[PI_NCOLL * kPool]; p.breed = i[PI_BREED * kPool];
-    p.species = i[PI_SPECIES * kPool]; p.domain = i[PI_DOMAIN * kPool]; p.cell = i[PI_CELL * kPool];
-    p.facet = i[PI_FACET * kPool]; p.group = i[PI_GROUP * kPool]; p.xs_key = i[PI_KEY * kPool];
-    st.prob = i[PI_PROB * kPool]; st.rep = i[PI_REP * kPool]; st.segs = (uint32_t)i[PI_SEGS * kPool];
+    p.last_event = i[PI_LAST * POOL]; p.num_collisions = i[PI_NCOLL * POOL]; p.breed = i[PI_BREED * POOL];
+    p.species = i[PI_SPECIES * POOL]; p.domain = i[PI_DOMAIN * POOL]; p.cell = i[PI_CELL * POOL];
+    const uint32_t pack = (uint32_t)i[PI_PACK * POOL];
+    p.facet = (int)(pack & 0xffu);
+    st.rep = (int)((pack >> 8) & 0xffu);
+    p.group = (int)(pack >> 16);
+    p.xs_key = i[PI_KEY * POOL];
+    st.segs = (uint32_t)i[PI_SEGS * POOL];
+    st.prob = tally.cell_problem ? __ldg(tally.cell_problem + p.cell) : 0;
 }
 
-template <int kPool>
+template <int POOL>
 __device__ __forceinline__ void pool_put(const PoolView& v, int s, const Particle& p, const SlotState& st)
 {
     double* d = v.d + s;
-    d[PD_X * kPool] = p.x; d[PD_Y * kPool] = p.y; d[PD_Z * kPool] = p.z;
-    d[PD_VX * kPool] = p.vx; d[PD_VY * kPool] = p.vy; d[PD_VZ * kPool] = p.vz;
-    d[PD_A * kPool] = p.alpha; d[PD_B * kPool] = p.beta; d[PD_G * kPool] = p.gamma;
-    d[PD_E * kPool] = p.kinetic_energy; d[PD_W * kPool] = p.weight;
-    d[PD_TTC * kPool] = p.time_to_census; d[PD_AGE * kPool] = p.age;
-    d[PD_NMFP * kPool] = p.num_mean_free_paths; d[PD_NSEG * kPool] = p.num_segments;
-    d[PD_SPEED * kPool] = p.speed; d[PD_SIG * kPool] = p.total_xs; d[PD_MFP * kPool] = p.mean_free_path;
-    d[PD_PE * kPool] = p.pend_e; d[PD_PA * kPool] = p.pend_a;
-    v.u[s] = p.seed; v.u[kPool + s] = p.identifier;
+    d[PD_X * POOL] = p.x; d[PD_Y * POOL] = p.y; d[PD_Z * POOL] = p.z;
+    d[PD_VX * POOL] = p.vx; d[PD_VY * POOL] = p.vy; d[PD_VZ * POOL] = p.vz;
+    d[PD_A * POOL] = p.alpha; d[PD_B * POOL] = p.beta; d[PD_G * POOL] = p.gamma;
+    d[PD_E * POOL] = p.kinetic_energy; d[PD_W * POOL] = p.weight;
+    d[PD_TTC * POOL] = p.time_to_census; d[PD_AGE * POOL] = p.age;
+    d[PD_NMFP * POOL] = p.num_mean_free_paths; d[PD_NSEG * POOL] = p.num_segments;
+    d[PD_SPEED * POOL] = p.speed; d[PD_SIG * POOL] = p.total_xs; d[PD_MFP * POOL] = p.mean_free_path;
+    v.u[s] = p.seed; v.u[POOL + s] = p.identifier;
     int32_t* i = v.i + s;
-    i[PI_LAST * kPool] = p.last_event; i[PI_NCOLL * kPool] = p.num_collisions; i[PI_BREED * kPool] = p.breed;
-    i[PI_SPECIES * kPool] = p.species; i[PI_DOMAIN * kPool] = p.domain; i[PI_CELL * kPool] = p.cell;
-    i[PI_FACET * kPool] = p.facet; i[PI_GROUP * kPool] = p.group; i[PI_KEY * kPool] = p.xs_key;
-    i[PI_PROB * kPool] = st.prob; i[PI_REP * kPool] = st.rep; i[PI_SEGS * kPool] = (int32_t)st.segs;
+    i[PI_LAST * POOL] = p.last_event; i[PI_NCOLL * POOL] = p.num_collisions; i[PI_BREED * POOL] = p.breed;
+    i[PI_SPECIES * POOL] = p.species; i[PI_DOMAIN * POOL] = p.domain; i[PI_CELL * POOL] = p.cell;
+    i[PI_PACK * POOL] = (int32_t)((uint32_t)p.facet | ((uint32_t)st.rep << 8) | ((uint32_t)p.group << 16));
+    i[PI_KEY * POOL] = p.xs_key;
+    i[PI_SEGS * POOL] = (int32_t)st.segs;
 }
 
 // Position of the n-th (0-based) set bit of m; n < popcount(m).
@@ -946,30 +968,51 @@ __device__ __forceinline__ int nth_set_bit(uint64_t m, int n)
     return base;
 }
 
-// 64-bit OR of one bit per lane (bit < 0: none) over the warp.
-__device__ __forceinline__ uint64_t warp_bits(int bit)
+// Warp-uniform set of pool slots (up to 128): bits 0..63 in lo, 64..127 in hi.
+struct SlotMask {
+    uint64_t lo, hi;
+    __device__ __forceinline__ int count() const { return __popcll(lo) + __popcll(hi); }
+    __device__ __forceinline__ int nth(int n) const
+    {
+        const int c = __popcll(lo);
+        return n < c ? nth_set_bit(lo, n) : 64 + nth_set_bit(hi, n - c);
+    }
+    __device__ __forceinline__ SlotMask operator|(const SlotMask& o) const { return {lo | o.lo, hi | o.hi}; }
+    __device__ __forceinline__ SlotMask operator&(const SlotMask& o) const { return {lo & o.lo, hi & o.hi}; }
+    __device__ __forceinline__ SlotMask operator~() const { return {~lo, ~hi}; }
+};
+
+template <int POOL>
+__device__ __forceinline__ SlotMask all_slots()
 {
-    const uint32_t lo = __reduce_or_sync(0xffffffffu, (bit >= 0 && bit < 32) ? (1u << bit) : 0u);
-    const uint32_t hi = __reduce_or_sync(0xffffffffu, (bit >= 32) ? (1u << (bit - 32)) : 0u);
-    return ((uint64_t)hi << 32) | lo;
+    return {POOL >= 64 ? ~0ull : ((1ull << POOL) - 1ull), POOL <= 64 ? 0ull : (POOL >= 128 ? ~0ull : ((1ull << (POOL - 64)) - 1ull))};
 }
 
-size_t track_pool_smem_bytes_per_block(int block, int num_problems, int K)
+// OR over the warp of one slot bit per lane (slot < 0: none).
+template <int POOL>
+__device__ __forceinline__ SlotMask warp_slots(int slot)
 {
-    const size_t counts = num_problems <= kSmemProblems ? (size_t)num_problems * LC_N * 8 : 0;
-    const int warps = block / 32;
-    const int pool = K > 0 ? kPoolSens : kPoolPlain;
-    return counts + (size_t)warps * pool_bytes_per_warp(pool) + (size_t)warps * K * pool * sizeof(double);
+    SlotMask m;
+    const uint32_t b0 = __reduce_or_sync(0xffffffffu, (slot >= 0 && slot < 32) ? (1u << slot) : 0u);
+    const uint32_t b1 = __reduce_or_sync(0xffffffffu, (slot >= 32 && slot < 64) ? (1u << (slot - 32)) : 0u);
+    m.lo = ((uint64_t)b1 << 32) | b0;
+    m.hi = 0;
+    if (POOL > 64) {
+        const uint32_t b2 = __reduce_or_sync(0xffffffffu, (slot >= 64 && slot < 96) ? (1u << (slot - 64)) : 0u);
+        uint32_t b3 = 0;
+        if (POOL > 96) b3 = __reduce_or_sync(0xffffffffu, (slot >= 96) ? (1u << (slot - 96)) : 0u);
+        m.hi = ((uint64_t)b3 << 32) | b2;
+    }
+    return m;
 }
 
-template <int BLOCK, bool SENS>
+template <int BLOCK, bool SENS, int POOL>
 __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / BLOCK)
     track_pool_kernel(DevTables t, DevTally tally, DevStore in, DevStore census, DevStore extra,
                       unsigned long long* cursor, DevSens sens)
 {
-    constexpr int kPool = SENS ? kPoolSens : kPoolPlain;
-    constexpr size_t kPoolBytesPerWarp = pool_bytes_per_warp(kPool);
-    constexpr uint64_t kPoolMask = pool_mask(kPool);
+    static_assert(POOL >= 32 && POOL <= 128, "pool size");
+    constexpr size_t kPoolBytesPerWarp = pool_bytes_per_warp(POOL);
     extern __shared__ unsigned long long s_counts[];
     BlockCounters bc;
     const bool counts_in_smem = tally.num_problems <= kSmemProblems;
@@ -983,66 +1026,68 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
     char* mine = pool_base + (size_t)warp * kPoolBytesPerWarp;
     PoolView v;
     v.d = reinterpret_cast<double*>(mine);
-    v.u = reinterpret_cast<uint64_t*>(mine + (size_t)kPoolD * 8 * kPool);
-    v.i = reinterpret_cast<int32_t*>(mine + (size_t)(kPoolD + kPoolU) * 8 * kPool);
-    double* s_scores = nullptr;   // [K][kPool] of this warp
+    v.u = reinterpret_cast<uint64_t*>(mine + (size_t)kPoolD * 8 * POOL);
+    v.i = reinterpret_cast<int32_t*>(mine + (size_t)(kPoolD + kPoolU) * 8 * POOL);
+    double* s_scores = nullptr;   // [K][POOL] of this warp
     if (SENS)
         s_scores = reinterpret_cast<double*>(pool_base + (size_t)(BLOCK / 32) * kPoolBytesPerWarp) +
-                   (size_t)warp * sens.K * kPool;
+                   (size_t)warp * sens.K * POOL;
     __syncthreads();
     uint32_t cnt[LC_N];
 #pragma unroll
     for (int k = 0; k < LC_N; k++) cnt[k] = 0;
     int cur_prob = -1;
     const uint64_t n = *in.count;
-    uint64_t ready = 0, coll = 0;   // warp-uniform slot masks
+    SlotMask ready = {0, 0}, coll = {0, 0};   // warp-uniform
     bool exhausted = false;
     for (;;) {
         // refill empty slots from the work queue (warp-aggregated claim)
-        const uint64_t empty = ~(ready | coll) & kPoolMask;
-        const int n_empty = __popcll(empty);
-        if (!exhausted && n_empty > 0 &&
-            (n_empty >= 16 || (__popcll(ready) < 32 && __popcll(coll) < 32))) {
+        const SlotMask empty = ~(ready | coll) & all_slots<POOL>();
+        const int n_empty = empty.count();
+        const int nr0 = ready.count(), nc0 = coll.count();
+        if (!exhausted && n_empty > 0 && (n_empty >= 16 || (nr0 < 32 && nc0 < 32))) {
             unsigned long long base = 0;
             if (lane == 0) base = atomicAdd(cursor, (unsigned long long)n_empty);
             base = __shfl_sync(0xffffffffu, base, 0);
             if (base + (unsigned long long)n_empty >= n) exhausted = true;
-            int filled = -1, filled2 = -1;
-            for (int k = lane; k < n_empty; k += 32) {
+            int filled[(POOL + 31) / 32];
+#pragma unroll
+            for (int r = 0; r < (POOL + 31) / 32; r++) {
+                filled[r] = -1;
+                const int k = lane + 32 * r;
                 const uint64_t i = base + (uint64_t)k;
-                if (i >= n) break;
-                const int slot = nth_set_bit(empty, k);
-                Particle p;
-                load_particle(t, in, i, p);
-                if (!(p.speed > 0.0)) raise_flag(tally, QSG_DEV_BAD_FACET);
-                SlotState st;
-                st.prob = tally.cell_problem ? __ldg(tally.cell_problem + p.cell) : 0;
-                // CycleTracking.cc:37-39 replica selection by particle index
-                st.rep = (int)(i % (uint64_t)tally.flux_replicas);
-                st.segs = 0;
-                p.pend_e = 0.0;
-                p.pend_a = 0.0;
-                pool_put<kPool>(v, slot, p, st);
-                if (SENS) load_scores(in, i, s_scores + slot, kPool, sens.K);
-                if (k < 32) filled = slot;
-                else filled2 = slot;
+                if (k < n_empty && i < n) {
+                    const int slot = empty.nth(k);
+                    Particle p;
+                    load_particle(t, in, i, p);
+                    if (!(p.speed > 0.0)) raise_flag(tally, QSG_DEV_BAD_FACET);
+                    SlotState st;
+                    // CycleTracking.cc:37-39 replica selection by particle index
+                    st.rep = (int)(i % (uint64_t)tally.flux_replicas);
+                    st.segs = 0;
+                    st.prob = 0;
+                    pool_put<POOL>(v, slot, p, st);
+                    if (SENS) load_scores(in, i, s_scores + slot, POOL, sens.K);
+                    filled[r] = slot;
+                }
             }
-            ready |= warp_bits(filled) | warp_bits(filled2);
+#pragma unroll
+            for (int r = 0; r < (POOL + 31) / 32; r++) ready = ready | warp_slots<POOL>(filled[r]);
         }
-        const int nr = __popcll(ready), nc = __popcll(coll);
+        const int nr = ready.count(), nc = coll.count();
         if (nr == 0 && nc == 0) {
             if (exhausted) break;
             continue;
         }
         const bool do_coll = (nc >= 32) || (nc > nr);
-        const uint64_t sel = do_coll ? coll : ready;
+        const SlotMask sel = do_coll ? coll : ready;
         const int nsel = do_coll ? nc : nr;
         int slot = -1, next_state = 0;   // 0 empty, 1 ready, 2 collision pending
         if (lane < nsel) {
-            slot = nth_set_bit(sel, lane);
+            slot = sel.nth(lane);
             Particle p;
             SlotState st;
-            pool_get<kPool>(v, slot, p, st);
+            pool_get<POOL>(v, slot, tally, p, st);
             if (st.prob != cur_prob) {
                 if (cur_prob >= 0) bc.add(cur_prob, cnt);
                 cur_prob = st.prob;
@@ -1051,14 +1096,14 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
             const int cls = __ldg(t.cell_class + p.cell);
             if (do_coll) {
                 // CollisionEvent, both parts (see collision_select / collision_finish)
-                const int kind = collision_select<SENS>(t, tally, p, cls, cnt, sens, S, kPool);
+                const int kind = collision_select<SENS>(t, tally, p, cls, cnt, sens, S, POOL);
                 const bool alive = (kind != COLL_ENDS) &&
-                                   collision_finish<SENS>(t, tally, p, kind, extra, cnt, sens, S, kPool);
+                                   collision_finish<SENS>(t, tally, p, kind, extra, cnt, sens, S, POOL);
                 next_state = alive ? 1 : 0;
             } else {
                 double* flux_row = tally.flux + (int64_t)st.rep * t.num_cells * t.num_groups;
                 const int outcome = segment_outcome(t, tally, p, cls, flux_row);
-                if (SENS) sens_segment(t, sens, p, cls, outcome == OUT_COLLISION, S, kPool);
+                if (SENS) sens_segment(t, sens, p, cls, outcome == OUT_COLLISION, S, POOL);
                 cnt[LC_SEG]++;
                 p.num_segments += 1.;
                 if (outcome == OUT_COLLISION) {
@@ -1078,7 +1123,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
                         if (SENS) {
                             atomicAdd(sens.leak + st.prob, p.weight);
                             for (int k = 0; k < sens.K; k++) {
-                                const double sv = S[k * kPool];
+                                const double sv = S[k * POOL];
                                 if (sv != 0.0) atomicAdd(sens.dleak + (int64_t)st.prob * sens.K + k, p.weight * sv);
                             }
                         }
@@ -1098,7 +1143,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
                     uint64_t cs = append_slot(census);
                     if (cs < census.capacity) {
                         store_particle(census, cs, p);
-                        if (SENS) store_scores(census, cs, S, kPool, sens.K);
+                        if (SENS) store_scores(census, cs, S, POOL, sens.K);
                     } else {
                         raise_flag(tally, QSG_DEV_STORE_OVERFLOW);
                     }
@@ -1110,15 +1155,15 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
                     next_state = 0;
                 }
             }
-            if (next_state != 0) pool_put<kPool>(v, slot, p, st);
+            if (next_state != 0) pool_put<POOL>(v, slot, p, st);
         }
-        const uint64_t taken = warp_bits(slot);
-        const uint64_t now_ready = warp_bits(next_state == 1 ? slot : -1);
-        const uint64_t now_coll = warp_bits(next_state == 2 ? slot : -1);
-        if (do_coll) coll &= ~taken;
-        else ready &= ~taken;
-        ready |= now_ready;
-        coll |= now_coll;
+        const SlotMask taken = warp_slots<POOL>(slot);
+        const SlotMask now_ready = warp_slots<POOL>(next_state == 1 ? slot : -1);
+        const SlotMask now_coll = warp_slots<POOL>(next_state == 2 ? slot : -1);
+        if (do_coll) coll = coll & ~taken;
+        else ready = ready & ~taken;
+        ready = ready | now_ready;
+        coll = coll | now_coll;
     }
     bc.add_final(cur_prob, cnt);
     bc.flush_block<BLOCK>();
@@ -1164,7 +1209,42 @@ size_t track_smem_bytes_sens(const QsgHandle* h)
     return track_smem_bytes(h) + (size_t)h->sens.K * h->block_size * sizeof(double);
 }
 
-size_t track_pool_smem_bytes_per_block(int block, int num_problems, int K);
+size_t track_pool_smem_bytes(int block, int num_problems, int K, int pool);
+int pool_for_scores(int K, int num_problems);
+
+// The pool packs facet, flux replica and group into one word.
+bool pool_kernel_usable(const QsgHandle* h) { return h->num_groups <= 65535 && h->flux_replicas <= 255; }
+
+template <int B>
+const void* pool_kernel_fn(bool sens, int pool)
+{
+    if (!sens) return (const void*)track_pool_kernel<B, false, kPoolPlain>;
+    if (pool == 64) return (const void*)track_pool_kernel<B, true, 64>;
+    if (pool == 48) return (const void*)track_pool_kernel<B, true, 48>;
+    return (const void*)track_pool_kernel<B, true, 32>;
+}
+
+template <int B, bool SENS, int POOL>
+void launch_pool_t(QsgHandle* h, int grid, size_t smem, cudaStream_t s, const DevTally& tv,
+                   unsigned long long* cursor)
+{
+    track_pool_kernel<B, SENS, POOL><<<grid, B, smem, s>>>(h->tables, tv, h->processing.view, h->processed.view,
+                                                           h->extra.view, cursor, SENS ? h->sens : DevSens{});
+}
+
+template <int B>
+void launch_pool(QsgHandle* h, cudaStream_t s, const DevTally& tv, unsigned long long* cursor)
+{
+    if (h->sens.K == 0) {
+        launch_pool_t<B, false, kPoolPlain>(h, h->pool_blocks,
+                                            track_pool_smem_bytes(B, h->num_problems, 0, kPoolPlain), s, tv, cursor);
+        return;
+    }
+    const size_t smem = track_pool_smem_bytes(B, h->num_problems, h->sens.K, h->pool_sens);
+    if (h->pool_sens == 64) launch_pool_t<B, true, 64>(h, h->pool_sens_blocks, smem, s, tv, cursor);
+    else if (h->pool_sens == 48) launch_pool_t<B, true, 48>(h, h->pool_sens_blocks, smem, s, tv, cursor);
+    else launch_pool_t<B, true, 32>(h, h->pool_sens_blocks, smem, s, tv, cursor);
+}
 
 // Persistent grid for the current block size: SMs x resident blocks.
 int configure_track_grid(QsgHandle* h)
@@ -1190,13 +1270,16 @@ int configure_track_grid(QsgHandle* h)
         h->sens_track_blocks = h->num_sms * (per_sm > 0 ? per_sm : 1);
     }
     // particle-pool kernels (their pools live in dynamic shared memory)
+    h->pool_sens = pool_for_scores(h->sens.K, h->num_problems);
     for (int sens = 0; sens < 2; sens++) {
         if (sens && h->sens.K == 0) continue;
-        const size_t ps = track_pool_smem_bytes_per_block(h->block_size, h->num_problems, sens ? h->sens.K : 0);
-        const void* fn = h->block_size == 256
-                             ? (sens ? (const void*)track_pool_kernel<256, true> : (const void*)track_pool_kernel<256, false>)
-                             : (sens ? (const void*)track_pool_kernel<128, true> : (const void*)track_pool_kernel<128, false>);
+        const int pool = sens ? h->pool_sens : kPoolPlain;
+        const size_t ps = track_pool_smem_bytes(h->block_size, h->num_problems, sens ? h->sens.K : 0, pool);
+        const void* fn = h->block_size == 256 ? pool_kernel_fn<256>(sens, pool) : pool_kernel_fn<128>(sens, pool);
         QSG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps));
+#ifdef QSG_CARVEOUT
+        QSG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, QSG_CARVEOUT));
+#endif
         per_sm = 0;
         QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, h->block_size, ps));
         (sens ? h->pool_sens_blocks : h->pool_blocks) = h->num_sms * (per_sm > 0 ? per_sm : 1);
@@ -1506,26 +1589,9 @@ int launch_pass(QsgHandle* h, cudaStream_t s)
     QSG_CUDA(cudaMemsetAsync(h->extra.count, 0, sizeof(unsigned long long), s));
     QSG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s));
     const DevTally tv = tally_view(h);
-    if (h->kernel_kind == 1) {
-        const bool sens = h->sens.K > 0;
-        const size_t ps = track_pool_smem_bytes_per_block(h->block_size, h->num_problems, h->sens.K);
-        const int grid = sens ? h->pool_sens_blocks : h->pool_blocks;
-        const DevSens ds = sens ? h->sens : DevSens{};
-        if (h->block_size == 256) {
-            if (sens)
-                track_pool_kernel<256, true><<<grid, 256, ps, s>>>(h->tables, tv, h->processing.view, h->processed.view,
-                                                                   h->extra.view, cursor, ds);
-            else
-                track_pool_kernel<256, false><<<grid, 256, ps, s>>>(h->tables, tv, h->processing.view,
-                                                                    h->processed.view, h->extra.view, cursor, ds);
-        } else {
-            if (sens)
-                track_pool_kernel<128, true><<<grid, 128, ps, s>>>(h->tables, tv, h->processing.view, h->processed.view,
-                                                                   h->extra.view, cursor, ds);
-            else
-                track_pool_kernel<128, false><<<grid, 128, ps, s>>>(h->tables, tv, h->processing.view,
-                                                                    h->processed.view, h->extra.view, cursor, ds);
-        }
+    if (h->kernel_kind == 1 && pool_kernel_usable(h)) {
+        if (h->block_size == 256) launch_pool<256>(h, s, tv, cursor);
+        else launch_pool<128>(h, s, tv, cursor);
     } else if (h->sens.K > 0) {
         const size_t smem = track_smem_bytes_sens(h);
         if (h->block_size == 256)

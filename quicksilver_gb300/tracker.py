@@ -61,6 +61,10 @@ class Tracker:
         soa = N.soa_from_columns(cols)
         N.check(N.lib().qsg_set_particles(self._h, C.byref(soa), len(recs)))
 
+    def set_track_kernel(self, kind: int) -> None:
+        """1 (default): warp particle pools; 0: one history per lane."""
+        N.check(N.lib().qsg_set_track_kernel(self._h, kind))
+
     def track(self) -> None:
         N.check(N.lib().qsg_track_cycle_sync(self._h))
 

@@ -35,10 +35,11 @@ def compare_census(got, want):
         np.testing.assert_allclose(g[f], w[f], rtol=1e-7, atol=1e-12, err_msg=f)
 
 
-def run_parity(name, cycles=None, flux_replicas=1):
+def run_parity(name, cycles=None, flux_replicas=1, kernel=1):
     _, sim, hp = load_problem(f"{name}.inp")
     run = oracle_run(hp, sim)
     trk = Tracker(hp, flux_replicas=flux_replicas)
+    trk.set_track_kernel(kernel)
     n_cycles = sim.n_steps if cycles is None else cycles
     for c in range(n_cycles):
         run.cycle_init()
@@ -69,6 +70,13 @@ def test_gpu_tracking_matches_oracle(gpu, name):
 
 def test_gpu_tracking_config1(gpu):
     run_parity("config1")
+
+
+@pytest.mark.parametrize("name", ["t_fission", "t_nonflat", "t_scatter_octant"])
+def test_gpu_tracking_lane_kernel(gpu, name):
+    """The one-history-per-lane kernel (qsg_set_track_kernel(h, 0)) gives the
+    same results as the default particle-pool kernel."""
+    run_parity(name, kernel=0)
 
 
 def test_gpu_flux_replicas(gpu):
