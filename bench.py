@@ -585,7 +585,8 @@ def main():
         "device_flags": flags,
         "clocks": clocks.summary(),
     }
-    if not args.no_forms:
+    if not args.no_forms and world == 1:
+        # the forms compare single-GPU paths; replica runs (N > 1) report the plain line only
         line["forms"] = {"batched": measure_batched(), "adjoint": measure_adjoint()}
     if not args.no_cpu_baseline:
         rate, seg, secs = cpu_port_rate(DECK, 2, os.cpu_count() or 1)

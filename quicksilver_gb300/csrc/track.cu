@@ -1560,21 +1560,21 @@ int check_soa(const QsgParticleSoA* s)
 int copy_soa(const DevStore& d, const QsgParticleSoA* h, uint64_t n, bool to_device)
 {
     if (n == 0) return QSG_OK;
+    // the 20 field copies are issued back to back on the legacy stream and
+    // waited for once (they overlap when the host arrays are pinned)
     cudaMemcpyKind kind = to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
-    double* dd[12] = {d.x, d.y, d.z, d.vx, d.vy, d.vz, d.kinetic_energy, d.weight,
-                      d.time_to_census, d.age, d.num_mean_free_paths, d.num_segments};
-    double* hd[12] = {h->x, h->y, h->z, h->vx, h->vy, h->vz, h->kinetic_energy, h->weight,
-                      h->time_to_census, h->age, h->num_mean_free_paths, h->num_segments};
-    for (int k = 0; k < 12; k++)
-        QSG_CUDA(to_device ? cudaMemcpy(dd[k], hd[k], n * 8, kind) : cudaMemcpy(hd[k], dd[k], n * 8, kind));
-    uint64_t* du[2] = {d.seed, d.identifier};
-    uint64_t* hu[2] = {h->random_number_seed, h->identifier};
-    for (int k = 0; k < 2; k++)
-        QSG_CUDA(to_device ? cudaMemcpy(du[k], hu[k], n * 8, kind) : cudaMemcpy(hu[k], du[k], n * 8, kind));
-    int32_t* di[6] = {d.last_event, d.num_collisions, d.breed, d.species, d.domain, d.cell};
-    int32_t* hi[6] = {h->last_event, h->num_collisions, h->breed, h->species, h->domain, h->cell};
-    for (int k = 0; k < 6; k++)
-        QSG_CUDA(to_device ? cudaMemcpy(di[k], hi[k], n * 4, kind) : cudaMemcpy(hi[k], di[k], n * 4, kind));
+    void* dev[20] = {d.x, d.y, d.z, d.vx, d.vy, d.vz, d.kinetic_energy, d.weight, d.time_to_census, d.age,
+                     d.num_mean_free_paths, d.num_segments, d.seed, d.identifier, d.last_event, d.num_collisions,
+                     d.breed, d.species, d.domain, d.cell};
+    void* host[20] = {h->x, h->y, h->z, h->vx, h->vy, h->vz, h->kinetic_energy, h->weight, h->time_to_census,
+                      h->age, h->num_mean_free_paths, h->num_segments, h->random_number_seed, h->identifier,
+                      h->last_event, h->num_collisions, h->breed, h->species, h->domain, h->cell};
+    for (int k = 0; k < 20; k++) {
+        const size_t bytes = n * (k < 14 ? 8 : 4);
+        QSG_CUDA(to_device ? cudaMemcpyAsync(dev[k], host[k], bytes, kind, 0)
+                           : cudaMemcpyAsync(host[k], dev[k], bytes, kind, 0));
+    }
+    QSG_CUDA(cudaStreamSynchronize(0));
     return QSG_OK;
 }
 
