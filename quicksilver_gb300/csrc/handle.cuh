@@ -213,7 +213,8 @@ struct QsgHandle {
     qsg::DevBuf<int32_t> class_num_reactions, class_material, cell_class, adj_cell;
     qsg::DevBuf<int8_t> class_type;
     qsg::DevBuf<uint8_t> adj_facet_event, proj;
-    qsg::DevBuf<float4> plane32;
+    qsg::DevBuf<float4> face32;
+    qsg::DevBuf<float2> face_slack;
     qsg::DevBuf<float> node32;
     qsg::DevTables tables{};
     // host copies needed by the cycle set-up

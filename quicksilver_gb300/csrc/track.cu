@@ -90,23 +90,61 @@ __device__ __forceinline__ double distance_to_segment(double plane_tolerance, do
 // exactly in FP64.
 enum ScreenResult { SCREEN_EXACT = 0, SCREEN_HUGE = 1, SCREEN_ACCEPT = 2 };
 
-__device__ __forceinline__ int facet_screen(const float4 pl, uint8_t proj, const float* n32, const int8_t* loc,
+// The four facets of one hex face (facets 4k..4k+3 share the face-centre node
+// 8+k) lie in one plane up to FP64 rounding, so the screen takes the normal
+// and offset of the face once: `pl` is the face's plane in float (cell-local
+// offset), and sn / sd bound how far any of its facets' FP64 planes differ
+// from the one rounded (|dA|+|dB|+|dC| and |d offset|).  The quantities the
+// four facets share -- direction dot, numerator, distance along the ray --
+// are computed here with their error bounds.
+struct FaceScreen {
+    int state;   // SCREEN_HUGE or SCREEN_EXACT for all four facets, or -1: screen each facet
+    float n, e_n, d, e_d, tt, att, e_t;
+};
+
+__device__ __forceinline__ FaceScreen face_screen(const float4 pl, float x, float y, float z, float a, float b,
+                                                  float g, float pos_max, float slack, float sn, float sd)
+{
+    constexpr float u = 5.9604645e-8f;
+    FaceScreen fs;
+    fs.state = -1;
+    const float s_dot = fabsf(pl.x * a) + fabsf(pl.y * b) + fabsf(pl.z * g);
+    const float d = pl.x * a + pl.y * b + pl.z * g;
+    const float e_d = 16.0f * u * s_dot + 1e-12f + sn;
+    fs.d = d;
+    fs.e_d = e_d;
+    if (d < -e_d) {                  // every facet's FP64 dot <= 0: not a candidate
+        fs.state = SCREEN_HUGE;
+        return fs;
+    }
+    if (!(d > 2.0f * e_d)) {         // sign uncertain (or NaN): evaluate exactly
+        fs.state = SCREEN_EXACT;
+        return fs;
+    }
+    const float t_n = fabsf(pl.x * x) + fabsf(pl.y * y) + fabsf(pl.z * z) + fabsf(pl.w);
+    const float n = -(pl.x * x + pl.y * y + pl.z * z + pl.w);
+    const float e_n = 16.0f * u * t_n + slack + sn * pos_max + sd;
+    const float tt = n * __frcp_rn(d);
+    const float att = fabsf(tt);
+    fs.n = n;
+    fs.e_n = e_n;
+    fs.tt = tt;
+    fs.att = att;
+    fs.e_t = (e_n + att * e_d * 1.01f) / (d - e_d) + 4.0f * u * att;
+    return fs;
+}
+
+// The rest of the screen for one facet of a face that passed face_screen:
+// returns SCREEN_HUGE when the reference's FP64 inside test (MCT.cc:331-393)
+// must fail, SCREEN_ACCEPT when it must pass (then the FP64 distance is just
+// numerator / dot), SCREEN_EXACT when the bounds do not decide.
+__device__ __forceinline__ int facet_screen(const FaceScreen& fs, uint8_t proj, const float* n32, const int8_t* loc,
                                             float x, float y, float z, float a, float b, float g,
                                             float pos_max, float slack)
 {
     constexpr float u = 5.9604645e-8f;
     if (proj == 0xff) return SCREEN_HUGE;   // no dominant normal component: the FP64 test always fails
-    const float s_dot = fabsf(pl.x * a) + fabsf(pl.y * b) + fabsf(pl.z * g);
-    const float d = pl.x * a + pl.y * b + pl.z * g;
-    const float e_d = 16.0f * u * s_dot + 1e-12f;
-    if (d < -e_d) return SCREEN_HUGE;            // FP64 dot <= 0: not a candidate
-    if (!(d > 2.0f * e_d)) return SCREEN_EXACT;  // sign uncertain (or NaN): evaluate exactly
-    const float t_n = fabsf(pl.x * x) + fabsf(pl.y * y) + fabsf(pl.z * z) + fabsf(pl.w);
-    const float n = -(pl.x * x + pl.y * y + pl.z * z + pl.w);
-    const float e_n = 16.0f * u * t_n + slack;
-    const float tt = n * __frcp_rn(d);
-    const float att = fabsf(tt);
-    const float e_t = (e_n + att * e_d * 1.01f) / (d - e_d) + 4.0f * u * att;
+    const float n = fs.n, e_n = fs.e_n, tt = fs.tt, att = fs.att, e_t = fs.e_t;
     const int iu = proj & 3, iv = proj >> 2;
     const float pu = (iu == 0) ? x : ((iu == 1) ? y : z);
     const float pv = (iv == 0) ? x : ((iv == 1) ? y : z);
@@ -175,7 +213,8 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
     const int cell = p.cell;
     const double* planes = t.planes + (int64_t)cell * (kFacets * 4);
     const double* nodes = t.cell_nodes + (int64_t)cell * (kCellPoints * 3);
-    const float4* pl32 = t.plane32 + (int64_t)cell * kFacets;
+    const float4* pf32 = t.face32 + (int64_t)cell * 6;
+    const float2 fsl = __ldg(t.face_slack + cell);
     const float* n32 = t.node32 + (int64_t)cell * (kCellPoints * 3);
     const uint8_t* proj = t.proj + (int64_t)cell * kFacets;
     const double* ctr = t.cell_center + 3 * (int64_t)cell;
@@ -188,12 +227,23 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
         const float x32 = (float)(p.x - cx), y32 = (float)(p.y - cy), z32 = (float)(p.z - cz);
         const float pos_max = fmaxf(fabsf(x32), fmaxf(fabsf(y32), fabsf(z32)));
         uint32_t exact = 0, accept = 0;
-#pragma unroll 4
-        for (int f = 0; f < kFacets; f++) {
-            const int s = facet_screen(__ldg(pl32 + f), __ldg(proj + f), n32, kFacetLocal[f], x32, y32, z32, a32, b32,
-                                       g32, pos_max, slack);
-            if (s == SCREEN_EXACT) exact |= 1u << f;
-            else if (s == SCREEN_ACCEPT) accept |= 1u << f;
+#pragma unroll 1
+        for (int fc = 0; fc < 6; fc++) {
+            const FaceScreen fs = face_screen(__ldg(pf32 + fc), x32, y32, z32, a32, b32, g32, pos_max, slack, fsl.x,
+                                              fsl.y);
+            if (fs.state == SCREEN_HUGE) continue;
+            if (fs.state == SCREEN_EXACT) {
+                exact |= 0xfu << (4 * fc);
+                continue;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int f = 4 * fc + k;
+                const int s = facet_screen(fs, __ldg(proj + f), n32, kFacetLocal[f], x32, y32, z32, a32, b32, g32,
+                                           pos_max, slack);
+                if (s == SCREEN_EXACT) exact |= 1u << f;
+                else if (s == SCREEN_ACCEPT) accept |= 1u << f;
+            }
         }
         // proven-accepted facets need only the reference's numerator / dot
         // (MCT.cc:291-307, 582-585); everything else screened is _hugeDouble
@@ -1508,7 +1558,8 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
     // FP32 screening tables in cell-local coordinates (origin: the cell's
     // MCT_Cell_Position_3D_G centre), and the projection of each facet's FP64
     // inside test (MCT.cc:331-385: C, then B, then A dominant).
-    std::vector<float4> plane32((size_t)C * kFacets);
+    std::vector<float4> face32((size_t)C * 6);
+    std::vector<float2> face_slack((size_t)C);
     std::vector<float> node32((size_t)C * kCellPoints * 3);
     std::vector<uint8_t> proj((size_t)C * kFacets);
     double lmax = 0.0, dmax = 0.0;
@@ -1521,11 +1572,18 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
             node32[(c * kCellPoints + k) * 3 + 2] = (float)(nd[2] - cz);
             lmax = std::max(lmax, fabs(nd[0]) + fabs(nd[1]) + fabs(nd[2]));
         }
+        double sn = 0.0, sd = 0.0;
         for (int f = 0; f < kFacets; f++) {
             const double* pl = &planes[(c * kFacets + f) * 4];
             const double A = pl[0], B = pl[1], Cc = pl[2], D = pl[3];
             const double dl = D + A * cx + B * cy + Cc * cz;
-            plane32[c * kFacets + f] = make_float4((float)A, (float)B, (float)Cc, (float)dl);
+            // the face's plane is its first facet's; the others' differences
+            // from it go into the face slack
+            const double* rep = &planes[(c * kFacets + (f & ~3)) * 4];
+            const double dlr = rep[3] + rep[0] * cx + rep[1] * cy + rep[2] * cz;
+            if ((f & 3) == 0) face32[c * 6 + f / 4] = make_float4((float)A, (float)B, (float)Cc, (float)dl);
+            sn = std::max(sn, fabs(A - rep[0]) + fabs(B - rep[1]) + fabs(Cc - rep[2]));
+            sd = std::max(sd, fabs(dl - dlr));
             dmax = std::max(dmax, fabs(D));
             uint8_t pr;
             if (Cc < -0.5 || Cc > 0.5) pr = 0 | (1 << 2);
@@ -1534,9 +1592,15 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
             else pr = 0xff;
             proj[c * kFacets + f] = pr;
         }
+        // twice the largest difference, rounded up to float (and above the
+        // FP64 rounding of the differences themselves)
+        face_slack[c] = make_float2((float)(2.0 * sn * (1.0 + 1e-6)) + 1e-30f, (float)(2.0 * sd * (1.0 + 1e-6)) + 1e-30f);
     }
-    if ((st = h->plane32.upload(plane32)) || (st = h->node32.upload(node32)) || (st = h->proj.upload(proj))) return st;
-    t.plane32 = h->plane32.ptr;
+    if ((st = h->face32.upload(face32)) || (st = h->face_slack.upload(face_slack)) || (st = h->node32.upload(node32)) ||
+        (st = h->proj.upload(proj)))
+        return st;
+    t.face32 = h->face32.ptr;
+    t.face_slack = h->face_slack.ptr;
     t.node32 = h->node32.ptr;
     t.proj = h->proj.ptr;
     // FP64 rounding of quantities formed from global coordinates (numerator,
@@ -1806,7 +1870,7 @@ extern "C" int qsg_destroy(QsgHandle* h)
     h->material_mass.free(); h->cell_nodes.free(); h->cell_center.free(); h->planes.free();
     h->class_num_reactions.free(); h->class_material.free(); h->cell_class.free(); h->adj_cell.free();
     h->class_type.free(); h->adj_facet_event.free();
-    h->plane32.free(); h->node32.free(); h->proj.free();
+    h->face32.free(); h->face_slack.free(); h->node32.free(); h->proj.free();
     h->flux.free(); h->balance.free(); h->flags.free(); h->flux_partial.free();
     h->cell_volume.free(); h->cell_id.free(); h->src_cell.free(); h->src_cell_count.free();
     h->src_cell_offset.free(); h->scalars.free(); h->history.free();

@@ -105,11 +105,14 @@ struct DevTables {
     const uint8_t* adj_facet_event;// [C][24] facet | (event << 5)
     double time_step;
     // FP32 pre-filter of the facet search, in cell-local coordinates
-    // (origin at cell_center): plane (A, B, C, D + A cx + B cy + C cz) rounded
-    // to float, node coordinates minus the centre rounded to float, and the
-    // projection the FP64 inside test uses for each facet (u | v << 2, or
-    // 0xff when no normal component exceeds 0.5 in magnitude).
-    const float4* plane32;         // [C][24]
+    // (origin at cell_center): each hex face's plane (A, B, C, D + A cx + B cy
+    // + C cz) rounded to float, with per-cell bounds on how far the face's
+    // four facets' FP64 planes differ from it, node coordinates minus the
+    // centre rounded to float, and the projection the FP64 inside test uses
+    // for each facet (u | v << 2, or 0xff when no normal component exceeds
+    // 0.5 in magnitude).
+    const float4* face32;          // [C][6]
+    const float2* face_slack;      // [C] (normal, offset)
     const float* node32;           // [C][14][3]
     const uint8_t* proj;           // [C][24]
     double abs_slack;              // bound on FP64 rounding of global-coordinate quantities
