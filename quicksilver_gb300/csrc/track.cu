@@ -198,6 +198,87 @@ __device__ __forceinline__ int facet_screen(const FaceScreen& fs, uint8_t proj, 
     return SCREEN_EXACT;
 }
 
+// The four facets of face fc together, when they share one projection (the
+// usual case: one normal): facet k of the face is the triangle (corner k,
+// corner k+1, centre) of the face's corner cycle (kFacetLocal[4fc+k] =
+// {corner k, corner k+1, centre}), so its three crosses are the rim cross
+// corner k -> corner k+1, the spoke cross corner k+1 -> centre, and the
+// reverse of the spoke cross corner k -> centre (in exact arithmetic
+// (c - m) x (ip - m) = -(m - c) x (ip - c)).  Eight crosses instead of twelve
+// and five vertex loads instead of twelve; each estimate keeps the error bound
+// of the cross it was computed as.  Bits 0-3 of the result: facets to
+// evaluate exactly; bits 4-7: proven accepted.
+__device__ __forceinline__ uint32_t face_facets_screen(const FaceScreen& fs, uint8_t proj, const float* n32, int fc,
+                                                       float x, float y, float z, float a, float b, float g,
+                                                       float pos_max, float slack)
+{
+    constexpr float u = 5.9604645e-8f;
+    const float n = fs.n, e_n = fs.e_n, tt = fs.tt, att = fs.att, e_t = fs.e_t;
+    const int iu = proj & 3, iv = proj >> 2;
+    const float pu = (iu == 0) ? x : ((iu == 1) ? y : z);
+    const float pv = (iv == 0) ? x : ((iv == 1) ? y : z);
+    const float du = (iu == 0) ? a : ((iu == 1) ? b : g);
+    const float dv = (iv == 0) ? a : ((iv == 1) ? b : g);
+    const float ipu = pu + tt * du;
+    const float ipv = pv + tt * dv;
+    const float ip_max = fmaxf(fabsf(ipu), fabsf(ipv));
+    const float e_ip = e_t + 3.0f * u * (pos_max + att + ip_max) + slack;
+    float cu[4], cv[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int node = kFacetLocal[4 * fc + k][0];
+        cu[k] = __ldg(n32 + 3 * node + iu);
+        cv[k] = __ldg(n32 + 3 * node + iv);
+    }
+    const int centre = kFacetLocal[4 * fc][2];
+    const float mu = __ldg(n32 + 3 * centre + iu), mv = __ldg(n32 + 3 * centre + iv);
+    float amax = fmaxf(fabsf(mu), fabsf(mv));
+#pragma unroll
+    for (int k = 0; k < 4; k++) amax = fmaxf(amax, fmaxf(fabsf(cu[k]), fabsf(cv[k])));
+    const float e_v = 3.0f * u * amax + slack;   // vertex: float rounding of (node - centre)
+    // rim[k]: corner k -> corner k+1; spoke[k]: corner k -> face centre
+    float rim[4], erim[4], spoke[4], espoke[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int k1 = (k + 1) & 3;
+        const float ru = ipu - cu[k], rv = ipv - cv[k];
+        {
+            const float eu = cu[k1] - cu[k], ev = cv[k1] - cv[k];
+            rim[k] = eu * rv - ev * ru;
+            erim[k] = (fabsf(ru) + fabsf(rv)) * (2.0f * e_v) + (fabsf(eu) + fabsf(ev)) * (e_ip + e_v) +
+                      8.0f * u * (fabsf(eu * rv) + fabsf(ev * ru));
+        }
+        {
+            const float eu = mu - cu[k], ev = mv - cv[k];
+            spoke[k] = eu * rv - ev * ru;
+            espoke[k] = (fabsf(ru) + fabsf(rv)) * (2.0f * e_v) + (fabsf(eu) + fabsf(ev)) * (e_ip + e_v) +
+                        8.0f * u * (fabsf(eu * rv) + fabsf(ev * ru));
+        }
+    }
+    uint32_t res = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int k1 = (k + 1) & 3;
+        // the reference's cross1 (0->1), cross2 (1->2), cross0 (2->0)
+        const float c1 = rim[k], c2 = spoke[k1], c0 = -spoke[k];
+        const float cmin = fminf(c0, fminf(c1, c2)), cmax = fmaxf(c0, fmaxf(c1, c2));
+        const float csum = c0 + c1 + c2;
+        const float ecmax = fmaxf(erim[k], fmaxf(espoke[k1], espoke[k]));
+        const float cabs = fmaxf(fabsf(cmin), fabsf(cmax));
+        const float tol = 1.01e-9f * (fabsf(csum) + 3.0f * ecmax + 12.0f * u * cabs) + 1e-30f;
+        const float thr = tol + ecmax;
+        if ((cmin <= -thr) && (cmax >= thr)) continue;   // proven outside: _hugeDouble
+        // proven acceptance, as in facet_screen
+        const float m = e_ip + e_v + slack;
+        const float umin = fminf(cu[k], fminf(cu[k1], mu)), umax = fmaxf(cu[k], fmaxf(cu[k1], mu));
+        const float vmin = fminf(cv[k], fminf(cv[k1], mv)), vmax = fmaxf(cv[k], fmaxf(cv[k1], mv));
+        const bool bbox_in = (umin <= ipu - m) && (umax >= ipu + m) && (vmin <= ipv - m) && (vmax >= ipv + m);
+        const bool same_sign = (cmin > ecmax) || (cmax < -ecmax);
+        res |= (n > e_n && bbox_in && same_sign) ? (16u << k) : (1u << k);
+    }
+    return res;
+}
+
 // MCT_Nearest_Facet (MCT.cc:86-137) with MCT_Nearest_Facet_3D_G
 // (MCT.cc:549-621) and both Find_Nearest overloads (MCT.cc:436-536).
 // Facets the FP32 screen proves to be _hugeDouble are not evaluated; the rest
@@ -234,6 +315,13 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
             if (fs.state == SCREEN_HUGE) continue;
             if (fs.state == SCREEN_EXACT) {
                 exact |= 0xfu << (4 * fc);
+                continue;
+            }
+            const uchar4 pr4 = __ldg(reinterpret_cast<const uchar4*>(proj) + fc);
+            if (pr4.x == pr4.y && pr4.x == pr4.z && pr4.x == pr4.w && pr4.x != 0xff) {
+                const uint32_t r = face_facets_screen(fs, pr4.x, n32, fc, x32, y32, z32, a32, b32, g32, pos_max, slack);
+                exact |= (r & 0xfu) << (4 * fc);
+                accept |= ((r >> 4) & 0xfu) << (4 * fc);
                 continue;
             }
 #pragma unroll
