@@ -617,6 +617,10 @@ __device__ __forceinline__ bool collision_finish(const DevTables& t, const DevTa
     if (kind == COLL_SCATTER) {
         update_trajectory(p.pend_e, p.pend_a, p);
         p.group = energy_group(t, p.kinetic_energy);
+        // |velocity| of the new velocity, which the next segment needs
+        // (MC_Segment_Outcome.cc recomputes it there; same expression, same
+        // bits), computed here while the warp's lanes run together
+        p.speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
         return true;
     }
     double e_out[4], a_out[4];
@@ -654,6 +658,7 @@ __device__ __forceinline__ bool collision_finish(const DevTables& t, const DevTa
         }
     }
     p.group = energy_group(t, p.kinetic_energy);
+    if (num == 1) p.speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
     return num == 1;
 }
 
