@@ -825,10 +825,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
     const uint64_t n = *in.count;
     Particle p;
     bool active = false, exhausted = false;
-    // collision stage of a parked lane: 0 none, 1 reaction selection pending,
-    // 2 trajectory update pending (kind in pend_kind)
-    int stage = 0;
-    int pend_kind = COLL_ENDS;
+    int stage = 0;   // 1: parked at a collision
     double* flux_row = tally.flux;
     uint64_t segs_this_history = 0;
     uint64_t next = 0, end = 0;   // this lane's claimed run of queue positions
@@ -867,44 +864,17 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
         // together once enough of them wait, or when nothing else can run.  A
         // particle's own state and random stream are untouched while it waits,
         // so the results are unchanged.
-#if QSG_COLL_MODE == 2
-        // two levels: the reaction selection for parked lanes, then (only for
-        // scatter / fission, an absorption ends the history there) the
-        // trajectory update -- log, sincos, rotation, most of the FP64 work --
-        // so that absorbed lanes do not idle through it
-        const unsigned fin_mask = __ballot_sync(0xffffffffu, active && stage == 2);
-        const unsigned sel_mask = __ballot_sync(0xffffffffu, active && stage == 1);
-        const unsigned run_mask = __ballot_sync(0xffffffffu, active && stage == 0);
-        if (fin_mask != 0u && (__popc(fin_mask) >= tally.collision_batch || (run_mask | sel_mask) == 0u)) {
-            if (stage == 2) {
-                stage = 0;
-                active = collision_finish<SENS>(t, tally, p, pend_kind, extra, cnt, sens, S, BLOCK);
-            }
-            continue;
-        }
-        if (sel_mask != 0u && (__popc(sel_mask) >= tally.collision_batch || run_mask == 0u)) {
-            if (stage == 1) {
-                pend_kind = collision_select<SENS>(t, tally, p, __ldg(t.cell_class + p.cell), cnt, sens, S, BLOCK);
-                stage = (pend_kind == COLL_ENDS) ? 0 : 2;
-                active = pend_kind != COLL_ENDS;
-            }
-            continue;
-        }
-#else
         const unsigned pend_mask = __ballot_sync(0xffffffffu, active && stage != 0);
         const unsigned run_mask = __ballot_sync(0xffffffffu, active && stage == 0);
         if (pend_mask != 0u && (__popc(pend_mask) >= tally.collision_batch || run_mask == 0u)) {
             if (stage != 0) {
-#if QSG_COLL_MODE == 0
-                pend_kind = collision_select<SENS>(t, tally, p, __ldg(t.cell_class + p.cell), cnt, sens, S, BLOCK);
-#endif
+                const int kind =
+                    collision_select<SENS>(t, tally, p, __ldg(t.cell_class + p.cell), cnt, sens, S, BLOCK);
                 stage = 0;
-                active = (pend_kind != COLL_ENDS) &&
-                         collision_finish<SENS>(t, tally, p, pend_kind, extra, cnt, sens, S, BLOCK);
+                active = (kind != COLL_ENDS) && collision_finish<SENS>(t, tally, p, kind, extra, cnt, sens, S, BLOCK);
             }
             continue;
         }
-#endif
         if (active && stage == 0) {
             bool keep;
             const int cls = __ldg(t.cell_class + p.cell);
@@ -913,15 +883,8 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
             cnt[LC_SEG]++;
             p.num_segments += 1.;
             if (outcome == OUT_COLLISION) {
-#if QSG_COLL_MODE == 1
-                // reaction selection right away: an absorption ends the history now
-                pend_kind = collision_select<SENS>(t, tally, p, cls, cnt, sens, S, BLOCK);
-                keep = pend_kind != COLL_ENDS;
-                stage = keep ? 2 : 0;
-#else
                 stage = 1;
                 keep = true;
-#endif
             } else if (outcome == OUT_FACET) {
                 // MC_Facet_Crossing_Event, MC_Facet_Crossing_Event.cc:23-70
                 const int64_t fi = (int64_t)p.cell * kFacets + p.facet;

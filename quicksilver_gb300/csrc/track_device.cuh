@@ -27,12 +27,6 @@ constexpr int kFacets = 24;
 #ifndef QSG_MIN_BLOCKS
 #define QSG_MIN_BLOCKS 3
 #endif
-// How a warp batches its collisions: 0 = selection and trajectory update in
-// one batched step; 1 = selection right after the segment, trajectory update
-// batched; 2 = both batched, in two levels.
-#ifndef QSG_COLL_MODE
-#define QSG_COLL_MODE 0
-#endif
 #ifndef QSG_COLLISION_BATCH
 #define QSG_COLLISION_BATCH 16
 #endif
