@@ -28,6 +28,15 @@ QSG_ERR_IO = 6
 QSG_ERR_NO_DEVICE = 7
 QSG_OBSERVE_FLUENCE = 1
 QSG_OBSERVE_SPECTRUM = 2
+# device error flag bits (qsg_device_status)
+QSG_DEV_SEGMENT_LIMIT = 1 << 0
+QSG_DEV_TRACKING_LIMIT = 1 << 1
+QSG_DEV_NO_REACTION = 1 << 2
+QSG_DEV_OFF_PROCESSOR = 1 << 3
+QSG_DEV_STORE_OVERFLOW = 1 << 4
+QSG_DEV_BAD_FACET = 1 << 5
+QSG_DEV_NEGATIVE_DISTANCE = 1 << 6
+QSG_DEV_PASS_LIMIT = 1 << 7
 
 BALANCE_FIELDS = ("absorb", "census", "escape", "collision", "end", "fission", "produce",
                   "scatter", "start", "source", "rr", "split", "num_segments")

@@ -274,7 +274,9 @@ __global__ void __launch_bounds__(kInitBlock) population_kernel(CycleArgs a, Dev
     if (use_smem)
         for (int k = threadIdx.x; k < 2 * a.num_problems; k += kInitBlock) s_rr[k] = 0;
     __syncthreads();
-    const uint64_t n = *in.count;
+    // a store that overflowed holds `capacity` particles (the writers raised
+    // QSG_DEV_STORE_OVERFLOW)
+    const uint64_t n = min((uint64_t)*in.count, in.capacity);
     for (uint64_t i = (uint64_t)blockIdx.x * kInitBlock + threadIdx.x; i < n; i += (uint64_t)gridDim.x * kInitBlock) {
         Particle p;
         load_record(in, i, p);

@@ -822,7 +822,9 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
 #pragma unroll
     for (int k = 0; k < LC_N; k++) cnt[k] = 0;
     int cur_prob = -1;
-    const uint64_t n = *in.count;
+    // a store that overflowed holds `capacity` particles (its writers raised
+    // QSG_DEV_STORE_OVERFLOW)
+    const uint64_t n = min((uint64_t)*in.count, in.capacity);
     Particle p;
     bool active = false, exhausted = false;
     int stage = 0;   // 1: parked at a collision
@@ -1143,7 +1145,9 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
 #pragma unroll
     for (int k = 0; k < LC_N; k++) cnt[k] = 0;
     int cur_prob = -1;
-    const uint64_t n = *in.count;
+    // a store that overflowed holds `capacity` particles (its writers raised
+    // QSG_DEV_STORE_OVERFLOW)
+    const uint64_t n = min((uint64_t)*in.count, in.capacity);
     SlotMask ready = {0, 0}, coll = {0, 0};   // warp-uniform
     bool exhausted = false;
     for (;;) {
@@ -2004,6 +2008,9 @@ extern "C" int qsg_get_census(QsgHandle* h, QsgParticleSoA* host, uint64_t cap, 
     *n_out = c;
     if (c > cap) return fail(QSG_ERR_CAPACITY, "qsg_get_census: %llu particles, capacity %llu", c,
                              (unsigned long long)cap);
+    if (c > h->processed.capacity)
+        return fail(QSG_ERR_DEVICE, "qsg_get_census: store overflowed (%llu > %llu)", c,
+                    (unsigned long long)h->processed.capacity);
     if (c == 0) return QSG_OK;
     if ((st = check_soa(host))) return st;
     return copy_soa(h->processed.view, host, c, false);
