@@ -177,13 +177,13 @@ def measure_batched(tune_space=None):
     offs = [seed_offset(d.simulation.seed) for d in decks]
     cycles = decks[0].simulation.n_steps
     t0 = time.perf_counter()
-    space = tune_space or {"block_size": (128, 256), "collision_batch": (16,), "queue_chunk": (1, 4),
+    space = tune_space or {"block_size": (128,), "pool_collision_step": (24, 32), "pool_refill": (8, 16, 32),
                            "flux_replicas": (1,)}
     best = autotune(texts, scale=0.1, cycles=1, warmup=1, cache_path=None, space=space, problems=problems)
     tune_s = time.perf_counter() - t0
     bmc = BatchMonteCarlo(decks, problems=problems, seed_offsets=offs, flux_replicas=best["flux_replicas"])
     try:
-        bmc.tune(best["block_size"], best["collision_batch"], best["queue_chunk"])
+        bmc.tune(**{k: best[k] for k in ("block_size", "pool_collision_step", "pool_refill") if k in best})
         bmc.run(1, use_graph=True)             # warm-up cycle (captures the graphs)
         first = bmc.cycles
         _sync()
@@ -219,7 +219,7 @@ def measure_batched(tune_space=None):
             "plain_problem_by_problem_segments_per_s": seg_plain / t_plain, "plain_s": t_plain,
             "speedup_at_equal_tally_error": (seg_b / t_batch) / (seg_plain / t_plain),
             "segments": seg_b, "balance_bit_exact_vs_plain": same, "device_flags": flags,
-            "tuning": {k: best[k] for k in ("block_size", "collision_batch", "queue_chunk", "flux_replicas")},
+            "tuning": {k: best[k] for k in ("block_size", "pool_collision_step", "pool_refill", "flux_replicas")},
             "tune_s": tune_s, "timing": "wall clock, whole cycles, synchronised"}
 
 

@@ -328,6 +328,11 @@ int qsg_set_tuning(QsgHandle* h, int32_t block_size, int32_t collision_batch, in
  * per step; 0 = one history per lane (collisions batched per warp).  Both
  * give the same results. */
 int qsg_set_track_kernel(QsgHandle* h, int32_t kind);
+/* Pool-kernel knobs: a collision step runs once this many pooled particles
+ * wait at a collision (1-32, default 32; otherwise the larger kind runs), and
+ * empty pool slots are refilled from the work queue once this many are empty
+ * (1-64, default 16); 0 keeps a value. */
+int qsg_set_pool_tuning(QsgHandle* h, int32_t collision_step, int32_t refill);
 
 /* ---- tracking without allocation ---------------------------------------- */
 /* No counterpart in the reference (Quicksilver allocates its vaults itself).

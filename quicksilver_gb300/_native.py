@@ -144,6 +144,7 @@ _SIGNATURES = {
     "qsg_num_problems": ([_VP, C.POINTER(C.c_int32), _ip], C.c_int),
     "qsg_set_tuning": ([_VP, C.c_int32, C.c_int32, C.c_int32], C.c_int),
     "qsg_set_track_kernel": ([_VP, C.c_int32], C.c_int),
+    "qsg_set_pool_tuning": ([_VP, C.c_int32, C.c_int32], C.c_int),
     "qsg_run_cycles": ([_VP, C.c_int32, C.c_int32, _VP], C.c_int),
     "qsg_cycle_init": ([_VP, _VP], C.c_int),
     "qsg_cycle_finalize": ([_VP, _VP], C.c_int),

@@ -1,8 +1,11 @@
 """Autotuner for the tracking kernel's shape on a given workload.
 
-Candidates: tracking-kernel block size (128 / 256 threads), collisions batched
-per warp step (8 / 16 / 24), particles claimed per work-queue atomic
-(1 / 4) and flux-tally replication (1 / 2 privatised copies).  Each candidate
+Candidates: tracking-kernel block size (128 / 256 threads), the pool kernel's
+collision-step threshold (24 / 32 pooled collisions) and refill threshold
+(8 / 16 / 32 empty slots), and flux-tally replication (1 / 2 privatised
+copies).  (The one-history-per-lane kernel's knobs -- collisions batched per
+warp step, particles claimed per queue atomic -- can be searched the same way
+by naming them in `space`.)  Each candidate
 runs whole cycles (CUDA-graph replays, as production does) on a *scratch*
 batch built from the same decks -- so tuning never advances the random
 streams of the run that is being tuned -- optionally with the particle counts
@@ -25,11 +28,12 @@ DEFAULT_CACHE = Path(os.environ.get("QSG_TUNE_CACHE", Path.home() / ".cache" / "
 
 CANDIDATES = {
     "block_size": (128, 256),
-    "collision_batch": (8, 16, 24),
-    "queue_chunk": (1, 4),
+    "pool_collision_step": (24, 32),
+    "pool_refill": (8, 16, 32),
     "flux_replicas": (1, 2),
 }
-DEFAULT = {"block_size": 128, "collision_batch": 16, "queue_chunk": 1, "flux_replicas": 1}
+DEFAULT = {"block_size": 128, "pool_collision_step": 32, "pool_refill": 16, "flux_replicas": 1}
+KNOBS = ("block_size", "collision_batch", "queue_chunk", "pool_collision_step", "pool_refill")
 
 
 def signature(decks: list) -> str:
@@ -43,9 +47,9 @@ def signature(decks: list) -> str:
 def _time_candidate(deck_texts, scale, cand, cycles, warmup, max_passes, problems=None):
     decks = [Deck.from_string(t, {"nParticles": max(1000, int(Deck.from_string(t).simulation.n_particles * scale))})
              for t in deck_texts]
-    bmc = BatchMonteCarlo(decks, flux_replicas=cand["flux_replicas"], max_passes=max_passes, problems=problems)
+    bmc = BatchMonteCarlo(decks, flux_replicas=cand.get("flux_replicas", 1), max_passes=max_passes, problems=problems)
     try:
-        bmc.tune(cand["block_size"], cand["collision_batch"], cand["queue_chunk"])
+        bmc.tune(**{k: cand[k] for k in KNOBS if k in cand})
         bmc.run(warmup, use_graph=True)
         t0 = time.perf_counter()
         hist = bmc.run(cycles, use_graph=True)   # history read synchronises
@@ -58,8 +62,8 @@ def _time_candidate(deck_texts, scale, cand, cycles, warmup, max_passes, problem
 def autotune(deck_texts: list, scale: float = 0.25, cycles: int = 2, warmup: int = 1, max_passes: int = 16,
              cache_path: Path | None = DEFAULT_CACHE, space: dict | None = None, refresh: bool = False,
              problems: list | None = None) -> dict:
-    """Return the fastest candidate for these decks (dict with the four knobs plus
-    `segments_per_s` and `trials`).  `deck_texts` are Quicksilver deck strings;
+    """Return the fastest candidate for these decks (dict with the searched knobs
+    plus `segments_per_s` and `trials`).  `deck_texts` are Quicksilver deck strings;
     `problems` (optional) are their already-built tables, reused by every
     candidate (the tables do not depend on the particle count)."""
     decks = [Deck.from_string(t) for t in deck_texts]

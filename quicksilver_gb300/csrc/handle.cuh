@@ -199,6 +199,8 @@ struct QsgHandle {
     int kernel_kind = 1;             // 0: one history per lane; 1: warp particle pool (qsg_set_track_kernel)
     int pool_blocks = 0, pool_sens_blocks = 0;   // persistent grids of the pool kernel
     int pool_sens = 64;                           // pool size of the sensitivity instantiation
+    int pool_collision_step = 32;                 // qsg_set_pool_tuning
+    int pool_refill = 16;
     int max_passes = 8;              // fission passes per asynchronous cycle
     int collision_batch = qsg::kCollisionBatch;
     int queue_chunk = 1;

@@ -1155,7 +1155,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
         const SlotMask empty = ~(ready | coll) & all_slots<POOL>();
         const int n_empty = empty.count();
         const int nr0 = ready.count(), nc0 = coll.count();
-        if (!exhausted && n_empty > 0 && (n_empty >= 16 || (nr0 < 32 && nc0 < 32))) {
+        if (!exhausted && n_empty > 0 && (n_empty >= tally.pool_refill || (nr0 < 32 && nc0 < 32))) {
             unsigned long long base = 0;
             if (lane == 0) base = atomicAdd(cursor, (unsigned long long)n_empty);
             base = __shfl_sync(0xffffffffu, base, 0);
@@ -1189,7 +1189,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
             if (exhausted) break;
             continue;
         }
-        const bool do_coll = (nc >= 32) || (nc > nr);
+        const bool do_coll = (nc >= tally.pool_collision_step) || (nc > nr);
         const SlotMask sel = do_coll ? coll : ready;
         const int nsel = do_coll ? nc : nr;
         int slot = -1, next_state = 0;   // 0 empty, 1 ready, 2 collision pending
@@ -1306,6 +1306,8 @@ DevTally tally_view(QsgHandle* h)
     t.num_problems = h->num_problems;
     t.collision_batch = h->collision_batch;
     t.queue_chunk = h->queue_chunk;
+    t.pool_collision_step = h->pool_collision_step;
+    t.pool_refill = h->pool_refill;
     return t;
 }
 
@@ -1896,6 +1898,17 @@ extern "C" int qsg_num_problems(QsgHandle* h, int32_t* n, int32_t* cell_offsets)
     *n = h->num_problems;
     if (cell_offsets)
         for (int k = 0; k <= h->num_problems; k++) cell_offsets[k] = h->h_problem_cell_offset[k];
+    return QSG_OK;
+}
+
+extern "C" int qsg_set_pool_tuning(QsgHandle* h, int32_t collision_step, int32_t refill)
+{
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_set_pool_tuning: null handle");
+    if (collision_step < 0 || collision_step > 32 || refill < 0 || refill > 64)
+        return fail(QSG_ERR_INVALID, "qsg_set_pool_tuning: collision step 1-32 and refill 1-64 (0 keeps a value)");
+    if (collision_step) h->pool_collision_step = collision_step;
+    if (refill) h->pool_refill = refill;
+    h->clear_graphs();   // captured launches carry the old values
     return QSG_OK;
 }
 

@@ -122,6 +122,8 @@ struct DevTally {
     int32_t balance_replicas;
     int32_t collision_batch;       // parked collisions that trigger a warp's collision step
     int32_t queue_chunk;           // consecutive particles a lane claims per work-queue atomic
+    int32_t pool_collision_step;   // pool kernel: parked collisions that make a collision step (1-32)
+    int32_t pool_refill;           // pool kernel: empty slots that trigger a refill from the queue (1-64)
     uint64_t max_segments;
 };
 

@@ -125,6 +125,16 @@ class _Driver:
         N.check(N.lib().qsg_run_cycles(self.tracker.handle, n_cycles, int(use_graph), _stream_ptr(stream)))
         self.cycles += n_cycles
 
+    def tune(self, block_size: int = 0, collision_batch: int = 0, queue_chunk: int = 0,
+             pool_collision_step: int = 0, pool_refill: int = 0) -> None:
+        """Kernel shape (0 keeps a value): threads per block; for the
+        one-history-per-lane kernel the collisions batched per warp step and the
+        particles claimed per queue atomic; for the pool kernel (default) the
+        pooled collisions that make a collision step and the empty slots that
+        trigger a refill."""
+        N.check(N.lib().qsg_set_tuning(self.tracker.handle, block_size, collision_batch, queue_chunk))
+        N.check(N.lib().qsg_set_pool_tuning(self.tracker.handle, pool_collision_step, pool_refill))
+
     def close(self):
         self.tracker.close()
 
@@ -194,5 +204,3 @@ class BatchMonteCarlo(_Driver):
             raise N.QsgError(N.QSG_ERR_DEVICE, f"device flags 0x{flags:x} raised during the run")
         return hist
 
-    def tune(self, block_size: int = 0, collision_batch: int = 0, queue_chunk: int = 0) -> None:
-        N.check(N.lib().qsg_set_tuning(self.tracker.handle, block_size, collision_batch, queue_chunk))

@@ -42,11 +42,12 @@ def test_batch_matches_each_problem_alone(gpu, use_graph):
     bmc.close()
 
 
-@pytest.mark.parametrize("block,batch,chunk,replicas", [(256, 8, 4, 2), (128, 24, 1, 1), (128, 1, 16, 3)])
-def test_tunings_do_not_change_results(gpu, block, batch, chunk, replicas):
+@pytest.mark.parametrize("block,batch,chunk,replicas,step,refill",
+                         [(256, 8, 4, 2, 24, 8), (128, 24, 1, 1, 1, 64), (128, 1, 16, 3, 32, 1)])
+def test_tunings_do_not_change_results(gpu, block, batch, chunk, replicas, step, refill):
     decks = [Deck.from_file(DECKS / f"{n}.inp") for n in BATCH]
     bmc = BatchMonteCarlo(decks, max_passes=64, flux_replicas=replicas)
-    bmc.tune(block, batch, chunk)
+    bmc.tune(block, batch, chunk, pool_collision_step=step, pool_refill=refill)
     check_against_golden(bmc.run(CYCLES, use_graph=True))
     bmc.close()
 
@@ -79,7 +80,7 @@ def test_sync_and_graph_cycles_interleave(gpu):
 def test_autotuner_returns_a_candidate(gpu, tmp_path):
     from quicksilver_gb300.autotune import autotune
     texts = [(DECKS / f"{n}.inp").read_text() for n in BATCH]
-    space = {"block_size": (128, 256), "collision_batch": (16,), "queue_chunk": (1, 4), "flux_replicas": (1,)}
+    space = {"block_size": (128, 256), "pool_collision_step": (32,), "pool_refill": (8, 16), "flux_replicas": (1,)}
     best = autotune(texts, scale=1.0, cycles=1, warmup=1, cache_path=tmp_path / "t.json", space=space)
     assert best["block_size"] in (128, 256) and best["segments_per_s"] > 0 and len(best["trials"]) == 4
     again = autotune(texts, cache_path=tmp_path / "t.json", space=space)   # cached
