@@ -590,9 +590,12 @@ def main():
         line["forms"] = {"batched": measure_batched(), "adjoint": measure_adjoint()}
     if not args.no_cpu_baseline:
         rate, seg, secs = cpu_port_rate(DECK, 2, os.cpu_count() or 1)
+        rate1, seg1, secs1 = cpu_port_rate(DECK, 1, 1)
         line["cpu_baseline"] = {"value": rate, "unit": "segments/s", "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"config2 cycles 0-1 ({seg} segments, {secs:.1f} s tracking) with "
-                                          f"{os.cpu_count()} OpenMP threads"}
+                                          f"{os.cpu_count()} OpenMP threads",
+                                "value_1_thread": rate1,
+                                "sample_1_thread": f"config2 cycle 0 ({seg1} segments, {secs1:.1f} s) on one core"}
     print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()
