@@ -49,6 +49,8 @@ def test_tuning_and_kernel_argument_errors(gpu):
         assert lib.qsg_set_tuning(h, 96, 0, 0) == N.QSG_ERR_INVALID
         assert lib.qsg_set_track_kernel(h, 2) == N.QSG_ERR_INVALID
         assert lib.qsg_set_observers(h, 8) == N.QSG_ERR_INVALID
+        assert lib.qsg_set_pool_tuning(h, 33, 0) == N.QSG_ERR_INVALID
+        assert lib.qsg_set_pool_tuning(h, 0, 65) == N.QSG_ERR_INVALID
         assert "flag" in N.last_error()
         with pytest.raises(N.QsgError):
             mc.fluence()            # observers are off
