@@ -55,7 +55,10 @@ enum {
     QSG_DEV_NEGATIVE_DISTANCE = 1u << 6,/* MC_Segment_Outcome.cc:265-276      */
     QSG_DEV_PASS_LIMIT = 1u << 7,       /* fission products left after max_passes */
     QSG_DEV_SCREEN_MISS = 1u << 8       /* verification build only: the FP32 facet
-                                           screen skipped a facet FP64 accepts */
+                                           screen skipped a facet FP64 accepts, or an
+                                           integer-pipe conversion or corrected-
+                                           reciprocal quotient differed from the
+                                           FP64 operation it replaces */
 };
 
 /* ---- enums shared with the reference ------------------------------------ */
@@ -369,6 +372,17 @@ int qsg_set_pool_tuning(QsgHandle* h, int32_t collision_step, int32_t refill);
 int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* particles, uint64_t n,
                                 QsgParticleSoA* census, uint64_t census_capacity, uint64_t* n_census,
                                 double* flux, uint64_t* balance, void* stream);
+
+/* No reference counterpart: a self-check of the library's replacements of
+ * FP64 operations in the tracking loop, which keep its results bit-identical
+ * while moving work off the FP64 pipe -- the double-to-float conversion of the
+ * facet screen, the corrected-reciprocal quotient of the mean-free-path
+ * update, and the bit-pattern comparisons -- against the FP64 operations
+ * themselves on `n` pseudo-random operands per kind (hard cases mixed in),
+ * drawn from `seed`, on CUDA device `device`.  mismatches[0..2] receive the
+ * disagreements of the conversion, the quotient and the comparisons (all
+ * zero on a correct build). */
+int qsg_check_arithmetic(int32_t device, uint64_t n, uint64_t seed, uint64_t* mismatches);
 
 /* Device pointers of the stores, for zero-copy callers (e.g. torch). */
 int qsg_processing_view(QsgHandle* h, QsgParticleSoA* device_view, uint64_t* n);

@@ -124,6 +124,7 @@ _SIGNATURES = {
     "qsg_abi_version": ([], C.c_int),
     "qsg_last_error": ([C.c_char_p, C.c_size_t], C.c_int),
     "qsg_device_count": ([C.POINTER(C.c_int)], C.c_int),
+    "qsg_check_arithmetic": ([C.c_int32, C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
     "qsg_create": ([C.POINTER(QsgProblem), C.POINTER(QsgOptions), C.POINTER(_VP)], C.c_int),
     "qsg_destroy": ([_VP], C.c_int),
     "qsg_set_particles": ([_VP, C.POINTER(QsgParticleSoA), C.c_uint64], C.c_int),
@@ -203,6 +204,15 @@ def device_count() -> int:
     n = C.c_int(0)
     check(lib().qsg_device_count(C.byref(n)))
     return n.value
+
+
+def check_arithmetic(n: int, seed: int = 1, device: int = 0) -> tuple:
+    """Disagreements (conversion, quotient, comparisons) of the tracking loop's
+    replacements of FP64 operations with those operations, on ``n`` random
+    operands per kind (qsg_check_arithmetic)."""
+    out = (C.c_uint64 * 3)()
+    check(lib().qsg_check_arithmetic(device, n, seed, out))
+    return tuple(int(v) for v in out)
 
 
 def soa_from_columns(cols: dict) -> QsgParticleSoA:

@@ -300,12 +300,25 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
     const uint8_t* proj = t.proj + (int64_t)cell * kFacets;
     const double* ctr = t.cell_center + 3 * (int64_t)cell;
     const double cx = __ldg(ctr + 0), cy = __ldg(ctr + 1), cz = __ldg(ctr + 2);
-    const float a32 = (float)p.alpha, b32 = (float)p.beta, g32 = (float)p.gamma;
+    // float copies for the screen, converted on the integer pipe (bounds as for (float))
+    const float a32 = f64_to_f32_rn(p.alpha), b32 = f64_to_f32_rn(p.beta), g32 = f64_to_f32_rn(p.gamma);
     const float slack = (float)t.abs_slack;
     int iteration = 0;
     double move_factor = 0.5 * kSmallDouble;
     for (;;) {
-        const float x32 = (float)(p.x - cx), y32 = (float)(p.y - cy), z32 = (float)(p.z - cz);
+        const float x32 = f64_to_f32_rn(p.x - cx), y32 = f64_to_f32_rn(p.y - cy), z32 = f64_to_f32_rn(p.z - cz);
+#ifdef QSG_VERIFY_SCREEN
+        {
+            // verification build: the integer-pipe conversions equal (float) in float's normal range
+            const double src[6] = {p.alpha, p.beta, p.gamma, p.x - cx, p.y - cy, p.z - cz};
+            const float got[6] = {a32, b32, g32, x32, y32, z32};
+            for (int k = 0; k < 6; k++) {
+                const float want = (float)src[k];
+                if (fabsf(want) >= 1.17549435e-38f && __float_as_uint(want) != __float_as_uint(got[k]))
+                    raise_flag(tally, QSG_DEV_SCREEN_MISS);
+            }
+        }
+#endif
         const float pos_max = fmaxf(fabsf(x32), fmaxf(fabsf(y32), fabsf(z32)));
         uint32_t exact = 0, accept = 0;
 #pragma unroll 1
@@ -403,11 +416,11 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
                     }
                     d = distance_to_segment(plane_tolerance, dot, ab.x, ab.y, cd.x, cd.y, q0, q1, q2, p);
                 }
-                if (d == kHugeDouble) {
+                if (f64_eq(d, kHugeDouble)) {
                     if (f > huge_f) huge_f = f;
-                } else if (d > 0.0) {
-                    if (d <= best) { best = d; best_f = f; }
-                } else if (d > neg) {
+                } else if (f64_gt0(d)) {
+                    if (f64_le(d, best)) { best = d; best_f = f; }
+                } else if (f64_lt(neg, d)) {
                     neg = d;
                     neg_f = f;
                 }
@@ -415,13 +428,14 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
         }
         // _hugeDouble is positive and larger than any finite distance, so it
         // only wins when no finite positive distance exists
-        if (best == 1e80 && huge_f >= 0) {
+        if (f64_eq(best, 1e80) && huge_f >= 0) {
             best = kHugeDouble;
             best_f = huge_f;
         }
-        if (best == kHugeDouble && neg != -kHugeDouble) { best = neg; best_f = neg_f; }
+        if (f64_eq(best, kHugeDouble) && !f64_eq(neg, -kHugeDouble)) { best = neg; best_f = neg_f; }
         bool retry = false;
-        if ((best == kHugeDouble && move_factor > 0) || (p.num_segments > 10000000 && best <= 0.0)) {
+        if ((f64_eq(best, kHugeDouble) && move_factor > 0) ||
+            (f64_lt(10000000.0, p.num_segments) && !f64_gt0(best))) {
             const double* c = t.cell_center + 3 * (int64_t)cell;
             p.x += move_factor * (__ldg(c + 0) - p.x);
             p.y += move_factor * (__ldg(c + 1) - p.y);
@@ -433,8 +447,8 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
             else retry = true;
         }
         if (!retry) {
-            if (best < 0) best = 0;
-            if (best >= kHugeDouble) raise_flag(tally, QSG_DEV_BAD_FACET);
+            if (f64_lt0(best)) best = 0;
+            if (!f64_lt(best, kHugeDouble)) raise_flag(tally, QSG_DEV_BAD_FACET);
             facet_out = best_f;
             return best;
         }
@@ -449,20 +463,20 @@ __device__ __forceinline__ int segment_outcome(const DevTables& t, const DevTall
 {
     double d_coll, d_facet, d_census;
     p.seg_len = 0.0;
-    if (p.speed < 0.0) p.speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
+    if (f64_lt0(p.speed)) p.speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
     const double speed = p.speed;
     bool force_collision = false;
-    if (p.num_mean_free_paths < 0.0) {
+    if (f64_lt0(p.num_mean_free_paths)) {
         force_collision = true;
         p.num_mean_free_paths = kSmallDouble;
     }
     const int key = cls * t.num_groups + p.group;
     if (key != p.xs_key) {
-        p.total_xs = __ldg(t.sigma_total + key);
         p.mean_free_path = __ldg(t.mfp_table + key);   // same bits as the reference's 1.0 / sigma
+        p.inv_mfp = __ldg(t.inv_mfp_table + key);
         p.xs_key = key;
     }
-    if (p.num_mean_free_paths == 0.0) {
+    if (f64_eq0(p.num_mean_free_paths)) {
         double r = rng_sample(p.seed);
         p.num_mean_free_paths = -1.0 * log(r);
     }
@@ -479,13 +493,20 @@ __device__ __forceinline__ int segment_outcome(const DevTables& t, const DevTall
     // MC_Find_Min (MC_Segment_Outcome.cc:232-248): strict <, ties keep the lower index
     int outcome = OUT_COLLISION;
     double seg = d_coll;
-    if (d_facet < seg) { seg = d_facet; outcome = OUT_FACET; }
-    if (d_census < seg) { seg = d_census; outcome = OUT_CENSUS; }
-    if (seg < 0) raise_flag(tally, QSG_DEV_NEGATIVE_DISTANCE);
+    if (f64_lt(d_facet, seg)) { seg = d_facet; outcome = OUT_FACET; }
+    if (f64_lt(d_census, seg)) { seg = d_census; outcome = OUT_CENSUS; }
+    if (f64_lt0(seg)) raise_flag(tally, QSG_DEV_NEGATIVE_DISTANCE);
     p.seg_len = seg;
     // a collision resets the mean free paths to 0 below: the reference's
-    // subtraction there is dead, so it is skipped (same bits)
-    if (outcome != OUT_COLLISION) p.num_mean_free_paths -= seg / p.mean_free_path;
+    // subtraction there is dead, so it is skipped (same bits); the division
+    // is div_rn's correctly rounded quotient (same bits)
+    if (outcome != OUT_COLLISION) {
+        const double q = div_rn(seg, p.mean_free_path, p.inv_mfp);
+#ifdef QSG_VERIFY_SCREEN
+        if (f64_bits(q) != f64_bits(seg / p.mean_free_path)) raise_flag(tally, QSG_DEV_SCREEN_MISS);
+#endif
+        p.num_mean_free_paths -= q;
+    }
     if (outcome == OUT_COLLISION) {
         p.last_event = QSG_EVENT_COLLISION;
         p.num_mean_free_paths = 0.0;
@@ -494,17 +515,17 @@ __device__ __forceinline__ int segment_outcome(const DevTables& t, const DevTall
         p.facet = facet;
     } else {
         p.last_event = QSG_EVENT_CENSUS;
-        p.time_to_census = (p.time_to_census < 0.0) ? p.time_to_census : 0.0;
+        p.time_to_census = f64_lt0(p.time_to_census) ? p.time_to_census : 0.0;
     }
     if (force_collision) p.num_mean_free_paths = 0.0;
-    if (seg == 0.0) return outcome;
+    if (f64_eq0(seg)) return outcome;
     p.x += (p.alpha * seg);
     p.y += (p.beta * seg);
     p.z += (p.gamma * seg);
     double seg_time = (seg / speed);
     p.time_to_census -= seg_time;
     p.age += seg_time;
-    if (p.time_to_census < 0.0) p.time_to_census = 0.0;
+    if (f64_lt0(p.time_to_census)) p.time_to_census = 0.0;
     atomicAdd(flux_row + (int64_t)p.cell * t.num_groups + p.group, seg * p.weight);
     return outcome;
 }
@@ -566,11 +587,11 @@ __device__ __forceinline__ int collision_select(const DevTables& t, const DevTal
     const int K = t.max_reactions;
     const int nk = __ldg(t.class_num_reactions + cls);
     const double* row = t.macro_xs + ((int64_t)cls * G + p.group) * K;
-    double current = p.total_xs * rng_sample(p.seed);
+    double current = __ldg(t.sigma_total + cls * G + p.group) * rng_sample(p.seed);
     int sel = -1;
     for (int k = 0; k < nk; k++) {
         current -= __ldg(row + k);
-        if (current < 0) { sel = k; break; }
+        if (f64_lt0(current)) { sel = k; break; }
     }
     if (sel < 0) {
         // the reference asserts and carries on with an invalid index
@@ -971,7 +992,7 @@ constexpr int kPoolD = 18, kPoolU = 2, kPoolI = 9;
 constexpr int kSlotBytes = kPoolD * 8 + kPoolU * 8 + kPoolI * 4;   // 196
 __host__ __device__ constexpr size_t pool_bytes_per_warp(int pool) { return (size_t)kSlotBytes * pool; }
 enum { PD_X, PD_Y, PD_Z, PD_VX, PD_VY, PD_VZ, PD_A, PD_B, PD_G, PD_E, PD_W, PD_TTC, PD_AGE, PD_NMFP, PD_NSEG,
-       PD_SPEED, PD_SIG, PD_MFP };
+       PD_SPEED, PD_IMFP, PD_MFP };
 // PI_PACK = facet | flux replica << 8 | group << 16
 enum { PI_LAST, PI_NCOLL, PI_BREED, PI_SPECIES, PI_DOMAIN, PI_CELL, PI_PACK, PI_KEY, PI_SEGS };
 
@@ -1015,7 +1036,7 @@ __device__ __forceinline__ void pool_get(const PoolView& v, int s, const DevTall
     p.kinetic_energy = d[PD_E * POOL]; p.weight = d[PD_W * POOL];
     p.time_to_census = d[PD_TTC * POOL]; p.age = d[PD_AGE * POOL];
     p.num_mean_free_paths = d[PD_NMFP * POOL]; p.num_segments = d[PD_NSEG * POOL];
-    p.speed = d[PD_SPEED * POOL]; p.total_xs = d[PD_SIG * POOL]; p.mean_free_path = d[PD_MFP * POOL];
+    p.speed = d[PD_SPEED * POOL]; p.inv_mfp = d[PD_IMFP * POOL]; p.mean_free_path = d[PD_MFP * POOL];
     p.seed = v.u[s]; p.identifier = v.u[POOL + s];
     const int32_t* i = v.i + s;
     p.last_event = i[PI_LAST * POOL]; p.num_collisions = i[PI_NCOLL * POOL]; p.breed = i[PI_BREED * POOL];
@@ -1039,7 +1060,7 @@ __device__ __forceinline__ void pool_put(const PoolView& v, int s, const Particl
     d[PD_E * POOL] = p.kinetic_energy; d[PD_W * POOL] = p.weight;
     d[PD_TTC * POOL] = p.time_to_census; d[PD_AGE * POOL] = p.age;
     d[PD_NMFP * POOL] = p.num_mean_free_paths; d[PD_NSEG * POOL] = p.num_segments;
-    d[PD_SPEED * POOL] = p.speed; d[PD_SIG * POOL] = p.total_xs; d[PD_MFP * POOL] = p.mean_free_path;
+    d[PD_SPEED * POOL] = p.speed; d[PD_IMFP * POOL] = p.inv_mfp; d[PD_MFP * POOL] = p.mean_free_path;
     v.u[s] = p.seed; v.u[POOL + s] = p.identifier;
     int32_t* i = v.i + s;
     i[PI_LAST * POOL] = p.last_event; i[PI_NCOLL * POOL] = p.num_collisions; i[PI_BREED * POOL] = p.breed;
@@ -1567,7 +1588,9 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
     // division whose bits the host reproduces
     std::vector<double> mfp(sigma_total.size());
     for (size_t k = 0; k < mfp.size(); k++) mfp[k] = (sigma_total[k] == 0.0) ? kHugeDouble : 1.0 / sigma_total[k];
-    if ((st = h->mfp_table.upload(mfp))) return st;
+    std::vector<double> inv_mfp(mfp.size());
+    for (size_t k = 0; k < mfp.size(); k++) inv_mfp[k] = 1.0 / mfp[k];   // IEEE division: RN(1 / mfp)
+    if ((st = h->mfp_table.upload(mfp)) || (st = h->inv_mfp_table.upload(inv_mfp))) return st;
     if ((st = h->energies.upload(energies)) || (st = h->sigma_total.upload(sigma_total)) ||
         (st = h->macro_xs.upload(macro)) || (st = h->class_nubar.upload(nubar)) ||
         (st = h->material_mass.upload(mass)) || (st = h->cell_nodes.upload(nodes)) ||
@@ -1589,6 +1612,7 @@ int upload_tables(QsgHandle* h, const QsgProblem* p)
     t.energies = h->energies.ptr;
     t.sigma_total = h->sigma_total.ptr;
     t.mfp_table = h->mfp_table.ptr;
+    t.inv_mfp_table = h->inv_mfp_table.ptr;
     // group hint: accepted when every edge but the last lies within a quarter
     // group of the log-linear fit through the first two
     t.group_hint_ln0 = 0.0f;
@@ -1939,7 +1963,7 @@ extern "C" int qsg_destroy(QsgHandle* h)
 {
     if (!h) return QSG_OK;
     cudaSetDevice(h->device);
-    h->energies.free(); h->sigma_total.free(); h->mfp_table.free(); h->macro_xs.free(); h->class_nubar.free();
+    h->energies.free(); h->sigma_total.free(); h->mfp_table.free(); h->inv_mfp_table.free(); h->macro_xs.free(); h->class_nubar.free();
     h->material_mass.free(); h->cell_nodes.free(); h->cell_center.free(); h->planes.free();
     h->class_num_reactions.free(); h->class_material.free(); h->cell_class.free(); h->adj_cell.free();
     h->class_type.free(); h->adj_facet_event.free();
@@ -2342,6 +2366,130 @@ extern "C" int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* p
     }
     QSG_CUDA(cudaStreamSynchronize(s));
     *n_census = counts[1];
+    return QSG_OK;
+    QSG_API_END
+}
+
+// ------------------------------------------------------------------------
+// Self-check of the tracking loop's replacements of FP64 operations
+// (f64_to_f32_rn, div_rn, the bit-pattern comparisons) against the FP64
+// operations themselves, on pseudo-random operands with hard cases mixed in.
+
+namespace qsg {
+namespace {
+
+// splitmix64's output function (Steele, Lea and Flood, OOPSLA 2014)
+__device__ __forceinline__ uint64_t mix64(uint64_t z)
+{
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double f64_make(uint64_t sign, int biased_exp, uint64_t mantissa)
+{
+    return __longlong_as_double((long long)((sign << 63) | ((uint64_t)biased_exp << 52) |
+                                            (mantissa & 0xfffffffffffffull)));
+}
+
+// one operand of the comparison check: zeros of both signs, tiny, ordinary
+// and huge magnitudes of both signs, or the other operand itself
+__device__ __forceinline__ double cmp_operand(uint64_t r, double other)
+{
+    const uint64_t s = r & 1;
+    switch ((r >> 1) & 7) {
+    case 0: return 0.0;
+    case 1: return -0.0;
+    case 2: return f64_make(s, 1 + (int)((r >> 8) % 40u), r >> 12);          // near the smallest normals
+    case 3: return s ? -kHugeDouble : kHugeDouble;
+    case 4: return other;
+    case 5: return f64_make(s, 1 + (int)((r >> 8) % 2046u), r >> 12);        // any normal magnitude
+    default: return f64_make(s, 1013 + (int)((r >> 8) % 20u), r >> 12);     // near 1
+    }
+}
+
+__global__ void check_arith_kernel(uint64_t n, uint64_t seed, unsigned long long* bad)
+{
+    unsigned long long nbad[3] = {0, 0, 0};
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint64_t r[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) r[k] = mix64(seed ^ mix64(6 * i + k));
+        {
+            // double -> float: |x| from 2^-140 to 2^100, with round-half,
+            // just-below/above-half and carry-into-the-exponent mantissas
+            uint64_t mant = r[0];
+            switch ((r[1] >> 60) & 7) {
+            case 0: mant = (mant & ~0x1fffffffull) | 0x10000000ull; break;
+            case 1: mant = (mant & ~0x1fffffffull) | 0x0fffffffull; break;
+            case 2: mant = (mant & ~0x1fffffffull) | 0x10000001ull; break;
+            case 3: mant = (mant & ~0x1fffffffull) | 0x30000000ull; break;
+            case 4: mant = ~0ull; break;
+            default: break;
+            }
+            const double x = f64_make(r[1] & 1, 1023 - 140 + (int)((r[1] >> 8) % 240u), mant);
+            const float want = (float)x, got = f64_to_f32_rn(x);
+            const bool ok = (fabsf(want) >= 1.17549435e-38f)
+                                ? __float_as_uint(got) == __float_as_uint(want)
+                                : __float_as_uint(got) == (__float_as_uint(want) & 0x80000000u);
+            nbad[0] += ok ? 0 : 1;
+        }
+        {
+            // a / b with y = RN(1 / b): a from 2^-60 to 2^40 (or 0), b from
+            // 2^-40 to 2^260, powers of two and all-ones mantissas included
+            uint64_t mb = r[3];
+            if (((r[2] >> 56) & 7) == 0) mb = 0;
+            if (((r[2] >> 56) & 7) == 1) mb = ~0ull;
+            const double b = f64_make(0, 1023 - 40 + (int)((r[2] >> 8) % 301u), mb);
+            double a = f64_make(0, 1023 - 60 + (int)((r[2] >> 24) % 101u), r[4]);
+            if (((r[2] >> 59) & 7) == 0) a = 0.0;
+            if (((r[2] >> 59) & 7) == 1) a = b * (double)(1 + (r[4] & 1023));
+            const double y = 1.0 / b;
+            const double got = div_rn(a, b, y), want = a / b;
+            nbad[1] += (f64_bits(got) == f64_bits(want)) ? 0 : 1;
+        }
+        {
+            const double a = cmp_operand(r[5], 1.0);
+            const double b = cmp_operand(r[5] >> 32, a);
+            bool ok = (f64_lt(a, b) == (a < b)) && (f64_le(a, b) == (a <= b)) && (f64_gt0(a) == (a > 0.0)) &&
+                      (f64_lt0(a) == (a < 0.0)) && (f64_eq0(a) == (a == 0.0));
+            if (!(b == 0.0)) ok = ok && (f64_eq(a, b) == (a == b));
+            nbad[2] += ok ? 0 : 1;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+        if (nbad[k]) atomicAdd(bad + k, nbad[k]);
+}
+
+}  // namespace
+}  // namespace qsg
+
+extern "C" int qsg_check_arithmetic(int32_t device, uint64_t n, uint64_t seed, uint64_t* mismatches)
+{
+    QSG_API_BEGIN
+    if (!mismatches) return fail(QSG_ERR_INVALID, "qsg_check_arithmetic: null argument");
+    int ndev = 0;
+    qsg_device_count(&ndev);
+    if (ndev == 0) return fail(QSG_ERR_NO_DEVICE, "qsg_check_arithmetic: no CUDA device visible");
+    if (device < 0 || device >= ndev)
+        return fail(QSG_ERR_INVALID, "qsg_check_arithmetic: device %d of %d", (int)device, ndev);
+    QSG_CUDA(cudaSetDevice(device));
+    qsg::DevBuf<unsigned long long> bad;
+    int st = bad.alloc(3);
+    if (st) return st;
+    unsigned long long host[3] = {0, 0, 0};
+    cudaError_t e = cudaMemset(bad.ptr, 0, 3 * sizeof(unsigned long long));
+    if (e == cudaSuccess && n > 0) {
+        qsg::check_arith_kernel<<<4 * 152, 256>>>(n, seed, bad.ptr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(host, bad.ptr, sizeof(host), cudaMemcpyDeviceToHost);
+    bad.free();
+    if (e != cudaSuccess) return fail(QSG_ERR_CUDA, "qsg_check_arithmetic: %s", cudaGetErrorString(e));
+    for (int k = 0; k < 3; k++) mismatches[k] = host[k];
     return QSG_OK;
     QSG_API_END
 }

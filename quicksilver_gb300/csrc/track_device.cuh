@@ -82,6 +82,7 @@ struct DevTables {
     const double* energies;        // [G+1]
     const double* sigma_total;     // [classes][G]  weightedMacroscopicCrossSection values
     const double* mfp_table;       // [classes][G]  1/Sigma_t, or _hugeDouble when Sigma_t = 0 (MC_Segment_Outcome.cc:129-131)
+    const double* inv_mfp_table;   // [classes][G]  RN(1 / mfp_table), for div_rn
     // energy-group hint for log-spaced grids: group ~ (ln E - ln E_0) * scale
     // (scale = 0: no hint); the exact search below confirms it
     float group_hint_ln0, group_hint_scale;
@@ -145,6 +146,60 @@ __device__ __forceinline__ uint64_t append_slot(const DevStore& s)
     if (g.thread_rank() == 0) base = atomicAdd(s.count, (unsigned long long)g.size());
     base = g.shfl(base, 0);
     return base + g.thread_rank();
+}
+
+// IEEE 754 comparisons of doubles evaluated on their bit patterns, for
+// operands that are never NaN.  They answer as the FP64 comparisons do (-0.0
+// equals +0.0) but run on the integer pipe: the tracking loop keeps the FP64
+// pipe busy, where a comparison costs as much as a multiply.
+__device__ __forceinline__ long long f64_bits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ bool f64_gt0(double x) { return f64_bits(x) > 0; }    // x > 0.0
+__device__ __forceinline__ bool f64_lt0(double x)                                // x < 0.0
+{
+    return (unsigned long long)f64_bits(x) > 0x8000000000000000ull;
+}
+__device__ __forceinline__ bool f64_eq0(double x) { return ((unsigned long long)f64_bits(x) << 1) == 0; }
+// x == c for a nonzero c
+__device__ __forceinline__ bool f64_eq(double x, double c) { return f64_bits(x) == f64_bits(c); }
+// a key whose signed order is the IEEE order (-0.0 and +0.0 share key 0)
+__device__ __forceinline__ long long f64_key(double x)
+{
+    const long long b = f64_bits(x);
+    return b >= 0 ? b : (long long)(0x8000000000000000ull - (unsigned long long)b);
+}
+__device__ __forceinline__ bool f64_lt(double a, double b) { return f64_key(a) < f64_key(b); }
+__device__ __forceinline__ bool f64_le(double a, double b) { return f64_key(a) <= f64_key(b); }
+
+// double -> float rounded to nearest even on the integer pipe: the 29
+// dropped mantissa bits are rounded into the kept ones by one 64-bit add
+// (a carry may step the exponent, as rounding does), then the exponent is
+// rebiased from 1023 to 127 and the fields shifted into place.  The same
+// value as (float)x for every x whose rounded magnitude is at least 2^-126
+// and below 2^128; smaller magnitudes give a zero of x's sign (an error
+// below 2^-126).
+__device__ __forceinline__ float f64_to_f32_rn(double x)
+{
+    unsigned long long b = (unsigned long long)f64_bits(x);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    b += 0x0fffffffull + ((b >> 29) & 1ull);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned f = __funnelshift_l(lo, hi - 0x38000000u, 3);
+    return __uint_as_float(((hi & 0x7fffffffu) < 0x38100000u) ? sign : (f | sign));
+}
+
+// a / b correctly rounded (round to nearest), given y = RN(1 / b): Markstein's
+// correction (P. Markstein, IBM J. Res. Dev. 34(1), 1990; Muller et al.,
+// Handbook of Floating-Point Arithmetic, the theorem on division with a
+// correctly rounded reciprocal).  q0 = RN(a y) is within 1.5 ulp of a/b; one
+// correction makes q1 faithful; for a faithful q1 and a reciprocal with
+// relative error below 2^-53, RN(q1 + (a - b q1) y) equals RN(a / b).  Three
+// FP64 multiply-adds and one multiply instead of a division, for normal
+// operands whose residuals do not underflow (a = 0 gives +0 as a / b does).
+__device__ __forceinline__ double div_rn(double a, double b, double y)
+{
+    const double q0 = a * y;
+    const double q1 = fma(fma(-q0, b, a), y, q0);
+    return fma(fma(-q1, b, a), y, q1);
 }
 
 // MC_RNG_State.hh:22-33
@@ -212,12 +267,13 @@ struct Particle {
     double x, y, z, vx, vy, vz;
     double alpha, beta, gamma;
     double kinetic_energy, weight, time_to_census, age;
-    double num_mean_free_paths, num_segments, total_xs, mean_free_path;
+    double num_mean_free_paths, num_segments, inv_mfp, mean_free_path;
     uint64_t seed, identifier;
     int32_t last_event, num_collisions, breed, species, domain, cell, facet, group;
     // caches of values the reference recomputes every segment from unchanged
     // inputs (same bits): |velocity| until the velocity changes, and
-    // 1/Sigma_t for the (cross-section class, group) key it was computed for
+    // 1/Sigma_t for the (cross-section class, group) key it was computed for;
+    // inv_mfp = RN(1 / mean_free_path) for the mean-free-path update
     double speed;                  // < 0: stale
     int32_t xs_key;                // -1: stale
     double seg_len;                // length of the last segment (MC_Particle::segment_path_length)
@@ -245,7 +301,7 @@ __device__ __forceinline__ void load_particle(const DevTables& t, const DevStore
     p.domain = s.domain[i];
     p.cell = s.cell[i];
     p.facet = 0;
-    p.total_xs = 0.0;
+    p.inv_mfp = 0.0;
     p.mean_free_path = 0.0;
     p.xs_key = -1;
     // direction from velocity (MC_Base_Particle.hh:317-325)

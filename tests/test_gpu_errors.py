@@ -46,12 +46,14 @@ def test_tuning_and_kernel_argument_errors(gpu):
     mc = _mc()
     try:
         lib, h = N.lib(), mc.tracker.handle
-        assert lib.qsg_set_tuning(h, 96, 0, 0) == N.QSG_ERR_INVALID
-        assert lib.qsg_set_track_kernel(h, 2) == N.QSG_ERR_INVALID
-        assert lib.qsg_set_observers(h, 8) == N.QSG_ERR_INVALID
-        assert lib.qsg_set_pool_tuning(h, 33, 0) == N.QSG_ERR_INVALID
-        assert lib.qsg_set_pool_tuning(h, 0, 65) == N.QSG_ERR_INVALID
-        assert "flag" in N.last_error()
+        calls = [(lib.qsg_set_tuning, (96, 0, 0), "block size"),
+                 (lib.qsg_set_track_kernel, (2,), "kind"),
+                 (lib.qsg_set_observers, (8,), "flag"),
+                 (lib.qsg_set_pool_tuning, (33, 0), "collision step"),
+                 (lib.qsg_set_pool_tuning, (0, 65), "refill")]
+        for fn, args, words in calls:
+            assert fn(h, *args) == N.QSG_ERR_INVALID
+            assert words in N.last_error()
         with pytest.raises(N.QsgError):
             mc.fluence()            # observers are off
         assert mc.run(1).segments() > 0
