@@ -377,11 +377,12 @@ int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* particles, u
  * FP64 operations in the tracking loop, which keep its results bit-identical
  * while moving work off the FP64 pipe -- the double-to-float conversion of the
  * facet screen, the corrected-reciprocal quotient of the mean-free-path
- * update, and the bit-pattern comparisons -- against the FP64 operations
- * themselves on `n` pseudo-random operands per kind (hard cases mixed in),
- * drawn from `seed`, on CUDA device `device`.  mismatches[0..2] receive the
- * disagreements of the conversion, the quotient and the comparisons (all
- * zero on a correct build). */
+ * update, the bit-pattern comparisons and the random-number sample's
+ * integer-to-double conversion -- against the FP64 operations themselves on
+ * `n` pseudo-random operands per kind (hard cases mixed in), drawn from
+ * `seed`, on CUDA device `device`.  mismatches[0..3] receive the disagreements
+ * of the conversion, the quotient, the comparisons and the sample (all zero
+ * on a correct build). */
 int qsg_check_arithmetic(int32_t device, uint64_t n, uint64_t seed, uint64_t* mismatches);
 
 /* Device pointers of the stores, for zero-copy callers (e.g. torch). */

@@ -207,10 +207,10 @@ def device_count() -> int:
 
 
 def check_arithmetic(n: int, seed: int = 1, device: int = 0) -> tuple:
-    """Disagreements (conversion, quotient, comparisons) of the tracking loop's
-    replacements of FP64 operations with those operations, on ``n`` random
-    operands per kind (qsg_check_arithmetic)."""
-    out = (C.c_uint64 * 3)()
+    """Disagreements (conversion, quotient, comparisons, random-number sample)
+    of the tracking loop's replacements of FP64 operations with those
+    operations, on ``n`` random operands per kind (qsg_check_arithmetic)."""
+    out = (C.c_uint64 * 4)()
     check(lib().qsg_check_arithmetic(device, n, seed, out))
     return tuple(int(v) for v in out)
 

@@ -377,9 +377,6 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
         }
 #endif
         if (exact) {
-            // (1e-8 * |r|)^2 of MCT.cc:569-571; only the full test uses it
-            const double plane_tolerance =
-                (exact & ~accept) ? 1e-16 * (p.x * p.x + p.y * p.y + p.z * p.z) : 0.0;
             uint32_t m = exact;
             while (m) {
                 const int f = __ffs(m) - 1;
@@ -398,6 +395,7 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
                         q1[k] = nodes[3 * kFacetLocal[f][1] + k];
                         q2[k] = nodes[3 * kFacetLocal[f][2] + k];
                     }
+                    const double plane_tolerance = 1e-16 * (p.x * p.x + p.y * p.y + p.z * p.z);
                     const double full = (dot > 0.0) ? distance_to_segment(plane_tolerance, dot, ab.x, ab.y, cd.x, cd.y,
                                                                           q0, q1, q2, p)
                                                     : kHugeDouble;
@@ -414,6 +412,8 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
                         q1[k] = __ldg(n1 + k);
                         q2[k] = __ldg(n2 + k);
                     }
+                    // (1e-8 * |r|)^2 of MCT.cc:569-571, which only the full test uses
+                    const double plane_tolerance = 1e-16 * (p.x * p.x + p.y * p.y + p.z * p.z);
                     d = distance_to_segment(plane_tolerance, dot, ab.x, ab.y, cd.x, cd.y, q0, q1, q2, p);
                 }
                 if (f64_eq(d, kHugeDouble)) {
@@ -978,7 +978,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
 // still follows its own history with its own random stream, in the
 // reference's order, so the results are those of the lane-resident kernel.
 //
-// Pool sizes: 96 particles per warp for the plain kernel; with K sensitivity
+// Pool sizes: 64 particles per warp for the plain kernel; with K sensitivity
 // scores per particle, 64, 48 or 32, the largest that still leaves room for
 // three 4-warp blocks per SM (pool_for_scores).
 #ifndef QSG_POOL
@@ -2372,8 +2372,9 @@ extern "C" int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* p
 
 // ------------------------------------------------------------------------
 // Self-check of the tracking loop's replacements of FP64 operations
-// (f64_to_f32_rn, div_rn, the bit-pattern comparisons) against the FP64
-// operations themselves, on pseudo-random operands with hard cases mixed in.
+// (f64_to_f32_rn, div_rn, the bit-pattern comparisons, u64_scaled_2m64)
+// against the FP64 operations themselves, on pseudo-random operands with hard
+// cases mixed in.
 
 namespace qsg {
 namespace {
@@ -2411,12 +2412,12 @@ __device__ __forceinline__ double cmp_operand(uint64_t r, double other)
 
 __global__ void check_arith_kernel(uint64_t n, uint64_t seed, unsigned long long* bad)
 {
-    unsigned long long nbad[3] = {0, 0, 0};
+    unsigned long long nbad[4] = {0, 0, 0, 0};
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
-        uint64_t r[6];
+        uint64_t r[8];
 #pragma unroll
-        for (int k = 0; k < 6; k++) r[k] = mix64(seed ^ mix64(6 * i + k));
+        for (int k = 0; k < 8; k++) r[k] = mix64(seed ^ mix64(8 * i + k));
         {
             // double -> float: |x| from 2^-140 to 2^100, with round-half,
             // just-below/above-half and carry-into-the-exponent mantissas
@@ -2458,9 +2459,26 @@ __global__ void check_arith_kernel(uint64_t n, uint64_t seed, unsigned long long
             if (!(b == 0.0)) ok = ok && (f64_eq(a, b) == (a == b));
             nbad[2] += ok ? 0 : 1;
         }
+        {
+            // the random-number sample 2^-64 (double)x: any x, small x, powers
+            // of two, round-half patterns of the 11 dropped bits, all ones, 0
+            uint64_t x = r[6];
+            switch ((r[7] >> 60) & 7) {
+            case 0: x >>= (r[7] & 63); break;
+            case 1: x = 1ull << (r[7] & 63); break;
+            case 2: x = (x & ~0x7ffull) | 0x400ull; break;
+            case 3: x = (x & ~0xfffull) | 0xc00ull; break;
+            case 4: x = ~0ull; break;
+            case 5: x = (x & ~0x7ffull) | 0x3ffull; break;
+            case 6: x = 0; break;
+            default: break;
+            }
+            const double want = 5.4210108624275222e-20 * __ull2double_rn(x);
+            nbad[3] += (f64_bits(u64_scaled_2m64(x)) == f64_bits(want)) ? 0 : 1;
+        }
     }
 #pragma unroll
-    for (int k = 0; k < 3; k++)
+    for (int k = 0; k < 4; k++)
         if (nbad[k]) atomicAdd(bad + k, nbad[k]);
 }
 
@@ -2478,10 +2496,10 @@ extern "C" int qsg_check_arithmetic(int32_t device, uint64_t n, uint64_t seed, u
         return fail(QSG_ERR_INVALID, "qsg_check_arithmetic: device %d of %d", (int)device, ndev);
     QSG_CUDA(cudaSetDevice(device));
     qsg::DevBuf<unsigned long long> bad;
-    int st = bad.alloc(3);
+    int st = bad.alloc(4);
     if (st) return st;
-    unsigned long long host[3] = {0, 0, 0};
-    cudaError_t e = cudaMemset(bad.ptr, 0, 3 * sizeof(unsigned long long));
+    unsigned long long host[4] = {0, 0, 0, 0};
+    cudaError_t e = cudaMemset(bad.ptr, 0, 4 * sizeof(unsigned long long));
     if (e == cudaSuccess && n > 0) {
         qsg::check_arith_kernel<<<4 * 152, 256>>>(n, seed, bad.ptr);
         e = cudaGetLastError();
@@ -2489,7 +2507,7 @@ extern "C" int qsg_check_arithmetic(int32_t device, uint64_t n, uint64_t seed, u
     if (e == cudaSuccess) e = cudaMemcpy(host, bad.ptr, sizeof(host), cudaMemcpyDeviceToHost);
     bad.free();
     if (e != cudaSuccess) return fail(QSG_ERR_CUDA, "qsg_check_arithmetic: %s", cudaGetErrorString(e));
-    for (int k = 0; k < 3; k++) mismatches[k] = host[k];
+    for (int k = 0; k < 4; k++) mismatches[k] = host[k];
     return QSG_OK;
     QSG_API_END
 }

@@ -202,11 +202,27 @@ __device__ __forceinline__ double div_rn(double a, double b, double y)
     return fma(fma(-q1, b, a), y, q1);
 }
 
-// MC_RNG_State.hh:22-33
+// 2^-64 * (double)x with the conversion rounded to nearest even, assembled on
+// the integer pipe: the leading bit is found, the 64 - 53 = 11 low bits are
+// rounded into the kept ones (a carry steps the exponent, as rounding does),
+// and the 2^-64 scale goes into the exponent (exact: no result is subnormal).
+__device__ __forceinline__ double u64_scaled_2m64(uint64_t x)
+{
+    if (x == 0) return 0.0;
+    const int lz = __clzll((long long)x);
+    const uint64_t m = x << lz;   // leading 1 at bit 63
+    const uint64_t round_up = (m >> 10) & 1ull & ((uint64_t)((m & 0x3ffull) != 0) | (m >> 11));
+    const uint64_t r = (m >> 11) + round_up;   // 2^52 <= r <= 2^53
+    return __longlong_as_double((long long)(((uint64_t)(1022 - lz) << 52) + r - (1ull << 52)));
+}
+
+// MC_RNG_State.hh:22-33.  The reference's 5.4210108624275222e-20 is 2^-64
+// exactly, so the sample is u64_scaled_2m64 of the new seed (same bits).
+static_assert(5.4210108624275222e-20 == 0x1p-64, "the sample scale is 2^-64");
 __device__ __forceinline__ double rng_sample(uint64_t& seed)
 {
     seed = 2862933555777941757ULL * seed + 3037000493ULL;
-    return 5.4210108624275222e-20 * __ull2double_rn(seed);
+    return u64_scaled_2m64(seed);
 }
 
 // Numerical Recipes psdes (2 rounds) as MC_RNG_State.cc:29-52, used by
@@ -244,7 +260,7 @@ __device__ __forceinline__ int energy_group(const DevTables& t, double e)
     // On a log-spaced grid a float estimate lands within a group of it; two
     // exact comparisons on each side confirm it, else the search runs.
     if (t.group_hint_scale > 0.0f) {
-        int g = (int)((__logf((float)e) - t.group_hint_ln0) * t.group_hint_scale);
+        int g = (int)((__logf(f64_to_f32_rn(e)) - t.group_hint_ln0) * t.group_hint_scale);
         g = max(0, min(g, n - 2));
         if (__ldg(en + g) <= e) {
             if (g + 1 > n - 2 || e < __ldg(en + g + 1)) return g;
