@@ -385,6 +385,26 @@ int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* particles, u
  * on a correct build). */
 int qsg_check_arithmetic(int32_t device, uint64_t n, uint64_t seed, uint64_t* mismatches);
 
+/* Tracks particles that live in the caller's page-locked host arrays
+ * (cudaHostAlloc / cudaHostRegister; device arrays work too) without staging
+ * copies: the tracking launch reads each particle from `particles` (n of them)
+ * and appends each census particle to `census` (room for census_capacity;
+ * *n_census receives the count) over the host link while it tracks, so the
+ * transfers overlap the tracking.  The replacement, for a host whose vaults
+ * live in host memory, of qsg_set_particles + qsg_track_cycle + qsg_get_census
+ * (the processing-vault hand-off and census collection around
+ * CycleTrackingKernel, main.cc:166-197), with the same results.  Fission
+ * products between passes stay in the handle's device stores, whose contents
+ * afterwards are unspecified; tallies accumulate in the handle
+ * (qsg_read_tallies).  Pageable arrays are rejected (QSG_ERR_INVALID), as is a
+ * handle with sensitivities on (QSG_ERR_UNSUPPORTED: scores do not travel
+ * through host arrays).  More census particles than census_capacity: the
+ * arrays hold the first census_capacity, the call returns QSG_ERR_CAPACITY
+ * with the full count in *n_census.  Returns when the work on `stream` has
+ * finished. */
+int qsg_track_host(QsgHandle* h, const QsgParticleSoA* particles, uint64_t n, QsgParticleSoA* census,
+                   uint64_t census_capacity, uint64_t* n_census, void* stream);
+
 /* Device pointers of the stores, for zero-copy callers (e.g. torch). */
 int qsg_processing_view(QsgHandle* h, QsgParticleSoA* device_view, uint64_t* n);
 int qsg_processed_view(QsgHandle* h, QsgParticleSoA* device_view, uint64_t* n);

@@ -179,7 +179,9 @@ struct CycleScalars {
     unsigned long long cycle;         // cycles finalised so far (history row)
     unsigned long long source_calls;  // cycle inits so far
     unsigned long long source_round;  // index of the running cycle init (source seeds)
-    unsigned long long pad[3];
+    unsigned long long host_in_count;      // qsg_track_host: particles in the caller's input arrays
+    unsigned long long host_census_count;  // qsg_track_host: census particles appended to the caller's arrays
+    unsigned long long pad;
 };
 
 // Per-cycle record written by the finalize kernel (device-resident history).

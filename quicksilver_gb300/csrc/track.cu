@@ -1357,26 +1357,32 @@ const void* pool_kernel_fn(bool sens, int pool)
     return (const void*)track_pool_kernel<B, true, 32>;
 }
 
+// The stores of one tracking pass: input, census, fission products.
+struct PassStores {
+    DevStore in, census, extra;
+};
+
 template <int B, bool SENS, int POOL>
 void launch_pool_t(QsgHandle* h, int grid, size_t smem, cudaStream_t s, const DevTally& tv,
-                   unsigned long long* cursor)
+                   unsigned long long* cursor, const PassStores& ps)
 {
-    track_pool_kernel<B, SENS, POOL><<<grid, B, smem, s>>>(h->tables, tv, h->processing.view, h->processed.view,
-                                                           h->extra.view, cursor, SENS ? h->sens : DevSens{});
+    track_pool_kernel<B, SENS, POOL><<<grid, B, smem, s>>>(h->tables, tv, ps.in, ps.census, ps.extra, cursor,
+                                                           SENS ? h->sens : DevSens{});
 }
 
 template <int B>
-void launch_pool(QsgHandle* h, cudaStream_t s, const DevTally& tv, unsigned long long* cursor)
+void launch_pool(QsgHandle* h, cudaStream_t s, const DevTally& tv, unsigned long long* cursor, const PassStores& ps)
 {
     if (h->sens.K == 0) {
         launch_pool_t<B, false, kPoolPlain>(h, h->pool_blocks,
-                                            track_pool_smem_bytes(B, h->num_problems, 0, kPoolPlain), s, tv, cursor);
+                                            track_pool_smem_bytes(B, h->num_problems, 0, kPoolPlain), s, tv, cursor,
+                                            ps);
         return;
     }
     const size_t smem = track_pool_smem_bytes(B, h->num_problems, h->sens.K, h->pool_sens);
-    if (h->pool_sens == 64) launch_pool_t<B, true, 64>(h, h->pool_sens_blocks, smem, s, tv, cursor);
-    else if (h->pool_sens == 48) launch_pool_t<B, true, 48>(h, h->pool_sens_blocks, smem, s, tv, cursor);
-    else launch_pool_t<B, true, 32>(h, h->pool_sens_blocks, smem, s, tv, cursor);
+    if (h->pool_sens == 64) launch_pool_t<B, true, 64>(h, h->pool_sens_blocks, smem, s, tv, cursor, ps);
+    else if (h->pool_sens == 48) launch_pool_t<B, true, 48>(h, h->pool_sens_blocks, smem, s, tv, cursor, ps);
+    else launch_pool_t<B, true, 32>(h, h->pool_sens_blocks, smem, s, tv, cursor, ps);
 }
 
 // Persistent grid for the current block size: SMs x resident blocks.
@@ -1730,39 +1736,45 @@ int copy_soa(const DevStore& d, const QsgParticleSoA* h, uint64_t n, bool to_dev
 
 namespace {
 
-// One tracking pass: processing store -> census + fission products (extra).
-// The pass's particle count is read by the kernel from the store's device
-// counter, so nothing here waits for the device.
-int launch_pass(QsgHandle* h, cudaStream_t s)
+// One tracking pass over explicit stores: input -> census + fission
+// products.  The pass's particle count is read by the kernel from the input's
+// device counter, so nothing here waits for the device.
+int launch_pass_stores(QsgHandle* h, cudaStream_t s, const PassStores& ps)
 {
     unsigned long long* cursor = &h->scalars.ptr->cursor;
-    QSG_CUDA(cudaMemsetAsync(h->extra.count, 0, sizeof(unsigned long long), s));
+    QSG_CUDA(cudaMemsetAsync(ps.extra.count, 0, sizeof(unsigned long long), s));
     QSG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s));
     const DevTally tv = tally_view(h);
     if (h->kernel_kind == 1 && pool_kernel_usable(h)) {
-        if (h->block_size == 256) launch_pool<256>(h, s, tv, cursor);
-        else launch_pool<128>(h, s, tv, cursor);
+        if (h->block_size == 256) launch_pool<256>(h, s, tv, cursor, ps);
+        else launch_pool<128>(h, s, tv, cursor, ps);
     } else if (h->sens.K > 0) {
         const size_t smem = track_smem_bytes_sens(h);
         if (h->block_size == 256)
-            track_kernel<256, true><<<h->sens_track_blocks, 256, smem, s>>>(
-                h->tables, tv, h->processing.view, h->processed.view, h->extra.view, cursor, h->sens);
+            track_kernel<256, true><<<h->sens_track_blocks, 256, smem, s>>>(h->tables, tv, ps.in, ps.census,
+                                                                            ps.extra, cursor, h->sens);
         else
-            track_kernel<128, true><<<h->sens_track_blocks, 128, smem, s>>>(
-                h->tables, tv, h->processing.view, h->processed.view, h->extra.view, cursor, h->sens);
+            track_kernel<128, true><<<h->sens_track_blocks, 128, smem, s>>>(h->tables, tv, ps.in, ps.census,
+                                                                            ps.extra, cursor, h->sens);
     } else {
         const size_t smem = track_smem_bytes(h);
         if (h->block_size == 256)
-            track_kernel<256, false><<<h->track_blocks, 256, smem, s>>>(h->tables, tv, h->processing.view,
-                                                                        h->processed.view, h->extra.view, cursor,
-                                                                        DevSens{});
+            track_kernel<256, false><<<h->track_blocks, 256, smem, s>>>(h->tables, tv, ps.in, ps.census, ps.extra,
+                                                                        cursor, DevSens{});
         else
-            track_kernel<128, false><<<h->track_blocks, 128, smem, s>>>(h->tables, tv, h->processing.view,
-                                                                        h->processed.view, h->extra.view, cursor,
-                                                                        DevSens{});
+            track_kernel<128, false><<<h->track_blocks, 128, smem, s>>>(h->tables, tv, ps.in, ps.census, ps.extra,
+                                                                        cursor, DevSens{});
     }
     QSG_CUDA(cudaGetLastError());
-    // the extra store becomes the next pass's input; the old input is free
+    return QSG_OK;
+}
+
+// One tracking pass over the handle's stores: processing -> processed +
+// extra; the extra store then becomes the next pass's input.
+int launch_pass(QsgHandle* h, cudaStream_t s)
+{
+    const int st = launch_pass_stores(h, s, PassStores{h->processing.view, h->processed.view, h->extra.view});
+    if (st) return st;
     std::swap(h->processing, h->extra);
     return QSG_OK;
 }
@@ -2051,6 +2063,97 @@ extern "C" int qsg_get_census(QsgHandle* h, QsgParticleSoA* host, uint64_t cap, 
     if (c == 0) return QSG_OK;
     if ((st = check_soa(host))) return st;
     return copy_soa(h->processed.view, host, c, false);
+    QSG_API_END
+}
+
+namespace {
+
+// Device view of a caller's particle arrays for qsg_track_host: each field
+// must be page-locked host memory (cudaHostAlloc / cudaHostRegister, which the
+// GPU reads and writes over the host link) or device memory.
+int device_soa_view(const QsgParticleSoA* soa, const char* what, DevStore& v)
+{
+    void* fields[20] = {soa->x, soa->y, soa->z, soa->vx, soa->vy, soa->vz, soa->kinetic_energy, soa->weight,
+                        soa->time_to_census, soa->age, soa->num_mean_free_paths, soa->num_segments,
+                        soa->random_number_seed, soa->identifier, soa->last_event, soa->num_collisions, soa->breed,
+                        soa->species, soa->domain, soa->cell};
+    void* dev[20];
+    for (int k = 0; k < 20; k++) {
+        cudaPointerAttributes a{};
+        QSG_CUDA(cudaPointerGetAttributes(&a, fields[k]));
+        if (a.type == cudaMemoryTypeHost && a.devicePointer) dev[k] = a.devicePointer;
+        else if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) dev[k] = fields[k];
+        else
+            return fail(QSG_ERR_INVALID, "qsg_track_host: %s field %d is pageable host memory; page-lock it "
+                        "(cudaHostAlloc / cudaHostRegister) or use qsg_set_particles", what, k);
+    }
+    v = DevStore{};
+    v.x = (double*)dev[0]; v.y = (double*)dev[1]; v.z = (double*)dev[2];
+    v.vx = (double*)dev[3]; v.vy = (double*)dev[4]; v.vz = (double*)dev[5];
+    v.kinetic_energy = (double*)dev[6]; v.weight = (double*)dev[7]; v.time_to_census = (double*)dev[8];
+    v.age = (double*)dev[9]; v.num_mean_free_paths = (double*)dev[10]; v.num_segments = (double*)dev[11];
+    v.seed = (uint64_t*)dev[12]; v.identifier = (uint64_t*)dev[13];
+    v.last_event = (int32_t*)dev[14]; v.num_collisions = (int32_t*)dev[15]; v.breed = (int32_t*)dev[16];
+    v.species = (int32_t*)dev[17]; v.domain = (int32_t*)dev[18]; v.cell = (int32_t*)dev[19];
+    return QSG_OK;
+}
+
+}  // namespace
+
+extern "C" int qsg_track_host(QsgHandle* h, const QsgParticleSoA* particles, uint64_t n, QsgParticleSoA* census,
+                              uint64_t census_capacity, uint64_t* n_census, void* stream)
+{
+    QSG_API_BEGIN
+    if (!h || !n_census) return fail(QSG_ERR_INVALID, "qsg_track_host: null argument");
+    *n_census = 0;
+    if (h->sens.K > 0)
+        return fail(QSG_ERR_UNSUPPORTED, "qsg_track_host: sensitivity scores do not travel through host arrays; "
+                    "use qsg_set_particles / qsg_track_cycle");
+    int st = set_device(h);
+    if (st) return st;
+    if (n == 0) return QSG_OK;
+    if ((st = check_soa(particles)) || (st = check_soa(census))) return st;
+    PassStores ps;
+    if ((st = device_soa_view(particles, "particles", ps.in)) || (st = device_soa_view(census, "census", ps.census)))
+        return st;
+    ps.in.count = &h->scalars.ptr->host_in_count;
+    ps.in.capacity = n;
+    ps.census.count = &h->scalars.ptr->host_census_count;
+    ps.census.capacity = census_capacity;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const unsigned long long nn = n;
+    QSG_CUDA(cudaMemcpyAsync(ps.in.count, &nn, sizeof(nn), cudaMemcpyHostToDevice, s));
+    QSG_CUDA(cudaMemsetAsync(ps.census.count, 0, sizeof(unsigned long long), s));
+    // pass 0 reads the caller's arrays; fission products go to the handle's
+    // stores, which later passes read; every pass appends census particles
+    // to the caller's arrays
+    if ((st = h->extra.reserve(4 * n))) return st;
+    ps.extra = h->extra.view;
+    if ((st = launch_pass_stores(h, s, ps))) return st;
+    unsigned long long counts[2] = {0, 0};
+    for (int pass = 1;; pass++) {
+        QSG_CUDA(cudaMemcpyAsync(&counts[0], h->extra.count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        QSG_CUDA(cudaMemcpyAsync(&counts[1], ps.census.count, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        QSG_CUDA(cudaStreamSynchronize(s));
+        if (counts[0] == 0) break;
+        if (counts[0] > h->extra.capacity)
+            return fail(QSG_ERR_CAPACITY, "qsg_track_host: pass %d made %llu fission products, more than the "
+                        "%llu the product store holds", pass - 1, counts[0], (unsigned long long)h->extra.capacity);
+        std::swap(h->processing, h->extra);   // this pass's input: the products
+        if ((st = h->extra.reserve(4 * counts[0]))) return st;
+        ps.in = h->processing.view;
+        ps.extra = h->extra.view;
+        if ((st = launch_pass_stores(h, s, ps))) return st;
+    }
+    QSG_CUDA(cudaMemsetAsync(h->processing.count, 0, sizeof(unsigned long long), s));
+    QSG_CUDA(cudaStreamSynchronize(s));
+    h->n_processing = 0;
+    *n_census = counts[1];
+    if (counts[1] > census_capacity)
+        return fail(QSG_ERR_CAPACITY, "qsg_track_host: %llu census particles exceed census_capacity %llu -- the "
+                    "census arrays hold the first %llu", counts[1], (unsigned long long)census_capacity,
+                    (unsigned long long)census_capacity);
+    return QSG_OK;
     QSG_API_END
 }
 

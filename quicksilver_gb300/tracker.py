@@ -68,6 +68,22 @@ class Tracker:
     def track(self) -> None:
         N.check(N.lib().qsg_track_cycle_sync(self._h))
 
+    def track_host(self, inputs: dict, n: int, census: dict, capacity: int, stream=None) -> int:
+        """qsg_track_host: track the ``n`` particles in ``inputs`` and append
+        census particles to ``census`` (room for ``capacity``), both mapping
+        SoA field names to page-locked host arrays (torch tensors made with
+        ``pin_memory=True``, or numpy views of page-locked memory); the GPU
+        reads and writes them over the host link during tracking.  Returns
+        the census count; tallies accumulate in the handle."""
+        def ptr(a):
+            return a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data
+        si = N.soa_from_pointers({k: ptr(v) for k, v in inputs.items()})
+        so = N.soa_from_pointers({k: ptr(v) for k, v in census.items()})
+        got = C.c_uint64()
+        N.check(N.lib().qsg_track_host(self._h, C.byref(si), n, C.byref(so), capacity, C.byref(got),
+                                       C.c_void_p(stream) if stream else None))
+        return got.value
+
     def sizes(self):
         a, b = C.c_uint64(), C.c_uint64()
         N.check(N.lib().qsg_sizes(self._h, C.byref(a), C.byref(b)))
