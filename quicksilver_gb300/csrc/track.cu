@@ -789,7 +789,7 @@ __device__ __forceinline__ void sens_segment(const DevTables& t, const DevSens& 
                                              bool collided, double* S, int ss)
 {
     const double l = p.seg_len;
-    if (l == 0.0) return;   // nothing moved: no flight score and no flux tally
+    if (f64_eq0(l)) return;   // nothing moved: no flight score and no flux tally
     const int64_t base = ((int64_t)cls * t.num_groups + p.group) * 3;
     int pk[3];
     double pd[3];
@@ -802,14 +802,27 @@ __device__ __forceinline__ void sens_segment(const DevTables& t, const DevSens& 
     const double lw = l * p.weight;
     atomicAdd(sens.flux_cell + p.cell, lw);
     double* row = sens.dflux + (int64_t)p.cell * sens.K;
+    // parameters without a collision term in this flight
     for (int k = 0; k < sens.K; k++) {
-        double v = S[k * ss];
-        if (collided) {
+        if (collided && (k == pk[0] || k == pk[1] || k == pk[2])) continue;
+        const double v = S[k * ss];
+        if (!f64_eq0(v)) atomicAdd(row + k, lw * v);
+    }
+    if (!collided) return;
+    // the (at most three) parameters the collision's cross sections depend
+    // on: S_k plus dSigma_t/dtheta_k / Sigma_t of each reaction type that
+    // parameter scales, added in reaction order -- the same sum as adding
+    // them inside the loop above, which a warp would run for every (k, j)
+    // some lane matches
 #pragma unroll
-            for (int j = 0; j < 3; j++)
-                if (pk[j] == k) v += pd[j] * p.mean_free_path;
-        }
-        if (v != 0.0) atomicAdd(row + k, lw * v);
+    for (int j = 0; j < 3; j++) {
+        const int k = pk[j];
+        if (k < 0 || (j >= 1 && pk[0] == k) || (j == 2 && pk[1] == k)) continue;   // first occurrence only
+        double v = S[k * ss];
+#pragma unroll
+        for (int j2 = j; j2 < 3; j2++)
+            if (pk[j2] == k) v += pd[j2] * p.mean_free_path;
+        if (!f64_eq0(v)) atomicAdd(row + k, lw * v);
     }
 }
 
@@ -1255,7 +1268,7 @@ __global__ void __launch_bounds__(BLOCK, (kTrackMinBlocks * 128 + BLOCK - 1) / B
                             atomicAdd(sens.leak + st.prob, p.weight);
                             for (int k = 0; k < sens.K; k++) {
                                 const double sv = S[k * POOL];
-                                if (sv != 0.0) atomicAdd(sens.dleak + (int64_t)st.prob * sens.K + k, p.weight * sv);
+                                if (!f64_eq0(sv)) atomicAdd(sens.dleak + (int64_t)st.prob * sens.K + k, p.weight * sv);
                             }
                         }
                         p.last_event = QSG_EVENT_FACET_ESCAPE;
