@@ -385,6 +385,19 @@ int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* particles, u
  * on a correct build). */
 int qsg_check_arithmetic(int32_t device, uint64_t n, uint64_t seed, uint64_t* mismatches);
 
+/* The reference's -DEXPONENTIAL_TALLY build (CycleTracking.cc:48-50) as a
+ * run-time switch: before every segment one random number r is drawn from the
+ * particle's stream and exp(r) added to its cell in a per-cell tally
+ * (Tallies.hh:357-360, TallyCellValue).  The extra draw moves every later
+ * random number, so with it on every result is that build's, not the default
+ * build's.  qsg_read_cell_tally copies the tally ([num_cells], this handle's
+ * cell order) accumulated since qsg_reset_tallies or the last
+ * qsg_cycle_finalize, both of which zero it as the reference's cycleFinalize
+ * does (Tallies.cc:91); the reference keeps one copy per cTally replication
+ * and sums them there, this library keeps the sum.  Off by default. */
+int qsg_set_exponential_tally(QsgHandle* h, int32_t enabled);
+int qsg_read_cell_tally(QsgHandle* h, double* cell_tally);
+
 /* Tracks particles that live in the caller's page-locked host arrays
  * (cudaHostAlloc / cudaHostRegister; device arrays work too) without staging
  * copies: the tracking launch reads each particle from `particles` (n of them)

@@ -87,6 +87,14 @@ def lib() -> C.CDLL:
         h.oracle_track.argtypes = [vp, vp, C.c_uint64, vp, C.c_uint64, C.POINTER(C.c_uint64),
                                    C.POINTER(C.c_uint64), C.POINTER(C.c_double), C.c_int]
         h.oracle_track.restype = C.c_int
+        h.oracle_track_cell_tally.argtypes = [vp, vp, C.c_uint64, vp, C.c_uint64, C.POINTER(C.c_uint64),
+                                              C.POINTER(C.c_uint64), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                              C.c_int]
+        h.oracle_track_cell_tally.restype = C.c_int
+        h.oracle_enable_exponential_tally.argtypes = [vp]
+        h.oracle_enable_exponential_tally.restype = C.c_int
+        h.oracle_read_cell_tally.argtypes = [vp, vp]
+        h.oracle_read_cell_tally.restype = C.c_int
         h.oracle_track_sens.argtypes = [vp, C.POINTER(OracleSens), vp, vp, C.c_uint64, vp, vp, C.c_uint64,
                                         C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_double), C.c_int]
         h.oracle_track_sens.restype = C.c_int
@@ -173,6 +181,19 @@ class OracleRun:
     def warnings(self) -> int:
         return int(lib().oracle_warning_count(self._h))
 
+    def enable_exponential_tally(self):
+        """Behave as the reference built with -DEXPONENTIAL_TALLY (an extra
+        random number per segment, exp of it tallied per cell)."""
+        if lib().oracle_enable_exponential_tally(self._h):
+            raise RuntimeError("oracle_enable_exponential_tally failed")
+
+    def cell_tally(self) -> np.ndarray:
+        """[C] exponential cell tally of the running cycle (reset by cycle_finalize)."""
+        out = np.zeros(self.num_cells)
+        if lib().oracle_read_cell_tally(self._h, out.ctypes.data):
+            raise RuntimeError("exponential cell tally is off")
+        return out
+
     def enable_sensitivity(self, params):
         """params: (material, reaction type, group_lo, group_hi, theta) per parameter."""
         self._sens = make_sens(params)
@@ -205,20 +226,32 @@ class OracleRun:
         return np.frombuffer(buf, dtype=np.float64).copy().reshape(n, self.K)
 
 
-def track(problem_ptr, num_cells: int, num_groups: int, particles: np.ndarray, nthreads: int = 0):
-    """One-shot tracking: returns (census records, balance[13], flux[C, G])."""
+def track(problem_ptr, num_cells: int, num_groups: int, particles: np.ndarray, nthreads: int = 0,
+          cell_tally: bool = False):
+    """One-shot tracking: returns (census records, balance[13], flux[C, G]),
+    plus the exponential cell tally [C] when ``cell_tally`` (the reference's
+    EXPONENTIAL_TALLY build)."""
     recs = np.ascontiguousarray(particles, dtype=PARTICLE_DTYPE)
     n = len(recs)
     cap = max(4 * n + 16, 1024)
-    census = np.empty(cap, dtype=PARTICLE_DTYPE)
-    bal = (C.c_uint64 * 13)()
-    flux = np.zeros(num_cells * num_groups, dtype=np.float64)
-    n_census = C.c_uint64(0)
-    st = lib().oracle_track(problem_ptr, recs.ctypes.data if n else None, n, census.ctypes.data, cap,
-                            C.byref(n_census), bal, flux.ctypes.data_as(C.POINTER(C.c_double)), nthreads)
+    while True:
+        census = np.empty(cap, dtype=PARTICLE_DTYPE)
+        bal = (C.c_uint64 * 13)()
+        flux = np.zeros(num_cells * num_groups, dtype=np.float64)
+        ct = np.zeros(num_cells, dtype=np.float64)
+        n_census = C.c_uint64(0)
+        st = lib().oracle_track_cell_tally(problem_ptr, recs.ctypes.data if n else None, n, census.ctypes.data, cap,
+                                           C.byref(n_census), bal, flux.ctypes.data_as(C.POINTER(C.c_double)),
+                                           ct.ctypes.data_as(C.POINTER(C.c_double)) if cell_tally else None,
+                                           nthreads)
+        if st == -3:   # fission grew the population past the census room: again, with room for all
+            cap = n_census.value + 16
+            continue
+        break
     if st:
         raise RuntimeError(f"oracle_track failed ({st})")
-    return census[: n_census.value].copy(), np.array(bal, dtype=np.uint64), flux.reshape(num_cells, num_groups)
+    out = (census[: n_census.value].copy(), np.array(bal, dtype=np.uint64), flux.reshape(num_cells, num_groups))
+    return out + (ct,) if cell_tally else out
 
 
 def track_sens(problem_ptr, num_cells: int, num_groups: int, particles: np.ndarray, params, scores=None,

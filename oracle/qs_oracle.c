@@ -92,6 +92,7 @@ typedef struct TrackCtx {
     uint64_t* warnings;
     int overflow;
     OracleSens* sens;        /* NULL: no sensitivity scores */
+    double* cell_tally;      /* [C] exponential cell tally (the reference's EXPONENTIAL_TALLY build); NULL: off */
 } TrackCtx;
 
 static void atomic_inc(uint64_t* a, uint64_t v)
@@ -548,7 +549,7 @@ static int collision_event(TrackCtx* ctx, WorkParticle* w)
         sel_iso = iso;
         sel_r = pb->isotope_reaction_offset[iso + 1] - 1;
     }
-    double energy_out[4], angle_out[4];
+    double energy_out[4] = {0}, angle_out[4] = {0};
     int n_out = 0;
     double mass = pb->material_mass[mat];
     int type = pb->reaction_type[sel_r];
@@ -638,6 +639,10 @@ static void track_one(TrackCtx* ctx, const OracleParticle* in, const double* in_
     int keep;
     do {
         if (ctx->sens) w.segment_path_length = 0.0;   /* a segment that returns early moves nothing */
+        /* EXPONENTIAL_TALLY build of the reference (CycleTracking.cc:48-50,
+         * Tallies.hh:357-360): one random number per segment, its exp tallied
+         * in the particle's cell, before the segment outcome */
+        if (ctx->cell_tally) atomic_add_d(&ctx->cell_tally[w.cell], exp(oracle_rng_sample(&w.seed)));
         int outcome = segment_outcome(ctx, &w);
         if (ctx->sens) sens_segment(ctx, &w, outcome == OUT_COLLISION);
         atomic_inc(&ctx->bal->v[QSG_BAL_NUM_SEGMENTS], 1);
@@ -708,7 +713,7 @@ static void set_threads(int nthreads)
  * (ParticleVaultContainer::addExtraParticle, :340-349) become the next
  * processing list (cleanExtraVaults, :357-400) until none are left. */
 static int track_all(const QsgProblem* pb, Store* processing, Store* census, Counters* bal, double* flux,
-                     uint64_t* warnings, int nthreads, OracleSens* sens)
+                     uint64_t* warnings, int nthreads, OracleSens* sens, double* cell_tally)
 {
     Store extra = {0, 0, 0, NULL, processing->K};
     set_threads(nthreads);
@@ -718,7 +723,7 @@ static int track_all(const QsgProblem* pb, Store* processing, Store* census, Cou
         /* worst case: every particle censuses; every fission makes <= 4 */
         if (store_reserve(census, census->n + n) || store_reserve(&extra, 4 * n)) { status = -1; break; }
         extra.n = 0;
-        TrackCtx ctx = {pb, flux, bal, census, &extra, warnings, 0, sens};
+        TrackCtx ctx = {pb, flux, bal, census, &extra, warnings, 0, sens, cell_tally};
         const OracleParticle* src = processing->p;
         const double* src_sc = processing->K > 0 ? processing->sc : NULL;
         const int K = processing->K;
@@ -752,6 +757,7 @@ struct OracleRun {
     uint64_t warnings;
     OracleSens sens;            /* sens.K == 0: off */
     int has_sens;
+    double* cell_tally;         /* [C] exponential cell tally, NULL: off */
 };
 
 OracleRun* oracle_create(const QsgProblem* pb, const double* source_rate, uint64_t n_particles,
@@ -787,6 +793,7 @@ void oracle_destroy(OracleRun* r)
     }
     free(r->flux);
     free(r->source_tally);
+    free(r->cell_tally);
     free(r);
 }
 
@@ -998,7 +1005,7 @@ int oracle_cycle_init(OracleRun* run)
 int oracle_cycle_tracking(OracleRun* run, int nthreads)
 {
     return track_all(run->pb, &run->processing, &run->processed, &run->bal, run->flux, &run->warnings, nthreads,
-                     run->has_sens ? &run->sens : NULL);
+                     run->has_sens ? &run->sens : NULL, run->cell_tally);
 }
 
 int oracle_cycle_finalize(OracleRun* run)
@@ -1008,6 +1015,21 @@ int oracle_cycle_finalize(OracleRun* run)
     memset(&run->bal, 0, sizeof(run->bal));
     run->bal.v[QSG_BAL_START] = run->last.v[QSG_BAL_END];
     memset(run->flux, 0, sizeof(double) * (size_t)run->pb->num_cells * run->pb->num_groups);
+    /* the reference resets its cell tally every cycle (Tallies.cc:91) */
+    if (run->cell_tally) memset(run->cell_tally, 0, sizeof(double) * (size_t)run->pb->num_cells);
+    return 0;
+}
+
+int oracle_enable_exponential_tally(OracleRun* r)
+{
+    if (!r->cell_tally) r->cell_tally = (double*)calloc((size_t)r->pb->num_cells, sizeof(double));
+    return r->cell_tally ? 0 : -1;
+}
+
+int oracle_read_cell_tally(const OracleRun* r, double* out)
+{
+    if (!r->cell_tally) return -1;
+    memcpy(out, r->cell_tally, sizeof(double) * (size_t)r->pb->num_cells);
     return 0;
 }
 
@@ -1067,6 +1089,13 @@ const double* oracle_flux(const OracleRun* r) { return r->flux; }
 int oracle_track(const QsgProblem* pb, const OracleParticle* in, uint64_t n, OracleParticle* census_out,
                  uint64_t cap, uint64_t* n_census, uint64_t* balance13, double* flux, int nthreads)
 {
+    return oracle_track_cell_tally(pb, in, n, census_out, cap, n_census, balance13, flux, NULL, nthreads);
+}
+
+int oracle_track_cell_tally(const QsgProblem* pb, const OracleParticle* in, uint64_t n, OracleParticle* census_out,
+                            uint64_t cap, uint64_t* n_census, uint64_t* balance13, double* flux, double* cell_tally,
+                            int nthreads)
+{
     Store processing = {0, 0, 0, NULL, 0}, census = {0, 0, 0, NULL, 0};
     if (store_reserve(&processing, n ? n : 1)) return -1;
     memcpy(processing.p, in, n * sizeof(OracleParticle));
@@ -1074,7 +1103,7 @@ int oracle_track(const QsgProblem* pb, const OracleParticle* in, uint64_t n, Ora
     Counters bal;
     memset(&bal, 0, sizeof(bal));
     uint64_t warnings = 0;
-    int st = track_all(pb, &processing, &census, &bal, flux, &warnings, nthreads, NULL);
+    int st = track_all(pb, &processing, &census, &bal, flux, &warnings, nthreads, NULL, cell_tally);
     for (int k = 0; k < QSG_BAL_COUNT; k++) balance13[k] += bal.v[k];
     uint64_t ncopy = census.n < cap ? census.n : cap;
     if (census_out && ncopy) memcpy(census_out, census.p, ncopy * sizeof(OracleParticle));
@@ -1099,7 +1128,7 @@ int oracle_track_sens(const QsgProblem* pb, OracleSens* sens, const OraclePartic
     Counters bal;
     memset(&bal, 0, sizeof(bal));
     uint64_t warnings = 0;
-    int st = track_all(pb, &processing, &census, &bal, flux, &warnings, nthreads, sens);
+    int st = track_all(pb, &processing, &census, &bal, flux, &warnings, nthreads, sens, NULL);
     for (int k = 0; k < QSG_BAL_COUNT; k++) balance13[k] += bal.v[k];
     uint64_t ncopy = census.n < cap ? census.n : cap;
     if (census_out && ncopy) memcpy(census_out, census.p, ncopy * sizeof(OracleParticle));

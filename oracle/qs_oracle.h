@@ -98,6 +98,20 @@ int oracle_track(const QsgProblem* problem, const OracleParticle* in, uint64_t n
                  OracleParticle* census_out, uint64_t cap, uint64_t* n_census,
                  uint64_t* balance13, double* flux, int nthreads);
 
+/* The reference built with -DEXPONENTIAL_TALLY (CycleTracking.cc:48-50):
+ * before every segment a random number r is drawn from the particle's stream
+ * and exp(r) added to the particle's cell in a per-cell tally
+ * (Tallies.hh:357-360), which cycleFinalize resets (Tallies.cc:91).
+ * oracle_enable_exponential_tally switches a run to that build's behaviour;
+ * oracle_read_cell_tally copies the current tally ([num_cells]).
+ * oracle_track_cell_tally is oracle_track with it (cell_tally NULL: off;
+ * otherwise num_cells doubles, added to). */
+int oracle_enable_exponential_tally(OracleRun* run);
+int oracle_read_cell_tally(const OracleRun* run, double* out);
+int oracle_track_cell_tally(const QsgProblem* problem, const OracleParticle* in, uint64_t n,
+                            OracleParticle* census_out, uint64_t cap, uint64_t* n_census,
+                            uint64_t* balance13, double* flux, double* cell_tally, int nthreads);
+
 /* MC_RNG_State restated (MC_RNG_State.hh:22-33, MC_RNG_State.cc:29-113). */
 double oracle_rng_sample(uint64_t* seed);
 uint64_t oracle_rng_spawn(uint64_t* parent_seed);

@@ -23,6 +23,9 @@
 //   QS_DUMP=<file>        write the binary dump there (format: see write_arr)
 //   QS_DUMP_TABLES=1      include problem tables
 //   QS_DUMP_PARTICLES=1   include initial and census particle records
+//   Built with -DEXPONENTIAL_TALLY (make -C oracle ref_exp) it also writes,
+//   per cycle, the reference's exponential cell tally.
+//
 //   QS_THETA=<file>       cross-section scale factors applied after initMC;
 //                         lines "material reactionType gLo gHi factor" with
 //                         reactionType 1=scatter 2=absorption 3=fission and
@@ -347,6 +350,22 @@ int main(int argc, char** argv)
          }
       }
       write_d("flux_c" + std::to_string(cyc), flux);
+#ifdef EXPONENTIAL_TALLY
+      // the exponential cell tally (CycleTracking.cc:48-50), summed over its
+      // replications, before cycleFinalize resets it (Tallies.cc:91)
+      std::vector<double> cell_tally(NC, 0.0);
+      for (int d = 0; d < mcco->domain.size(); ++d)
+      {
+         MC_Domain& dom = mcco->domain[d];
+         for (int r = 0; r < t->GetNumCellTallyReplications(); ++r)
+         {
+            CellTallyTask& task = t->_cellTallyDomain[d]._task[r];
+            for (int c = 0; c < dom.cell_state.size(); ++c)
+               cell_tally[(int64_t)(dom.cell_state[c]._id >> 32)] += task._cell[c];
+         }
+      }
+      write_d("cell_tally_c" + std::to_string(cyc), cell_tally);
+#endif
       if (want_particles) dump_particles("census_c" + std::to_string(cyc), false);
 
       cycleFinalize();

@@ -138,6 +138,8 @@ _SIGNATURES = {
                                      C.POINTER(C.c_uint64), _VP, _VP, _VP], C.c_int),
     "qsg_track_host": ([_VP, C.POINTER(QsgParticleSoA), C.c_uint64, C.POINTER(QsgParticleSoA), C.c_uint64,
                         C.POINTER(C.c_uint64), _VP], C.c_int),
+    "qsg_set_exponential_tally": ([_VP, C.c_int32], C.c_int),
+    "qsg_read_cell_tally": ([_VP, _dp], C.c_int),
     "qsg_read_tallies": ([_VP, _up, _dp], C.c_int),
     "qsg_reset_tallies": ([_VP], C.c_int),
     "qsg_device_status": ([_VP, C.POINTER(C.c_uint32), C.c_int], C.c_int),

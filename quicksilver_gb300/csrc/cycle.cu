@@ -515,6 +515,8 @@ int cycle_finalize_enqueue(QsgHandle* h, cudaStream_t s)
     cycle_advance_kernel<<<1, 1, 0, s>>>(h->scalars.ptr);
     QSG_CUDA(cudaGetLastError());
     QSG_CUDA(cudaMemsetAsync(h->flux.ptr, 0, (size_t)h->flux_replicas * stride * sizeof(double), s));
+    // the reference's cycleFinalize resets its cell tally too (Tallies.cc:91)
+    if (h->exp_tally) QSG_CUDA(cudaMemsetAsync(h->cell_tally.ptr, 0, h->cell_tally.n * sizeof(double), s));
     h->cycles_finalized++;
     return QSG_OK;
 }

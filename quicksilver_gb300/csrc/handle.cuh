@@ -213,6 +213,8 @@ struct QsgHandle {
     uint64_t max_segments = (uint64_t)1 << 40;
     int32_t num_cells = 0, num_groups = 0, num_materials = 0;
     // tables
+    bool exp_tally = false;          // the reference's EXPONENTIAL_TALLY build (qsg_set_exponential_tally)
+    qsg::DevBuf<double> cell_tally;  // [num_cells]
     qsg::DevBuf<double> energies, sigma_total, mfp_table, inv_mfp_table, macro_xs, class_nubar, material_mass, cell_nodes, cell_center, planes;
     qsg::DevBuf<int32_t> class_num_reactions, class_material, cell_class, adj_cell;
     qsg::DevBuf<int8_t> class_type;

@@ -461,6 +461,10 @@ enum { OUT_COLLISION = 0, OUT_FACET = 1, OUT_CENSUS = 2 };
 __device__ __forceinline__ int segment_outcome(const DevTables& t, const DevTally& tally, Particle& p,
                                                int cls, double* flux_row)
 {
+    // The reference's EXPONENTIAL_TALLY build (CycleTracking.cc:48-50,
+    // Tallies.hh:357-360): one random number per segment, its exp added to
+    // the particle's cell, before the segment outcome
+    if (tally.cell_tally) atomicAdd(tally.cell_tally + p.cell, exp(rng_sample(p.seed)));
     double d_coll, d_facet, d_census;
     p.seg_len = 0.0;
     if (f64_lt0(p.speed)) p.speed = sqrt(p.vx * p.vx + p.vy * p.vy + p.vz * p.vz);
@@ -1342,6 +1346,7 @@ DevTally tally_view(QsgHandle* h)
     t.queue_chunk = h->queue_chunk;
     t.pool_collision_step = h->pool_collision_step;
     t.pool_refill = h->pool_refill;
+    t.cell_tally = h->exp_tally ? h->cell_tally.ptr : nullptr;
     return t;
 }
 
@@ -1988,7 +1993,7 @@ extern "C" int qsg_destroy(QsgHandle* h)
 {
     if (!h) return QSG_OK;
     cudaSetDevice(h->device);
-    h->energies.free(); h->sigma_total.free(); h->mfp_table.free(); h->inv_mfp_table.free(); h->macro_xs.free(); h->class_nubar.free();
+    h->energies.free(); h->sigma_total.free(); h->mfp_table.free(); h->inv_mfp_table.free(); h->cell_tally.free(); h->macro_xs.free(); h->class_nubar.free();
     h->material_mass.free(); h->cell_nodes.free(); h->cell_center.free(); h->planes.free();
     h->class_num_reactions.free(); h->class_material.free(); h->cell_class.free(); h->adj_cell.free();
     h->class_type.free(); h->adj_facet_event.free();
@@ -2243,7 +2248,38 @@ extern "C" int qsg_reset_tallies(QsgHandle* h)
     if (st) return st;
     QSG_CUDA(cudaMemset(h->flux.ptr, 0, h->flux.n * sizeof(double)));
     QSG_CUDA(cudaMemset(h->balance.ptr, 0, h->balance.n * sizeof(unsigned long long)));
+    if (h->cell_tally.ptr) QSG_CUDA(cudaMemset(h->cell_tally.ptr, 0, h->cell_tally.n * sizeof(double)));
     return QSG_OK;
+}
+
+extern "C" int qsg_set_exponential_tally(QsgHandle* h, int32_t enabled)
+{
+    QSG_API_BEGIN
+    if (!h) return fail(QSG_ERR_INVALID, "qsg_set_exponential_tally: null handle");
+    if (enabled != 0 && enabled != 1) return fail(QSG_ERR_INVALID, "qsg_set_exponential_tally: enabled must be 0 or 1");
+    int st = set_device(h);
+    if (st) return st;
+    if (enabled && !h->cell_tally.ptr) {
+        if ((st = h->cell_tally.alloc((size_t)h->num_cells))) return st;
+        QSG_CUDA(cudaMemset(h->cell_tally.ptr, 0, h->cell_tally.n * sizeof(double)));
+    }
+    h->exp_tally = enabled != 0;
+    h->clear_graphs();   // captured launches carry the old tally view
+    return QSG_OK;
+    QSG_API_END
+}
+
+extern "C" int qsg_read_cell_tally(QsgHandle* h, double* cell_tally)
+{
+    QSG_API_BEGIN
+    if (!h || !cell_tally) return fail(QSG_ERR_INVALID, "qsg_read_cell_tally: null argument");
+    if (!h->exp_tally) return fail(QSG_ERR_INVALID, "qsg_read_cell_tally: the exponential tally is off");
+    int st = set_device(h);
+    if (st) return st;
+    QSG_CUDA(cudaDeviceSynchronize());
+    QSG_CUDA(cudaMemcpy(cell_tally, h->cell_tally.ptr, h->cell_tally.n * sizeof(double), cudaMemcpyDeviceToHost));
+    return QSG_OK;
+    QSG_API_END
 }
 
 extern "C" int qsg_device_status(QsgHandle* h, uint32_t* flags, int clear)

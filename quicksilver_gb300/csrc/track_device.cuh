@@ -126,6 +126,7 @@ struct DevTally {
     int32_t pool_collision_step;   // pool kernel: parked collisions that make a collision step (1-32)
     int32_t pool_refill;           // pool kernel: empty slots that trigger a refill from the queue (1-64)
     uint64_t max_segments;
+    double* cell_tally;            // [C] exponential cell tally (the reference's EXPONENTIAL_TALLY build); null: off
 };
 
 // Problems whose counters a tracking block accumulates in shared memory

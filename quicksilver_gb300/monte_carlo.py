@@ -107,6 +107,16 @@ class _Driver:
         N.check(N.lib().qsg_set_observers(self.tracker.handle, flags))
         self._observe_flags = flags
 
+    def exponential_tally(self, enabled: bool = True) -> None:
+        """Run as the reference built with -DEXPONENTIAL_TALLY: one extra
+        random number per segment, exp of it tallied per cell (every later
+        result then follows that build).  The tally of the running cycle is
+        ``cell_tally()``; cycle finalize resets it."""
+        self.tracker.set_exponential_tally(enabled)
+
+    def cell_tally(self) -> np.ndarray:
+        return self.tracker.cell_tally()
+
     def fluence(self) -> np.ndarray:
         out = np.zeros(self.tracker.num_cells, dtype=np.float64)
         N.check(N.lib().qsg_read_observers(self.tracker.handle, out.ctypes.data_as(C.POINTER(C.c_double)), None))

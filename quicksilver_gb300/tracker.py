@@ -107,6 +107,16 @@ class Tracker:
     def reset_tallies(self) -> None:
         N.check(N.lib().qsg_reset_tallies(self._h))
 
+    def set_exponential_tally(self, enabled: bool = True) -> None:
+        """qsg_set_exponential_tally: the reference's -DEXPONENTIAL_TALLY build."""
+        N.check(N.lib().qsg_set_exponential_tally(self._h, int(enabled)))
+
+    def cell_tally(self) -> np.ndarray:
+        """[num_cells] exponential cell tally since the last reset."""
+        out = np.zeros(self.num_cells, dtype=np.float64)
+        N.check(N.lib().qsg_read_cell_tally(self._h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
     # ---- sensitivities (qsg_enable_sensitivity) ----
     def material_offsets(self) -> np.ndarray:
         """[problems + 1] offsets of each problem's materials in this handle."""

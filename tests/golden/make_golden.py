@@ -17,7 +17,13 @@ quicksilver_gb300/decks it runs the reference harness and stores in
 * ``rng_*``          known-answer vectors of rngSample / rngSpawn
 * ``track_seconds``  reference cycleTracking wall time per cycle (8 threads here)
 
-Usage: python tests/golden/make_golden.py [deck ...]
+With ``--exponential-tally`` it builds the reference with -DEXPONENTIAL_TALLY
+(``make -C oracle ref_exp``: one extra random number per segment, its exp
+tallied per cell, CycleTracking.cc:48-50) and stores ``exp_<deck>.npz``:
+``balance``, ``flux_cell``, ``flux_total``, ``census_sha`` / ``census_n`` and
+``cell_tally`` [cycles, cells] (gid order) for t_homog and t_fission by default.
+
+Usage: python tests/golden/make_golden.py [--exponential-tally] [deck ...]
 """
 from __future__ import annotations
 
@@ -34,6 +40,7 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 DECKS = ROOT / "quicksilver_gb300" / "decks"
 HARNESS = ROOT / "oracle" / "_ref" / "qs_ref_harness"
+HARNESS_EXP = ROOT / "oracle" / "_ref_exp" / "qs_ref_harness"
 REF_SRC = os.environ.get("QS_REF_SRC", "/root/reference/src")
 FULL_FLUX_LIMIT = 20000   # store the whole flux array when cells*groups is at most this
 
@@ -98,17 +105,17 @@ def projection_weights(cells: int, groups: int) -> np.ndarray:
     return np.random.default_rng(20240601).uniform(0.5, 1.5, size=(4, cells * groups))
 
 
-def ensure_harness() -> None:
-    res = subprocess.run(["make", "-C", str(ROOT / "oracle"), "ref", f"REF_SRC={REF_SRC}", "-j8"],
+def ensure_harness(target: str = "ref") -> None:
+    res = subprocess.run(["make", "-C", str(ROOT / "oracle"), target, f"REF_SRC={REF_SRC}", "-j8"],
                          capture_output=True, text=True)
     if res.returncode != 0:
         raise SystemExit(f"reference build failed:\n{res.stderr[-4000:]}")
 
 
-def run_deck(deck: Path, workdir: Path) -> dict:
+def run_deck(deck: Path, workdir: Path, harness: Path = HARNESS) -> dict:
     dump = workdir / (deck.stem + ".dump")
     env = dict(os.environ, QS_DUMP=str(dump), QS_DUMP_TABLES="1", QS_DUMP_PARTICLES="1", OMP_NUM_THREADS="8")
-    res = subprocess.run([str(HARNESS), "-i", str(deck)], env=env, capture_output=True, text=True)
+    res = subprocess.run([str(harness), "-i", str(deck)], env=env, capture_output=True, text=True)
     if res.returncode != 0:
         raise SystemExit(f"reference run failed on {deck}:\n{res.stderr[-4000:]}")
     return read_dump(dump)
@@ -151,13 +158,35 @@ def make(deck: Path, workdir: Path) -> None:
     print(f"{deck.name}: cycles={cycles} cells={C} groups={G} segments={int(out['balance'][:, 12].sum())}")
 
 
+def make_exp(deck: Path, workdir: Path) -> None:
+    d = run_deck(deck, workdir, HARNESS_EXP)
+    cycles = sum(1 for k in d if k.startswith("balance_c"))
+    G = len(d["energies"]) - 1
+    C = len(d["cell_volume"])
+    flux = np.stack([d[f"flux_c{c}"] for c in range(cycles)]).reshape(cycles, C, G)
+    out = {"balance": np.stack([d[f"balance_c{c}"] for c in range(cycles)]),
+           "flux_cell": flux.sum(axis=2), "flux_total": flux.sum(axis=(1, 2)),
+           "cell_tally": np.stack([d[f"cell_tally_c{c}"] for c in range(cycles)])}
+    cens = [sort_records(particles(d, f"census_c{c}")) for c in range(cycles)]
+    out["census_sha"] = np.array([sha(c) for c in cens])
+    out["census_n"] = np.array([len(c) for c in cens], dtype=np.int64)
+    np.savez_compressed(HERE / ("exp_" + deck.stem + ".npz"), **out)
+    print(f"exp_{deck.name}: cycles={cycles} cells={C} segments={int(out['balance'][:, 12].sum())} "
+          f"cell tally total {out['cell_tally'].sum():.6e}")
+
+
 def main(argv: list[str]) -> None:
     import tempfile
-    ensure_harness()
-    names = argv or sorted(p.stem for p in DECKS.glob("*.inp") if p.stem.startswith("t_") or p.stem == "config1")
+    exp = "--exponential-tally" in argv
+    argv = [a for a in argv if a != "--exponential-tally"]
+    ensure_harness("ref_exp" if exp else "ref")
+    if exp:
+        names = argv or ["t_homog", "t_fission"]
+    else:
+        names = argv or sorted(p.stem for p in DECKS.glob("*.inp") if p.stem.startswith("t_") or p.stem == "config1")
     with tempfile.TemporaryDirectory() as tmp:
         for name in names:
-            make(DECKS / f"{name}.inp", Path(tmp))
+            (make_exp if exp else make)(DECKS / f"{name}.inp", Path(tmp))
 
 
 if __name__ == "__main__":
