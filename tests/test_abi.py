@@ -58,3 +58,16 @@ def test_create_without_gpu_fails_loudly(has_gpu):
     h = ctypes.c_void_p()
     rc = N.lib().qsg_create(ctypes.byref(hp.view), None, ctypes.byref(h))
     assert rc == N.QSG_ERR_NO_DEVICE and "no CUDA device" in N.last_error()
+
+
+def test_new_entry_points_check_arguments_before_any_cuda_call(native_lib):
+    """Null handles and arguments are reported, not dereferenced (no GPU needed)."""
+    lib = N.lib()
+    got = ctypes.c_uint64(7)
+    assert lib.qsg_track_host(None, None, 0, None, 0, ctypes.byref(got), None) == N.QSG_ERR_INVALID
+    assert lib.qsg_set_exponential_tally(None, 1) == N.QSG_ERR_INVALID
+    assert lib.qsg_read_cell_tally(None, None) == N.QSG_ERR_INVALID
+    assert "null" in N.last_error()
+    assert lib.qsg_check_arithmetic(0, 16, 1, None) == N.QSG_ERR_INVALID
+    out = (ctypes.c_uint64 * 4)()
+    assert lib.qsg_check_arithmetic(-1, 16, 1, out) in (N.QSG_ERR_INVALID, N.QSG_ERR_NO_DEVICE)
