@@ -394,6 +394,20 @@ def run_config5(args):
     print(json.dumps(line), flush=True)
 
 
+def reduce_over_ranks(pg, times, counts, device):
+    """Whole-job figures of a multi-rank run: the max over ranks of each
+    timed duration, the sum over ranks of each count (every rank tracks its
+    own replica of the workload, so the units add up).  pg None: one rank."""
+    if pg is None:
+        return list(times), [int(c) for c in counts]
+    import torch
+    t = torch.tensor(list(times), dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    c = torch.tensor(list(counts), dtype=torch.float64, device=device)
+    pg.all_reduce(c)
+    return t.tolist(), [int(v) for v in c.tolist()]
+
+
 def run_reference_arm(args, world, rank):
     """--impl reference: the CPU port of the reference algorithm on the host cores."""
     if rank != 0:
@@ -566,14 +580,8 @@ def main():
         mc.cycle_finalize(stream)
     flags |= mc.device_status()
 
-    # max over ranks
-    if pg is not None:
-        t = torch.tensor([track_s, e2e_s, wall, staged_s], dtype=torch.float64, device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        track_s, e2e_s, wall, staged_s = t.tolist()
-        s = torch.tensor([segments, e2e_seg, staged_seg], dtype=torch.float64, device="cuda")
-        pg.all_reduce(s)
-        segments, e2e_seg, staged_seg = int(s[0]), int(s[1]), int(s[2])
+    (track_s, e2e_s, wall, staged_s), (segments, e2e_seg, staged_seg) = reduce_over_ranks(
+        pg, [track_s, e2e_s, wall, staged_s], [segments, e2e_seg, staged_seg], "cuda")
     if rank != 0:
         return
 
