@@ -352,7 +352,9 @@ int qsg_set_pool_tuning(QsgHandle* h, int32_t collision_step, int32_t refill);
  * ADDED into `flux` (device, [num_cells * G], the handle's cell numbering) and
  * the balance counters into `balance` (device, [problems * 13], QSG_BAL_*
  * order), so zero them first for fresh tallies.  The handle's own stores and
- * tallies are left alone.  The call returns when the work on `stream` (a
+ * tallies are left alone, except the exponential cell tally: with
+ * qsg_set_exponential_tally on, the per-segment draw happens here too and
+ * its tally adds to the handle's (allocated when it was switched on).  The call returns when the work on `stream` (a
  * cudaStream_t, or NULL) has finished.
  *
  * Allocates nothing: the fission products handed from one pass to the next
