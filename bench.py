@@ -18,11 +18,11 @@ calls with particles already in HBM (L2 flushed before every step);
 (the tracking launch reads the cycle's particles from, and appends census
 particles to, the pinned host arrays over the host link) and the D2H read of
 counters and flux, all inside the timed region; `e2e.staged_value` times the
-staged calls on the same vaults (H2D copy, tracking, D2H copy of the census).  `--impl reference` times the CPU port of the
-reference algorithm (oracle/qs_oracle.c, all host threads) on the same deck:
-the reference's own C++ cannot be built on the benchmark host (its sources
-are not there), so the port -- bit-exact with the reference on the golden
-decks -- stands in for it.
+staged calls on the same vaults (H2D copy, tracking, D2H copy of the census).
+`--impl reference` times the CPU port of the reference algorithm
+(oracle/qs_oracle.c, all host threads) on the same deck: the reference's own
+C++ sources are not present where the benchmark runs, so the port --
+bit-exact with the reference on the golden decks -- stands in for it.
 """
 from __future__ import annotations
 
