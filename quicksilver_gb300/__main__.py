@@ -9,7 +9,9 @@ figure of merit (segments per second of tracking), the census energy
 spectrum file when the deck names one (EnergySpectrum.cc:38-59) and the
 CORAL2 checks when the deck sets coralBenchmark (CoralBenchmark.cc:17-44).
 Simulation keys may be overridden on the command line (``--nParticles 1e5``),
-as the reference's flags do (Parameters.cc:230-255).
+as the reference's flags do (Parameters.cc:230-255).  ``--exponential-tally``
+runs as the reference built with -DEXPONENTIAL_TALLY (CycleTracking.cc:48-50)
+and adds each cycle's exponential cell-tally total to its line.
 """
 from __future__ import annotations
 
@@ -32,6 +34,8 @@ HEADER = ["start", "source", "rr", "split", "absorb", "scatter", "fission", "pro
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(prog="python -m quicksilver_gb300", description=__doc__.split("\n\n")[1])
     ap.add_argument("deck")
+    ap.add_argument("--exponential-tally", action="store_true",
+                    help="behave as the reference built with -DEXPONENTIAL_TALLY")
     args, extra = ap.parse_known_args(argv)
     deck = Deck.from_file(args.deck)
     it = iter(extra)
@@ -43,9 +47,12 @@ def main(argv=None) -> int:
     mc = MonteCarlo(deck)
     spectrum_stem = deck.energy_spectrum
     mc.observe(fluence=bool(sim.coral_benchmark), spectrum=bool(spectrum_stem))
+    if args.exponential_tally:
+        mc.exponential_tally(True)
     out = sys.stdout
     out.write("%-8s " % "cycle" + " ".join("%12s" % h for h in HEADER) +
-              " %14s %14s %14s %14s\n" % ("scalar_flux", "cycleInit", "cycleTracking", "cycleFinalize"))
+              " %14s %14s %14s %14s" % ("scalar_flux", "cycleInit", "cycleTracking", "cycleFinalize") +
+              (" %14s" % "cell_tally" if args.exponential_tally else "") + "\n")
     track_s = 0.0
     for cycle in range(sim.n_steps):
         t0 = time.perf_counter()
@@ -56,13 +63,15 @@ def main(argv=None) -> int:
         mc.cycle_tracking()
         mc_sync(h)
         t2 = time.perf_counter()
+        cell_total = mc.cell_tally().sum() if args.exponential_tally else None   # finalize resets it
         mc.cycle_finalize()
         row = mc.history(cycle, 1)
         t3 = time.perf_counter()
         track_s += t2 - t1
         bal = row.balance[0]
         out.write("%8d " % cycle + " ".join("%12d" % int(bal[N.BAL[c]]) for c in COLUMNS) +
-                  " %14e %14e %14e %14e\n" % (row.flux_total[0], t1 - t0, t2 - t1, t3 - t2))
+                  " %14e %14e %14e %14e" % (row.flux_total[0], t1 - t0, t2 - t1, t3 - t2) +
+                  (" %14e" % cell_total if cell_total is not None else "") + "\n")
     flags = mc.device_status()
     if flags:
         raise N.QsgError(N.QSG_ERR_DEVICE, f"device flags 0x{flags:x} raised during the run")

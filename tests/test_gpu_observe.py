@@ -70,3 +70,22 @@ def test_gpu_command_line_driver(gpu, tmp_path):
     counts = [int(l.split("\t")[2]) for l in open(str(stem) + ".dat").read().splitlines()]
     census = sum(int(r[11]) for r in rows)
     assert sum(counts) == census
+
+
+def test_gpu_command_line_driver_exponential_tally(gpu):
+    """--exponential-tally: the per-cycle counters the driver prints are those
+    of the reference built with -DEXPONENTIAL_TALLY, and so are the cell-tally
+    totals (to summation order and CUDA's exp)."""
+    res = subprocess.run([sys.executable, "-m", "quicksilver_gb300", str(DECKS / "t_homog.inp"),
+                          "--exponential-tally"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr
+    gold = np.load(ROOT / "tests" / "golden" / "exp_t_homog.npz")
+    rows = [l.split() for l in res.stdout.splitlines() if l.strip() and l.split()[0].isdigit()]
+    assert len(rows) == len(gold["balance"])
+    cols = ["start", "source", "rr", "split", "absorb", "scatter", "fission", "produce", "collision", "escape",
+            "census", "num_segments"]
+    for c, r in enumerate(rows):
+        for k, name in enumerate(cols):
+            assert int(r[1 + k]) == int(gold["balance"][c][N.BAL[name]]), (c, name)
+        want = gold["cell_tally"][c].sum()
+        assert abs(float(r[-1]) - want) <= 1e-6 * want   # printed with 7 significant digits
