@@ -119,17 +119,35 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def profile_traffic_per_segment():
-    """DRAM bytes per segment of the tracking kernel from the committed ncu summary."""
+def profile_value(key: str):
+    """A per-segment figure (``key: value`` line) of the committed ncu summary."""
     if not PROFILE_SUMMARY.exists():
         return None
     for line in PROFILE_SUMMARY.read_text().splitlines():
-        if line.strip().startswith("traffic_bytes_per_segment:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].strip().split()[0])
             except ValueError:
                 return None
     return None
+
+
+def profile_traffic_per_segment():
+    """DRAM bytes per segment of the tracking kernel from the committed ncu summary."""
+    return profile_value("traffic_bytes_per_segment")
+
+
+def fp64_roofline(fp64_per_segment, segments_per_s_per_gpu, peak):
+    """The tracking kernel against its binding roof: FP64 warp instructions
+    per second (ncu's count per segment x the measured segment rate) over the
+    device's FP64 issue rate (qsg_measure_fp64_rate)."""
+    if not fp64_per_segment or not peak:
+        return None
+    achieved = fp64_per_segment * segments_per_s_per_gpu
+    return {"achieved": achieved, "peak": peak, "unit": "FP64 warp instructions/s", "frac": achieved / peak,
+            "fp64_warp_instructions_per_segment": fp64_per_segment,
+            "peak_source": "measured in this run (qsg_measure_fp64_rate: independent DFMA chains, 16 warps/SM)",
+            "per_segment_source": "ncu sm__inst_executed_pipe_fp64.sum / segments, " + PROFILE_SUMMARY.name}
 
 
 def cpu_port_rate(deck_path: Path, cycles: int, threads: int):
@@ -585,6 +603,7 @@ def main():
     if rank != 0:
         return
 
+    fp64_peak = N.measure_fp64_rate(local)
     value = segments / track_s
     peak, peak_kind = measured_peak_hbm()
     seg_per_launch = segments / world / args.steps
@@ -603,7 +622,9 @@ def main():
                      "frac": achieved / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "traffic": (tps * seg_per_launch) if tps else None,
                      "algorithmic_bytes_per_segment": B_ALG_PER_SEGMENT,
-                     "note": "FP64-issue bound on GB300, see profiles/"},
+                     "note": "not HBM-bound: the binding roof is FP64 issue (fp64_issue)",
+                     "fp64_issue": fp64_roofline(profile_value("fp64_warp_instructions_per_segment"),
+                                                 seg_per_launch / (track_s / args.steps), fp64_peak)},
         "e2e": {"value": e2e_seg / e2e_s, "unit": "segments/s", "h2d_bytes_per_step": h2d // e2e_steps,
                 "d2h_bytes_per_step": d2h // e2e_steps,
                 "path": "qsg_track_host (the tracking launch reads the vault from and appends the census to "

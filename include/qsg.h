@@ -387,6 +387,13 @@ int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* particles, u
  * on a correct build). */
 int qsg_check_arithmetic(int32_t device, uint64_t n, uint64_t seed, uint64_t* mismatches);
 
+/* No reference counterpart: the FP64 issue rate of CUDA device `device`, in
+ * FP64 warp instructions per second, measured with independent multiply-add
+ * chains at 16 warps per SM (the best of two timed launches).  It is the roof
+ * of the tracking loop, whose binding resource is FP64 warp instructions: on
+ * this architecture their cost does not depend on how many lanes are active. */
+int qsg_measure_fp64_rate(int32_t device, double* warp_instructions_per_second);
+
 /* The reference's -DEXPONENTIAL_TALLY build (CycleTracking.cc:48-50) as a
  * run-time switch: before every segment one random number r is drawn from the
  * particle's stream and exp(r) added to its cell in a per-cell tally

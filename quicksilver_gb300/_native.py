@@ -125,6 +125,7 @@ _SIGNATURES = {
     "qsg_last_error": ([C.c_char_p, C.c_size_t], C.c_int),
     "qsg_device_count": ([C.POINTER(C.c_int)], C.c_int),
     "qsg_check_arithmetic": ([C.c_int32, C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
+    "qsg_measure_fp64_rate": ([C.c_int32, C.POINTER(C.c_double)], C.c_int),
     "qsg_create": ([C.POINTER(QsgProblem), C.POINTER(QsgOptions), C.POINTER(_VP)], C.c_int),
     "qsg_destroy": ([_VP], C.c_int),
     "qsg_set_particles": ([_VP, C.POINTER(QsgParticleSoA), C.c_uint64], C.c_int),
@@ -217,6 +218,13 @@ def check_arithmetic(n: int, seed: int = 1, device: int = 0) -> tuple:
     out = (C.c_uint64 * 4)()
     check(lib().qsg_check_arithmetic(device, n, seed, out))
     return tuple(int(v) for v in out)
+
+
+def measure_fp64_rate(device: int = 0) -> float:
+    """FP64 warp instructions per second the device issues (qsg_measure_fp64_rate)."""
+    out = C.c_double(0.0)
+    check(lib().qsg_measure_fp64_rate(device, C.byref(out)))
+    return out.value
 
 
 def soa_from_columns(cols: dict) -> QsgParticleSoA:

@@ -2663,3 +2663,74 @@ extern "C" int qsg_check_arithmetic(int32_t device, uint64_t n, uint64_t seed, u
     return QSG_OK;
     QSG_API_END
 }
+
+// ------------------------------------------------------------------------
+// FP64 issue rate of the device: the roof of the tracking loop, whose
+// binding resource is FP64 warp instructions (their cost does not depend on
+// how many lanes are active).
+
+namespace qsg {
+namespace {
+
+constexpr int kFp64ProbeBlock = 256;     // 8 warps; two blocks per SM keep the pipe saturated
+constexpr int kFp64ProbeChains = 4;      // independent multiply-add chains per thread
+
+__global__ void fp64_rate_kernel(int iters, double* out)
+{
+    double v[kFp64ProbeChains];
+#pragma unroll
+    for (int k = 0; k < kFp64ProbeChains; k++) v[k] = 1.0 + 1e-9 * (threadIdx.x + 1024 * k);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < kFp64ProbeChains; k++) v[k] = fma(v[k], 0.999999999, 1e-12);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < kFp64ProbeChains; k++) s += v[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+}  // namespace qsg
+
+extern "C" int qsg_measure_fp64_rate(int32_t device, double* warp_instructions_per_second)
+{
+    QSG_API_BEGIN
+    if (!warp_instructions_per_second) return fail(QSG_ERR_INVALID, "qsg_measure_fp64_rate: null argument");
+    int ndev = 0;
+    qsg_device_count(&ndev);
+    if (ndev == 0) return fail(QSG_ERR_NO_DEVICE, "qsg_measure_fp64_rate: no CUDA device visible");
+    if (device < 0 || device >= ndev)
+        return fail(QSG_ERR_INVALID, "qsg_measure_fp64_rate: device %d of %d", (int)device, ndev);
+    QSG_CUDA(cudaSetDevice(device));
+    int sms = 0;
+    QSG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    const int blocks = 2 * sms, iters = 20000;
+    qsg::DevBuf<double> out;
+    int st = out.alloc((size_t)blocks * qsg::kFp64ProbeBlock);
+    if (st) return st;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    float best_ms = 0.0f;
+    for (int rep = 0; rep < 3 && e == cudaSuccess; rep++) {   // the first launch warms up
+        e = cudaEventRecord(e0, 0);
+        if (e == cudaSuccess) {
+            qsg::fp64_rate_kernel<<<blocks, qsg::kFp64ProbeBlock>>>(iters, out.ptr);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(e1, 0);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess && rep > 0 && (best_ms == 0.0f || ms < best_ms)) best_ms = ms;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    out.free();
+    if (e != cudaSuccess) return fail(QSG_ERR_CUDA, "qsg_measure_fp64_rate: %s", cudaGetErrorString(e));
+    const double warp_instr = (double)blocks * (qsg::kFp64ProbeBlock / 32) * qsg::kFp64ProbeChains * iters;
+    *warp_instructions_per_second = warp_instr / (1e-3 * best_ms);
+    return QSG_OK;
+    QSG_API_END
+}

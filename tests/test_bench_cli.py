@@ -22,3 +22,14 @@ def test_reference_arm_json_line():
     assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "segments/s"
     assert line["warmup"] >= 3 and line["e2e"]["h2d_bytes_per_step"] == 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+
+
+def test_profile_figures_and_fp64_roofline():
+    sys.path.insert(0, str(ROOT))
+    import bench
+    assert bench.profile_traffic_per_segment() > 0
+    per_seg = bench.profile_value("fp64_warp_instructions_per_segment")
+    assert 1.0 < per_seg < 50.0
+    r = bench.fp64_roofline(per_seg, 2.0e9, 1.5e10)
+    assert abs(r["achieved"] - per_seg * 2.0e9) < 1.0 and abs(r["frac"] - r["achieved"] / 1.5e10) < 1e-12
+    assert bench.fp64_roofline(None, 2.0e9, 1.5e10) is None

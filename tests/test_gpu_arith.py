@@ -23,3 +23,13 @@ def test_check_arithmetic_arguments(gpu):
         N.check_arithmetic(16, device=N.device_count())
     assert ei.value.code == N.QSG_ERR_INVALID
     assert N.check_arithmetic(0) == (0, 0, 0, 0)
+
+
+def test_fp64_issue_rate_is_measured(gpu):
+    """The FP64 roof the bench reports the tracking kernel against: a few
+    times 1e10 FP64 warp instructions per second on a GB300-class part (one
+    per ~20 cycles per SM); anything far outside means the probe is broken."""
+    rate = N.measure_fp64_rate()
+    assert 1e9 < rate < 1e12
+    with pytest.raises(N.QsgError):
+        N.measure_fp64_rate(device=N.device_count())
