@@ -422,8 +422,10 @@ int qsg_read_cell_tally(QsgHandle* h, double* cell_tally);
  * handle with sensitivities on (QSG_ERR_UNSUPPORTED: scores do not travel
  * through host arrays).  More census particles than census_capacity: the
  * arrays hold the first census_capacity, the call returns QSG_ERR_CAPACITY
- * with the full count in *n_census.  Returns when the work on `stream` has
- * finished. */
+ * with the full count in *n_census.  The census arrays must not overlap the
+ * particle arrays (particles are still being read while census particles are
+ * appended); the particle arrays are only read, so a call can be repeated.
+ * Returns when the work on `stream` has finished. */
 int qsg_track_host(QsgHandle* h, const QsgParticleSoA* particles, uint64_t n, QsgParticleSoA* census,
                    uint64_t census_capacity, uint64_t* n_census, void* stream);
 
