@@ -2086,6 +2086,25 @@ extern "C" int qsg_get_census(QsgHandle* h, QsgParticleSoA* host, uint64_t cap, 
 
 namespace {
 
+// Whether any field array of `a` (n particles) overlaps any of `b` (m particles).
+bool soa_ranges_overlap(const QsgParticleSoA* a, uint64_t n, const QsgParticleSoA* b, uint64_t m)
+{
+    const void* fa[20] = {a->x, a->y, a->z, a->vx, a->vy, a->vz, a->kinetic_energy, a->weight, a->time_to_census,
+                          a->age, a->num_mean_free_paths, a->num_segments, a->random_number_seed, a->identifier,
+                          a->last_event, a->num_collisions, a->breed, a->species, a->domain, a->cell};
+    const void* fb[20] = {b->x, b->y, b->z, b->vx, b->vy, b->vz, b->kinetic_energy, b->weight, b->time_to_census,
+                          b->age, b->num_mean_free_paths, b->num_segments, b->random_number_seed, b->identifier,
+                          b->last_event, b->num_collisions, b->breed, b->species, b->domain, b->cell};
+    for (int i = 0; i < 20; i++) {
+        const uintptr_t a0 = (uintptr_t)fa[i], a1 = a0 + n * (i < 14 ? 8 : 4);
+        for (int j = 0; j < 20; j++) {
+            const uintptr_t b0 = (uintptr_t)fb[j], b1 = b0 + m * (j < 14 ? 8 : 4);
+            if (a0 < b1 && b0 < a1) return true;
+        }
+    }
+    return false;
+}
+
 // Device view of a caller's particle arrays for qsg_track_host: each field
 // must be page-locked host memory (cudaHostAlloc / cudaHostRegister, which the
 // GPU reads and writes over the host link) or device memory.
@@ -2127,10 +2146,12 @@ extern "C" int qsg_track_host(QsgHandle* h, const QsgParticleSoA* particles, uin
     if (h->sens.K > 0)
         return fail(QSG_ERR_UNSUPPORTED, "qsg_track_host: sensitivity scores do not travel through host arrays; "
                     "use qsg_set_particles / qsg_track_cycle");
-    int st = set_device(h);
-    if (st) return st;
     if (n == 0) return QSG_OK;
+    int st;
     if ((st = check_soa(particles)) || (st = check_soa(census))) return st;
+    if (soa_ranges_overlap(particles, n, census, census_capacity))
+        return fail(QSG_ERR_INVALID, "qsg_track_host: the census arrays overlap the particle arrays");
+    if ((st = set_device(h))) return st;
     PassStores ps;
     if ((st = device_soa_view(particles, "particles", ps.in)) || (st = device_soa_view(census, "census", ps.census)))
         return st;

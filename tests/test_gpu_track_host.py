@@ -87,6 +87,9 @@ def test_track_host_errors(gpu):
         assert ei.value.code == N.QSG_ERR_CAPACITY and "census_capacity" in str(ei.value)
         assert trk.device_status() & N.QSG_DEV_STORE_OVERFLOW
         assert trk.track_host(inp, 0, small, 64) == 0
+        with pytest.raises(N.QsgError) as ei:   # census written over the particles still being read
+            trk.track_host(inp, n, inp, n)
+        assert ei.value.code == N.QSG_ERR_INVALID and "overlap" in str(ei.value)
         trk.enable_sensitivity(band_params(hp.array("energies"), hp.num_materials))
         with pytest.raises(N.QsgError) as ei:
             trk.track_host(inp, n, _pinned(4 * n), 4 * n)
