@@ -164,6 +164,13 @@ int qsg_abi_version(void);
 int qsg_last_error(char* buf, size_t len);
 /* Number of visible CUDA devices (0 when none; never fails on a CPU host). */
 int qsg_device_count(int* count);
+/* The checks qsg_create makes on a problem before it touches a device (host
+ * only): tables present, indices in range, the 24-facet hex-cell convention
+ * (MC_Domain.cc:41-46), nuclear data, and the reference's mesh self-test
+ * consistencyCheck (initMC.cc:202-234): every facet's neighbour across leads
+ * back to it.  QSG_OK, or the first problem found (QSG_ERR_INVALID /
+ * QSG_ERR_UNSUPPORTED with a message). */
+int qsg_problem_check(const QsgProblem* problem);
 
 /* ---- tracking handle ----------------------------------------------------- */
 /* Copies every table into device memory owned by the handle

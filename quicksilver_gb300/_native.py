@@ -124,6 +124,7 @@ _SIGNATURES = {
     "qsg_abi_version": ([], C.c_int),
     "qsg_last_error": ([C.c_char_p, C.c_size_t], C.c_int),
     "qsg_device_count": ([C.POINTER(C.c_int)], C.c_int),
+    "qsg_problem_check": ([C.POINTER(QsgProblem)], C.c_int),
     "qsg_check_arithmetic": ([C.c_int32, C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
     "qsg_measure_fp64_rate": ([C.c_int32, C.POINTER(C.c_double)], C.c_int),
     "qsg_create": ([C.POINTER(QsgProblem), C.POINTER(QsgOptions), C.POINTER(_VP)], C.c_int),

@@ -1501,6 +1501,17 @@ int validate_problem(const QsgProblem* p)
                 return fail(QSG_ERR_INVALID, "problem: facet adjacency out of range");
         }
     }
+    // consistencyCheck (initMC.cc:202-234): the facet across from a facet
+    // leads back to it (a boundary facet is its own neighbour)
+    for (int64_t c = 0; c < C; c++)
+        for (int f = 0; f < kFacets; f++) {
+            const int64_t ac = p->facet_adjacent_cell[c * kFacets + f];
+            const int af = p->facet_adjacent_facet[c * kFacets + f];
+            if (p->facet_adjacent_cell[ac * kFacets + af] != c || p->facet_adjacent_facet[ac * kFacets + af] != f)
+                return fail(QSG_ERR_INVALID, "problem: facet adjacency not symmetric: cell %lld facet %d -> cell %lld "
+                            "facet %d, which leads to cell %d facet %d", (long long)c, f, (long long)ac, af,
+                            p->facet_adjacent_cell[ac * kFacets + af], p->facet_adjacent_facet[ac * kFacets + af]);
+        }
     return QSG_OK;
 }
 
@@ -1842,6 +1853,14 @@ int track_passes_sync(QsgHandle* h, cudaStream_t s)
 }  // namespace qsg
 
 using namespace qsg;
+
+extern "C" int qsg_problem_check(const QsgProblem* problem)
+{
+    QSG_API_BEGIN
+    if (!problem) return fail(QSG_ERR_INVALID, "qsg_problem_check: null problem");
+    return validate_problem(problem);
+    QSG_API_END
+}
 
 extern "C" int qsg_device_count(int* count)
 {

@@ -71,3 +71,24 @@ def test_new_entry_points_check_arguments_before_any_cuda_call(native_lib):
     assert lib.qsg_check_arithmetic(0, 16, 1, None) == N.QSG_ERR_INVALID
     out = (ctypes.c_uint64 * 4)()
     assert lib.qsg_check_arithmetic(-1, 16, 1, out) in (N.QSG_ERR_INVALID, N.QSG_ERR_NO_DEVICE)
+
+
+@pytest.mark.parametrize("name", ["t_homog.inp", "t_scatter_octant.inp", "t_nonflat.inp", "config1.inp"])
+def test_problem_check_accepts_built_decks(name):
+    hp = Deck.from_file(DECKS / name).build()
+    assert N.lib().qsg_problem_check(ctypes.byref(hp.view)) == N.QSG_OK, N.last_error()
+
+
+def test_problem_check_runs_the_reference_mesh_self_test():
+    """consistencyCheck (initMC.cc:202-234): a facet whose neighbour does not
+    lead back to it is rejected before any device is touched."""
+    hp = Deck.from_file(DECKS / "t_homog.inp").build()
+    view = N.QsgProblem.from_buffer_copy(hp.view)
+    adj = hp.array("facet_adjacent_facet").astype(np.int32).copy()
+    cells = hp.array("facet_adjacent_cell")
+    inner = int(np.nonzero(cells != np.repeat(np.arange(hp.num_cells), 24))[0][0])   # an interior facet
+    adj[inner] = (adj[inner] + 1) % 24
+    view.facet_adjacent_facet = adj.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    assert N.lib().qsg_problem_check(ctypes.byref(view)) == N.QSG_ERR_INVALID
+    assert "not symmetric" in N.last_error()
+    assert N.lib().qsg_problem_check(None) == N.QSG_ERR_INVALID
