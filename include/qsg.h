@@ -463,6 +463,13 @@ int qsg_deck_simulation(const QsgDeck* deck, QsgSimulation* out);
 /* The Simulation block's energySpectrum value (output file stem, "" when
  * absent; EnergySpectrum.cc:38-59 appends ".dat"). */
 int qsg_deck_energy_spectrum(const QsgDeck* deck, char* buf, size_t len);
+/* printParameters (Parameters.cc:97-215): the deck as the reference echoes it
+ * at start-up (Simulation, Geometry, Material and CrossSection blocks, with
+ * every default filled in, text for text).  It reads back as the same deck,
+ * except that, as in the reference, a sphere's radius is not printed and
+ * inputFile comes from the command line.  *needed receives the size with the
+ * terminating NUL; a NULL or short buffer gives QSG_ERR_CAPACITY. */
+int qsg_deck_write(const QsgDeck* deck, char* buf, size_t len, size_t* needed);
 
 /* Host-built problem tables (initNuclearData / initMesh restated,
  * initMC.cc:130-320, NuclearData.cc:12-187, MC_Domain.cc:77-394,

@@ -23,6 +23,8 @@
 //   QS_DUMP=<file>        write the binary dump there (format: see write_arr)
 //   QS_DUMP_TABLES=1      include problem tables
 //   QS_DUMP_PARTICLES=1   include initial and census particle records
+//   QS_ECHO=<file>        write the reference's start-up deck echo there
+//                         (QS_ECHO_ONLY=1: then stop)
 //   Built with -DEXPONENTIAL_TALLY (make -C oracle ref_exp) it also writes,
 //   per cycle, the reference's exponential cell tally.
 //
@@ -290,6 +292,13 @@ int main(int argc, char** argv)
 {
    mpiInit(&argc, &argv);
    Parameters params = getParameters(argc, argv);
+   if (const char* echo = getenv("QS_ECHO"))
+   {
+      // the reference's start-up echo of the deck (printParameters, Parameters.cc:97-215)
+      std::ofstream f(echo);
+      printParameters(params, f);
+      if (getenv("QS_ECHO_ONLY")) return 0;
+   }
    mcco = initMC(params);
 
    const char* theta = getenv("QS_THETA");

@@ -1,7 +1,8 @@
 """``python -m quicksilver_gb300 DECK [--nSteps N] [--key value ...]``
 
 Runs a Quicksilver input deck with every cycle on the GPU, the way the
-reference's driver does (main.cc:38-85): nSteps cycles of cycleInit /
+reference's driver does (main.cc:38-85): the deck echoed with every default
+filled in (printParameters, Parameters.cc:97-215), nSteps cycles of cycleInit /
 cycleTracking / cycleFinalize, one summary line per cycle with the balance
 counters, the scalar-flux total and the three phase times (the columns of
 Tallies::PrintSummary, Tallies.cc:122-144, Tallies.hh:60-76), then the
@@ -50,6 +51,7 @@ def main(argv=None) -> int:
     if args.exponential_tally:
         mc.exponential_tally(True)
     out = sys.stdout
+    out.write(deck.text() + "\n")
     out.write("%-8s " % "cycle" + " ".join("%12s" % h for h in HEADER) +
               " %14s %14s %14s %14s" % ("scalar_flux", "cycleInit", "cycleTracking", "cycleFinalize") +
               (" %14s" % "cell_tally" if args.exponential_tally else "") + "\n")

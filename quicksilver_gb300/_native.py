@@ -169,6 +169,7 @@ _SIGNATURES = {
     "qsg_deck_free": ([_VP], C.c_int),
     "qsg_deck_simulation": ([_VP, C.POINTER(QsgSimulation)], C.c_int),
     "qsg_deck_energy_spectrum": ([_VP, C.c_char_p, C.c_size_t], C.c_int),
+    "qsg_deck_write": ([_VP, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)], C.c_int),
     "qsg_set_observers": ([_VP, C.c_int32], C.c_int),
     "qsg_read_observers": ([_VP, _dp, _up], C.c_int),
     "qsg_deck_build": ([_VP, C.POINTER(_VP)], C.c_int),

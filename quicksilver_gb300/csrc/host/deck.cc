@@ -14,6 +14,7 @@
 #include <fstream>
 #include <sstream>
 #include <stdexcept>
+#include <type_traits>
 
 #include "status.h"
 
@@ -65,6 +66,16 @@ struct Block {
     {
         auto it = kv.find(key);
         if (it == kv.end()) return;
+        if constexpr (std::is_same<T, std::string>::value) {
+            // an empty string value: the reference's extraction fails and
+            // qs_assert (which only prints) leaves the value "" -- the same
+            // end result, taken here without the message, so that the
+            // start-up echo (which prints empty strings) reads back
+            if (it->second.find_first_not_of(" \t\r") == std::string::npos) {
+                out.clear();
+                return;
+            }
+        }
         std::istringstream in(it->second);
         T v{};
         in >> v;
@@ -140,6 +151,9 @@ void scan_simulation(const Block& b, SimulationSpec& s)
     b.get("cTally", s.cell_replications);
     b.get("coralBenchmark", s.coral_benchmark);
     b.get("energySpectrum", s.energy_spectrum);
+    b.get("crossSectionsOut", s.cross_sections_out);
+    b.get("cycleTimers", s.cycle_timers);
+    b.get("debugThreads", s.debug_threads);
 }
 
 void scan_geometry(const Block& b, Deck& d)
@@ -252,11 +266,102 @@ void set_simulation_key(Deck& deck, const std::string& key, const std::string& v
                                   "nParticles", "batchSize", "nBatches", "nSteps", "nx", "ny", "nz",
                                   "seed", "xDom", "yDom", "zDom", "eMax", "eMin", "nGroups",
                                   "lowWeightCutoff", "bTally", "fTally", "cTally", "coralBenchmark",
-                                  "energySpectrum"};
+                                  "energySpectrum", "crossSectionsOut", "cycleTimers", "debugThreads"};
     bool ok = false;
     for (const char* k : known) ok = ok || key == k;
     if (!ok) throw std::runtime_error("deck: unknown Simulation key '" + key + "'");
     scan_simulation(b, deck.sim);
+}
+
+// The operator<< overloads of Parameters.cc:121-215, block by block, with the
+// stream's default formatting, in the order printParameters writes them
+// (geometries in deck order, materials and cross sections sorted by name).
+// As there, a sphere's radius is not printed.
+std::string deck_text(const Deck& d)
+{
+    std::ostringstream out;
+    const SimulationSpec& s = d.sim;
+    out << "Simulation:\n";
+    out << "   dt: " << s.dt << "\n";
+    out << "   fMax: " << s.f_max << "\n";
+    out << "   inputFile: " << s.input_file << "\n";
+    out << "   energySpectrum: " << s.energy_spectrum << "\n";
+    out << "   boundaryCondition: " << s.boundary_condition << "\n";
+    out << "   loadBalance: " << s.load_balance << "\n";
+    out << "   cycleTimers: " << s.cycle_timers << "\n";
+    out << "   debugThreads: " << s.debug_threads << "\n";
+    out << "   lx: " << s.lx << "\n";
+    out << "   ly: " << s.ly << "\n";
+    out << "   lz: " << s.lz << "\n";
+    out << "   nParticles: " << s.n_particles << "\n";
+    out << "   batchSize: " << s.batch_size << "\n";
+    out << "   nBatches: " << s.n_batches << "\n";
+    out << "   nSteps: " << s.n_steps << "\n";
+    out << "   nx: " << s.nx << "\n";
+    out << "   ny: " << s.ny << "\n";
+    out << "   nz: " << s.nz << "\n";
+    out << "   seed: " << s.seed << "\n";
+    out << "   xDom: " << s.x_dom << "\n";
+    out << "   yDom: " << s.y_dom << "\n";
+    out << "   zDom: " << s.z_dom << "\n";
+    out << "   eMax: " << s.e_max << "\n";
+    out << "   eMin: " << s.e_min << "\n";
+    out << "   nGroups: " << s.n_groups << "\n";
+    out << "   lowWeightCutoff: " << s.low_weight_cutoff << "\n";
+    out << "   bTally: " << s.balance_replications << "\n";
+    out << "   fTally: " << s.flux_replications << "\n";
+    out << "   cTally: " << s.cell_replications << "\n";
+    out << "   coralBenchmark: " << s.coral_benchmark << "\n";
+    out << "   crossSectionsOut:" << s.cross_sections_out << "\n";
+    out << "\n";
+    for (const GeometrySpec& g : d.geometry) {
+        out << "Geometry:\n";
+        out << "   material: " << g.material << "\n";
+        if (g.shape == GeometrySpec::BRICK) {
+            out << "   shape: brick\n";
+            out << "   xMax: " << g.x_max << "\n";
+            out << "   xMin: " << g.x_min << "\n";
+            out << "   yMax: " << g.y_max << "\n";
+            out << "   yMin: " << g.y_min << "\n";
+            out << "   zMax: " << g.z_max << "\n";
+            out << "   zMin: " << g.z_min << "\n";
+        } else {
+            out << "   shape: sphere\n";
+            out << "   xCenter: " << g.x_center << "\n";
+            out << "   yCenter: " << g.y_center << "\n";
+            out << "   zCenter: " << g.z_center << "\n";
+        }
+        out << "\n";
+    }
+    for (const auto& kv : d.materials) {
+        const MaterialSpec& m = kv.second;
+        out << "Material:\n";
+        out << "   name: " << m.name << "\n";
+        out << "   mass: " << m.mass << "\n";
+        out << "   nIsotopes: " << m.n_isotopes << "\n";
+        out << "   nReactions: " << m.n_reactions << "\n";
+        out << "   sourceRate: " << m.source_rate << "\n";
+        out << "   totalCrossSection: " << m.total_cross_section << "\n";
+        out << "   absorptionCrossSection: " << m.absorption_cross_section << "\n";
+        out << "   fissionCrossSection: " << m.fission_cross_section << "\n";
+        out << "   scatteringCrossSection: " << m.scattering_cross_section << "\n";
+        out << "   absorptionCrossSectionRatio: " << m.absorption_ratio << "\n";
+        out << "   fissionCrossSectionRatio: " << m.fission_ratio << "\n";
+        out << "   scatteringCrossSectionRatio: " << m.scattering_ratio << "\n";
+        out << "\n";
+    }
+    for (const auto& kv : d.cross_sections) {
+        const CrossSectionSpec& x = kv.second;
+        out << "CrossSection:\n";
+        out << "   name: " << x.name << "\n";
+        out << "   A: " << x.aa << "\n";
+        out << "   B: " << x.bb << "\n";
+        out << "   C: " << x.cc << "\n";
+        out << "   D: " << x.dd << "\n";
+        out << "   E: " << x.ee << "\n";
+        out << "   nuBar: " << x.nu_bar << "\n";
+    }
+    return out.str();
 }
 
 int boundary_condition_code(const std::string& bc)
@@ -296,7 +401,22 @@ extern "C" int qsg_deck_parse_file(const char* path, QsgDeck** out)
     std::stringstream ss;
     ss << in.rdbuf();
     std::string text = ss.str();
-    return qsg_deck_parse_string(text.c_str(), out);
+    const int st = qsg_deck_parse_string(text.c_str(), out);
+    if (st == QSG_OK) (*out)->deck.sim.input_file = path;
+    return st;
+    QSG_API_END
+}
+
+extern "C" int qsg_deck_write(const QsgDeck* deck, char* buf, size_t len, size_t* needed)
+{
+    QSG_API_BEGIN
+    if (!deck) return qsg::fail(QSG_ERR_INVALID, "qsg_deck_write: null deck");
+    const std::string text = qsg::deck_text(deck->deck);
+    if (needed) *needed = text.size() + 1;
+    if (!buf || len < text.size() + 1)
+        return qsg::fail(QSG_ERR_CAPACITY, "qsg_deck_write: the deck text needs %zu bytes", text.size() + 1);
+    memcpy(buf, text.c_str(), text.size() + 1);
+    return QSG_OK;
     QSG_API_END
 }
 

@@ -37,8 +37,11 @@ struct CrossSectionSpec {      // CrossSectionParameters, Parameters.hh:76-95
 };
 
 struct SimulationSpec {        // SimulationParameters, Parameters.hh:97-167
+    std::string input_file;        // the deck file read (qsg_deck_parse_file)
     std::string boundary_condition = "reflect";
     std::string energy_spectrum;   // output file stem of the census energy spectrum ("" = none)
+    std::string cross_sections_out;  // kept and echoed; this library writes no cross-section file
+    int cycle_timers = 0, debug_threads = 0;   // kept and echoed (no effect here)
     int load_balance = 0;
     uint64_t n_particles = 1000000;
     uint64_t batch_size = 0;
@@ -71,6 +74,8 @@ void parse_deck_text(const std::string& text, Deck& deck);
 void supply_defaults(Deck& deck);
 // Apply one Simulation key (command-line override); throws on bad value.
 void set_simulation_key(Deck& deck, const std::string& key, const std::string& value);
+// printParameters, Parameters.cc:97-215: the deck as the reference echoes it.
+std::string deck_text(const Deck& deck);
 int boundary_condition_code(const std::string& bc);
 
 }  // namespace qsg

@@ -57,6 +57,15 @@ class Deck:
         N.check(N.lib().qsg_deck_energy_spectrum(self._h, buf, len(buf)))
         return buf.value.decode()
 
+    def text(self) -> str:
+        """The deck as the reference echoes it at start-up (printParameters,
+        Parameters.cc:97-215), defaults filled in."""
+        need = C.c_size_t(0)
+        N.lib().qsg_deck_write(self._h, None, 0, C.byref(need))
+        buf = C.create_string_buffer(need.value)
+        N.check(N.lib().qsg_deck_write(self._h, buf, len(buf), C.byref(need)))
+        return buf.value.decode()
+
     def build(self) -> "HostProblem":
         h = C.c_void_p()
         N.check(N.lib().qsg_deck_build(self._h, C.byref(h)))

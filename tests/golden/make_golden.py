@@ -23,7 +23,11 @@ tallied per cell, CycleTracking.cc:48-50) and stores ``exp_<deck>.npz``:
 ``balance``, ``flux_cell``, ``flux_total``, ``census_sha`` / ``census_n`` and
 ``cell_tally`` [cycles, cells] (gid order) for t_homog and t_fission by default.
 
-Usage: python tests/golden/make_golden.py [--exponential-tally] [deck ...]
+With ``--echo`` it stores the reference's start-up echo of every deck in
+quicksilver_gb300/decks (printParameters, Parameters.cc:97-215) in
+``deck_echo.npz`` (one string per deck stem).
+
+Usage: python tests/golden/make_golden.py [--exponential-tally | --echo] [deck ...]
 """
 from __future__ import annotations
 
@@ -175,8 +179,28 @@ def make_exp(deck: Path, workdir: Path) -> None:
           f"cell tally total {out['cell_tally'].sum():.6e}")
 
 
+def make_echo(names: list[str], workdir: Path) -> None:
+    out = {}
+    for name in names:
+        deck = (DECKS / f"{name}.inp").relative_to(ROOT)   # the echo records the path it was given
+        echo = workdir / f"{name}.echo"
+        env = dict(os.environ, QS_ECHO=str(echo), QS_ECHO_ONLY="1")
+        res = subprocess.run([str(HARNESS), "-i", str(deck)], env=env, cwd=ROOT, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise SystemExit(f"reference run failed on {deck}:\n{res.stderr[-4000:]}")
+        out[name] = np.array(echo.read_text())
+    np.savez_compressed(HERE / "deck_echo.npz", **out)
+    print(f"deck_echo.npz: {len(out)} decks")
+
+
 def main(argv: list[str]) -> None:
     import tempfile
+    if "--echo" in argv:
+        ensure_harness("ref")
+        names = [a for a in argv if a != "--echo"] or sorted(p.stem for p in DECKS.glob("*.inp"))
+        with tempfile.TemporaryDirectory() as tmp:
+            make_echo(names, Path(tmp))
+        return
     exp = "--exponential-tally" in argv
     argv = [a for a in argv if a != "--exponential-tally"]
     ensure_harness("ref_exp" if exp else "ref")

@@ -8,7 +8,7 @@ import pytest
 from helpers import DECKS, load_problem
 
 GOLDEN = DECKS.parent.parent / "tests" / "golden"
-NAMES = sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("exp_"))   # exp_*: no tables
+NAMES = sorted(p.stem for p in GOLDEN.glob("*.npz") if (DECKS / f"{p.stem}.inp").exists())   # per-deck fixtures
 
 
 def _sha(a):
