@@ -25,6 +25,8 @@
 //   QS_DUMP_PARTICLES=1   include initial and census particle records
 //   QS_ECHO=<file>        write the reference's start-up deck echo there
 //                         (QS_ECHO_ONLY=1: then stop)
+//   QS_INIT_ONLY=1        stop after initMC (which writes the crossSectionsOut
+//                         file when the deck or -S names one)
 //   Built with -DEXPONENTIAL_TALLY (make -C oracle ref_exp) it also writes,
 //   per cycle, the reference's exponential cell tally.
 //
@@ -300,6 +302,7 @@ int main(int argc, char** argv)
       if (getenv("QS_ECHO_ONLY")) return 0;
    }
    mcco = initMC(params);
+   if (getenv("QS_INIT_ONLY")) return 0;   // e.g. for initMC's crossSectionsOut file only
 
    const char* theta = getenv("QS_THETA");
    if (theta && theta[0]) apply_theta(theta);

@@ -23,7 +23,7 @@ import time
 
 from . import _native as N
 from .monte_carlo import MonteCarlo
-from .observe import coral_benchmark_correctness, cumulative_balance, write_energy_spectrum
+from .observe import coral_benchmark_correctness, cumulative_balance, write_cross_sections, write_energy_spectrum
 from .problem import Deck
 
 COLUMNS = ["start", "source", "rr", "split", "absorb", "scatter", "fission", "produce", "collision", "escape",
@@ -52,6 +52,8 @@ def main(argv=None) -> int:
         mc.exponential_tally(True)
     out = sys.stdout
     out.write(deck.text() + "\n")
+    if deck.cross_sections_out:   # written by initMC in the reference (initMC.cc:392-490)
+        write_cross_sections(deck.cross_sections_out, mc.problem, deck.material_names)
     out.write("%-8s " % "cycle" + " ".join("%12s" % h for h in HEADER) +
               " %14s %14s %14s %14s" % ("scalar_flux", "cycleInit", "cycleTracking", "cycleFinalize") +
               (" %14s" % "cell_tally" if args.exponential_tally else "") + "\n")

@@ -38,6 +38,9 @@ QSG_DEV_BAD_FACET = 1 << 5
 QSG_DEV_NEGATIVE_DISTANCE = 1 << 6
 QSG_DEV_PASS_LIMIT = 1 << 7
 
+# NuclearDataReaction::Enum (NuclearData.hh:33-40), QSG_REACT_* in qsg.h
+QSG_REACT_SCATTER, QSG_REACT_ABSORPTION, QSG_REACT_FISSION = 1, 2, 3
+
 BALANCE_FIELDS = ("absorb", "census", "escape", "collision", "end", "fission", "produce",
                   "scatter", "start", "source", "rr", "split", "num_segments")
 BAL = {name: i for i, name in enumerate(BALANCE_FIELDS)}

@@ -120,3 +120,44 @@ def write_energy_spectrum(stem: str, energies: np.ndarray, counts: np.ndarray) -
         for i, (e, c) in enumerate(zip(energies, counts)):
             fh.write(f"{i}\t{float(e):g}\t{int(c)}\n")
     return path
+
+
+def cross_section_table(hp, material_names) -> str:
+    """The file the reference writes when the deck sets crossSectionsOut
+    (initMC.cc:392-490): per energy group its midpoint energy and, for every
+    material in name order, the absorption, fission and scatter microscopic
+    cross sections summed over the material's isotopes and their reactions,
+    each divided by the isotope count (accumulated in the same order: isotope,
+    reaction, group).  `material_names`: the materials in this problem's
+    order, which is name order."""
+    e = hp.array("energies")
+    G = len(e) - 1
+    iso_off = hp.array("isotope_reaction_offset")
+    rtype = hp.array("reaction_type")
+    xs = hp.array("reaction_xs").reshape(-1, G)
+    mat_off = hp.array("material_isotope_offset")
+    gid = hp.array("material_isotope_gid")
+    kind = {N.QSG_REACT_ABSORPTION: 0, N.QSG_REACT_FISSION: 1, N.QSG_REACT_SCATTER: 2}
+    table = []
+    for m in range(len(material_names)):
+        isos = gid[mat_off[m]:mat_off[m + 1]]
+        acc = np.zeros((3, G))
+        for iso in isos:
+            for r in range(iso_off[iso], iso_off[iso + 1]):
+                acc[kind[int(rtype[r])]] += xs[r] / float(len(isos))
+        table.append(acc)
+    order = sorted(range(len(material_names)), key=lambda m: material_names[m])
+    energy = (e[:-1] + e[1:]) / 2.0
+    lines = ["#group  energy" + "".join("  %s_a  %s_f  %s_s" % ((material_names[m],) * 3) for m in order)]
+    for g in range(G):
+        lines.append("%u  %g" % (g, energy[g]) +
+                     "".join("  %g  %g  %g" % (table[m][0, g], table[m][1, g], table[m][2, g]) for m in order))
+    return "\n".join(lines) + "\n"
+
+
+def write_cross_sections(stem: str, hp, material_names) -> str:
+    """Write cross_section_table to <stem>.dat, as the reference does; returns the path."""
+    path = stem + ".dat"
+    with open(path, "w") as f:
+        f.write(cross_section_table(hp, material_names))
+    return path

@@ -66,6 +66,26 @@ class Deck:
         N.check(N.lib().qsg_deck_write(self._h, buf, len(buf), C.byref(need)))
         return buf.value.decode()
 
+    def _echo_values(self, block: str, key: str) -> list:
+        out, cur = [], None
+        for line in self.text().splitlines():
+            if line and not line.startswith(" "):
+                cur = line.rstrip(":")
+            elif cur == block and line.strip().startswith(key + ":"):
+                out.append(line.split(":", 1)[1].strip())
+        return out
+
+    @property
+    def material_names(self) -> list:
+        """The materials in name order -- the order of the built problem's materials."""
+        return self._echo_values("Material", "name")
+
+    @property
+    def cross_sections_out(self) -> str:
+        """The Simulation block's crossSectionsOut file stem ("" when absent)."""
+        vals = self._echo_values("Simulation", "crossSectionsOut")
+        return vals[0] if vals else ""
+
     def build(self) -> "HostProblem":
         h = C.c_void_p()
         N.check(N.lib().qsg_deck_build(self._h, C.byref(h)))

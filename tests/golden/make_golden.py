@@ -27,7 +27,11 @@ With ``--echo`` it stores the reference's start-up echo of every deck in
 quicksilver_gb300/decks (printParameters, Parameters.cc:97-215) in
 ``deck_echo.npz`` (one string per deck stem).
 
-Usage: python tests/golden/make_golden.py [--exponential-tally | --echo] [deck ...]
+With ``--xsec`` it stores the file the reference's initMC writes for
+``-S <stem>`` (crossSectionsOut, initMC.cc:392-490) for a few decks in
+``xsec_out.npz``.
+
+Usage: python tests/golden/make_golden.py [--exponential-tally | --echo | --xsec] [deck ...]
 """
 from __future__ import annotations
 
@@ -193,8 +197,28 @@ def make_echo(names: list[str], workdir: Path) -> None:
     print(f"deck_echo.npz: {len(out)} decks")
 
 
+def make_xsec(names: list[str], workdir: Path) -> None:
+    out = {}
+    for name in names:
+        deck = DECKS / f"{name}.inp"
+        env = dict(os.environ, QS_INIT_ONLY="1")
+        res = subprocess.run([str(HARNESS), "-i", str(deck), "-S", "xsout"], env=env, cwd=workdir,
+                             capture_output=True, text=True)
+        if res.returncode != 0:
+            raise SystemExit(f"reference run failed on {deck}:\n{res.stderr[-4000:]}")
+        out[name] = np.array((workdir / "xsout.dat").read_text())
+    np.savez_compressed(HERE / "xsec_out.npz", **out)
+    print(f"xsec_out.npz: {len(out)} decks")
+
+
 def main(argv: list[str]) -> None:
     import tempfile
+    if "--xsec" in argv:
+        ensure_harness("ref")
+        names = [a for a in argv if a != "--xsec"] or ["t_homog", "t_nonflat", "t_fission", "config2", "config4"]
+        with tempfile.TemporaryDirectory() as tmp:
+            make_xsec(names, Path(tmp))
+        return
     if "--echo" in argv:
         ensure_harness("ref")
         names = [a for a in argv if a != "--echo"] or sorted(p.stem for p in DECKS.glob("*.inp"))
