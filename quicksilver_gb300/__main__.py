@@ -33,6 +33,7 @@ HEADER = ["start", "source", "rr", "split", "absorb", "scatter", "fission", "pro
 
 
 def main(argv=None) -> int:
+    t_main = time.perf_counter()   # MC_Fast_Timer::main covers the whole run
     ap = argparse.ArgumentParser(prog="python -m quicksilver_gb300", description=__doc__.split("\n\n")[1])
     ap.add_argument("deck")
     ap.add_argument("--exponential-tally", action="store_true",
@@ -54,10 +55,12 @@ def main(argv=None) -> int:
     out.write(deck.text() + "\n")
     if deck.cross_sections_out:   # written by initMC in the reference (initMC.cc:392-490)
         write_cross_sections(deck.cross_sections_out, mc.problem, deck.material_names)
+    # Tallies::PrintSummary's layout (Tallies.cc:122-144, Tallies.hh:60-76)
     out.write("%-8s " % "cycle" + " ".join("%12s" % h for h in HEADER) +
-              " %14s %14s %14s %14s" % ("scalar_flux", "cycleInit", "cycleTracking", "cycleFinalize") +
+              "%14s %14s %14s %14s" % ("scalar_flux", "cycleInit", "cycleTracking", "cycleFinalize") +
               (" %14s" % "cell_tally" if args.exponential_tally else "") + "\n")
     track_s = 0.0
+    clock = {name: [0, 0.0] for name in TIMERS}   # calls, seconds
     for cycle in range(sim.n_steps):
         t0 = time.perf_counter()
         mc.cycle_init()
@@ -72,17 +75,21 @@ def main(argv=None) -> int:
         row = mc.history(cycle, 1)
         t3 = time.perf_counter()
         track_s += t2 - t1
+        for name, dt in (("cycleInit", t1 - t0), ("cycleTracking", t2 - t1), ("cycleTracking_Kernel", t2 - t1),
+                         ("cycleFinalize", t3 - t2)):
+            clock[name][0] += 1
+            clock[name][1] += dt
         bal = row.balance[0]
         out.write("%8d " % cycle + " ".join("%12d" % int(bal[N.BAL[c]]) for c in COLUMNS) +
-                  " %14e %14e %14e %14e" % (row.flux_total[0], t1 - t0, t2 - t1, t3 - t2) +
+                  "%14e %14e %14e %14e" % (row.flux_total[0], t1 - t0, t2 - t1, t3 - t2) +
                   (" %14e" % cell_total if cell_total is not None else "") + "\n")
     flags = mc.device_status()
     if flags:
         raise N.QsgError(N.QSG_ERR_DEVICE, f"device flags 0x{flags:x} raised during the run")
     hist = mc.history(0, sim.n_steps)
     cum = cumulative_balance(hist.balance)
-    out.write(f"\nFigure of merit: {cum['num_segments'] / track_s:.4e} segments/s "
-              f"({cum['num_segments']} segments, {track_s:.3f} s of tracking)\n")
+    clock["main"] = [1, time.perf_counter() - t_main]
+    timer_report(out, clock, cum["num_segments"])
     if spectrum_stem:
         path = write_energy_spectrum(spectrum_stem, mc.problem.array("energies"), mc.energy_spectrum()[0])
         out.write(f"energy spectrum written to {path}\n")
@@ -90,6 +97,32 @@ def main(argv=None) -> int:
         coral_benchmark_correctness(cum, mc.fluence(), sim.coral_benchmark, out)
     mc.close()
     return 0
+
+
+# MC_Fast_Timer's timers (MC_Fast_Timer.hh:31-41, MC_Fast_Timer.cc:8-17); one
+# process and one domain: no particle exchange, so the MPI and test-for-done
+# timers are never started
+TIMERS = ["main", "cycleInit", "cycleTracking", "cycleTracking_Kernel", "cycleTracking_MPI",
+          "cycleTracking_Test_Done", "cycleFinalize"]
+
+
+def timer_report(out, clock: dict, num_segments: int) -> None:
+    """MC_Fast_Timer_Container::Cumulative_Report (MC_Fast_Timer.cc:45-104)
+    for one rank: microseconds per timer (min = avg = max, no spread) and the
+    figure of merit, segments per second of cycleTracking."""
+    out.write("\n%-25s %12s %12s %12s %12s %12s %12s\n" % ("Timer", "Cumulative", "Cumulative", "Cumulative",
+                                                          "Cumulative", "Cumulative", "Cumulative"))
+    out.write("%-25s %12s %12s %12s %12s %12s %12s\n" % ("Name", "number", "microSecs", "microSecs", "microSecs",
+                                                        "microSecs", "Efficiency"))
+    out.write("%-25s %12s %12s %12s %12s %12s %12s\n" % ("", "of calls", "min", "avg", "max", "stddev", "Rating"))
+    for name in TIMERS:
+        calls, secs = clock.get(name, [0, 0.0])
+        us = float(int(secs * 1e6))   # the reference keeps whole microseconds
+        out.write("%-25s %12d %12.3e %12.3e %12.3e %12.3e %12.2f\n" %
+                  (name, calls, us, us, us, 0.0, 100.0 * us / (us + 1.0e-80)))
+    track_us = float(int(clock["cycleTracking"][1] * 1e6))
+    out.write("%-25s %12.3e %-25s\n" % ("Figure Of Merit", num_segments / (track_us * 1e-6),
+                                         "[Num Segments / Cycle Tracking Time]"))
 
 
 def mc_sync(tracker) -> None:

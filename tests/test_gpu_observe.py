@@ -63,7 +63,8 @@ def test_gpu_command_line_driver(gpu, tmp_path):
                           "--energySpectrum", str(stem)], cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert res.returncode == 0, res.stderr
     out = res.stdout
-    assert "Figure of merit" in out and "PASS:: No Particles Lost During Run" in out
+    assert "Figure Of Merit" in out and "[Num Segments / Cycle Tracking Time]" in out
+    assert "PASS:: No Particles Lost During Run" in out
     assert "PASS:: Absorption / Fission / Scatter Ratios maintained" in out
     rows = [l.split() for l in out.splitlines() if l.strip() and l.split()[0].isdigit()]
     assert len(rows) == Deck.from_file(DECKS / "t_coral1.inp").simulation.n_steps
