@@ -25,6 +25,7 @@
 //   QS_DUMP_PARTICLES=1   include initial and census particle records
 //   QS_ECHO=<file>        write the reference's start-up deck echo there
 //                         (QS_ECHO_ONLY=1: then stop)
+//   QS_PRINT_SPECTRUM=1   print the energy spectrum file after the last cycle
 //   QS_INIT_ONLY=1        stop after initMC (which writes the crossSectionsOut
 //                         file when the deck or -S names one)
 //   Built with -DEXPONENTIAL_TALLY (make -C oracle ref_exp) it also writes,
@@ -383,6 +384,9 @@ int main(int argc, char** argv)
       cycleFinalize();
    }
    write_d("track_seconds", track_seconds);
+   // the census energy spectrum file (EnergySpectrum.cc:38-59), which the
+   // reference's gameOver prints when energySpectrum (-e) is set
+   if (getenv("QS_PRINT_SPECTRUM")) mcco->_tallies->_spectrum.PrintSpectrum(mcco);
    double tsum = 0;
    for (double s : track_seconds) tsum += s;
    fprintf(stderr, "qs_ref_harness: segments=%llu tracking_s=%.6f FOM=%.6e seg/s\n",

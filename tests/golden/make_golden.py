@@ -31,7 +31,11 @@ With ``--xsec`` it stores the file the reference's initMC writes for
 ``-S <stem>`` (crossSectionsOut, initMC.cc:392-490) for a few decks in
 ``xsec_out.npz``.
 
-Usage: python tests/golden/make_golden.py [--exponential-tally | --echo | --xsec] [deck ...]
+With ``--spectrum`` it stores the census energy spectrum file the reference
+prints for ``-e <stem>`` (EnergySpectrum.cc:38-59) after all cycles of a few
+decks in ``spectrum_out.npz``.
+
+Usage: python tests/golden/make_golden.py [--exponential-tally | --echo | --xsec | --spectrum] [deck ...]
 """
 from __future__ import annotations
 
@@ -211,8 +215,28 @@ def make_xsec(names: list[str], workdir: Path) -> None:
     print(f"xsec_out.npz: {len(out)} decks")
 
 
+def make_spectrum(names: list[str], workdir: Path) -> None:
+    out = {}
+    for name in names:
+        deck = DECKS / f"{name}.inp"
+        env = dict(os.environ, QS_PRINT_SPECTRUM="1", OMP_NUM_THREADS="8")
+        res = subprocess.run([str(HARNESS), "-i", str(deck), "-e", "spec"], env=env, cwd=workdir,
+                             capture_output=True, text=True)
+        if res.returncode != 0:
+            raise SystemExit(f"reference run failed on {deck}:\n{res.stderr[-4000:]}")
+        out[name] = np.array((workdir / "spec.dat").read_text())
+    np.savez_compressed(HERE / "spectrum_out.npz", **out)
+    print(f"spectrum_out.npz: {len(out)} decks")
+
+
 def main(argv: list[str]) -> None:
     import tempfile
+    if "--spectrum" in argv:
+        ensure_harness("ref")
+        names = [a for a in argv if a != "--spectrum"] or ["t_homog", "t_fission", "t_nonflat"]
+        with tempfile.TemporaryDirectory() as tmp:
+            make_spectrum(names, Path(tmp))
+        return
     if "--xsec" in argv:
         ensure_harness("ref")
         names = [a for a in argv if a != "--xsec"] or ["t_homog", "t_nonflat", "t_fission", "config2", "config4"]
