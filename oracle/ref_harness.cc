@@ -26,6 +26,7 @@
 //   QS_ECHO=<file>        write the reference's start-up deck echo there
 //                         (QS_ECHO_ONLY=1: then stop)
 //   QS_PRINT_SPECTRUM=1   print the energy spectrum file after the last cycle
+//   QS_CORAL=1            run coralBenchmarkCorrectness after the last cycle
 //   QS_INIT_ONLY=1        stop after initMC (which writes the crossSectionsOut
 //                         file when the deck or -S names one)
 //   Built with -DEXPONENTIAL_TALLY (make -C oracle ref_exp) it also writes,
@@ -58,6 +59,7 @@
 #include "MC_RNG_State.hh"
 #include "MC_Time_Info.hh"
 #include "utilsMpi.hh"
+#include "CoralBenchmark.hh"
 
 extern MonteCarlo* mcco;
 void cycleInit(bool loadBalance);
@@ -387,6 +389,8 @@ int main(int argc, char** argv)
    // the census energy spectrum file (EnergySpectrum.cc:38-59), which the
    // reference's gameOver prints when energySpectrum (-e) is set
    if (getenv("QS_PRINT_SPECTRUM")) mcco->_tallies->_spectrum.PrintSpectrum(mcco);
+   // the CORAL2 correctness checks main.cc runs after the cycles (to stdout)
+   if (getenv("QS_CORAL")) coralBenchmarkCorrectness(mcco, params);
    double tsum = 0;
    for (double s : track_seconds) tsum += s;
    fprintf(stderr, "qs_ref_harness: segments=%llu tracking_s=%.6f FOM=%.6e seg/s\n",

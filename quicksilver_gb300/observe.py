@@ -33,38 +33,56 @@ def cumulative_balance(history_balance: np.ndarray) -> dict:
     return {name: int(tot[i]) for name, i in B.items()}
 
 
+def _c_div(a, b) -> np.float64:
+    """a / b as C evaluates it in double (x/0 = +-inf, 0/0 = nan)."""
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.float64(a) / np.float64(b)
+
+
 def balance_ratio_test(bal: dict, coral_benchmark: int):
-    """BalanceRatioTest (CoralBenchmark.cc:46-118)."""
+    """BalanceRatioTest (CoralBenchmark.cc:46-118): the six relative ratios in
+    C double arithmetic (a zero count gives inf, or nan, which passes, as
+    there) and the reference's lines."""
     if coral_benchmark not in CORAL_RATIOS:
         raise ValueError(f"coralBenchmark must be 1 or 2, not {coral_benchmark}")
     absorb_r, fission_r, scatter_r, pct = CORAL_RATIOS[coral_benchmark]
     tol = pct / 100.0
-    a, f, s = float(bal["absorb"]), float(bal["fission"]), float(bal["scatter"])
+    a, f, s = int(bal["absorb"]), int(bal["fission"]), int(bal["scatter"])
     with np.errstate(divide="ignore", invalid="ignore"):
         rel = {
-            "Absorb to Scatter": abs((a / absorb_r) * (scatter_r / s) - 1) if s else np.inf,
-            "Absorb to Fission": abs((a / absorb_r) * (fission_r / f) - 1) if f else np.inf,
-            "Scatter to Absorb": abs((s / scatter_r) * (absorb_r / a) - 1) if a else np.inf,
-            "Scatter to Fission": abs((s / scatter_r) * (fission_r / f) - 1) if f else np.inf,
-            "Fission to Absorb": abs((f / fission_r) * (absorb_r / a) - 1) if a else np.inf,
-            "Fission to Scatter": abs((f / fission_r) * (scatter_r / s) - 1) if s else np.inf,
+            "Absorb to Scatter": abs(_c_div(a, absorb_r) * _c_div(scatter_r, s) - 1),
+            "Absorb to Fission": abs(_c_div(a, absorb_r) * _c_div(fission_r, f) - 1),
+            "Scatter to Absorb": abs(_c_div(s, scatter_r) * _c_div(absorb_r, a) - 1),
+            "Scatter to Fission": abs(_c_div(s, scatter_r) * _c_div(fission_r, f) - 1),
+            "Fission to Absorb": abs(_c_div(f, fission_r) * _c_div(absorb_r, a) - 1),
+            "Fission to Scatter": abs(_c_div(f, fission_r) * _c_div(scatter_r, s) - 1),
         }
-    ok = all(v <= tol for v in rel.values())
-    msg = (f"PASS:: Absorption / Fission / Scatter Ratios maintained with {tol * 100:g}% tolerance" if ok else
-           f"FAIL:: Absorption / Fission / Scatter Ratios NOT maintained with {tol * 100:g}% tolerance\n" +
-           "\n".join(f"Relative {k}:  {v:g} < {tol:g}" for k, v in rel.items()))
+    ok = not any(v > tol for v in rel.values())
+    if ok:
+        msg = "PASS:: Absorption / Fission / Scatter Ratios maintained with %g%% tolerance" % (tol * 100.0)
+    else:
+        labels = {"Absorb to Scatter": "Absorb to Scatter:  ", "Absorb to Fission": "Absorb to Fission:  ",
+                  "Scatter to Absorb": "Scatter to Absorb:  ", "Scatter to Fission": "Scatter to Fission: ",
+                  "Fission to Absorb": "Fission to Absorb:  ", "Fission to Scatter": "Fission to Scatter: "}
+        msg = "\n".join(["FAIL:: Absorption / Fission / Scatter Ratios NOT maintained with %g%% tolerance" %
+                         (tol * 100.0),
+                         "absorb:  %12d\t%g" % (a, absorb_r), "scatter: %12d\t%g" % (s, scatter_r),
+                         "fission: %12d\t%g" % (f, fission_r)] +
+                        ["Relative %s%g < %g" % (labels[k], v, tol) for k, v in rel.items()])
     return ok, msg, rel
 
 
 def balance_event_test(bal: dict):
     """BalanceEventTest (CoralBenchmark.cc:120-152): facet crossings
-    (segments - census - collisions) within 1% of the collisions."""
-    facet = bal["num_segments"] - bal["census"] - bal["collision"]
-    ratio = abs(facet / bal["collision"] - 1) if bal["collision"] else np.inf
-    ok = ratio <= 0.01
-    msg = ("PASS:: Collision to Facet Crossing Ratio maintained even balanced within 1% tolerance" if ok else
-           f" FAIL:: Collision to Facet Crossing Ratio balanced NOT maintained within 1% tolerance\n"
-           f"\tFacet Crossing: {facet}\tCollision: {bal['collision']}\tRatio: {ratio:g}")
+    (segments - census - collisions, as uint64) within 1% of the collisions."""
+    facet = (int(bal["num_segments"]) - int(bal["census"]) - int(bal["collision"])) % (1 << 64)
+    ratio = abs(_c_div(facet, int(bal["collision"])) - 1)
+    tolerance = 1.0
+    ok = not (ratio > tolerance / 100.0)
+    msg = ("PASS:: Collision to Facet Crossing Ratio maintained even balanced within %g%% tolerance" % tolerance
+           if ok else
+           " FAIL:: Collision to Facet Crossing Ratio balanced NOT maintained within %g%% tolerance\n"
+           "\tFacet Crossing: %d\tCollision: %d\tRatio: %g" % (tolerance, facet, int(bal["collision"]), ratio))
     return ok, msg, ratio
 
 
@@ -81,16 +99,23 @@ def missing_particle_test(bal: dict):
 
 def fluence_test(fluence: np.ndarray):
     """FluenceTest (CoralBenchmark.cc:177-228): max over cells of
-    |cell - mean| / ((cell + mean) / 2) in percent, within 6%."""
+    |cell - mean| / ((cell + mean) / 2) in percent, within 6%, evaluated as
+    there: the mean from a running sum, the maximum by `max > d ? max : d`
+    (a nan difference replaces the running maximum)."""
     f = np.asarray(fluence, dtype=np.float64)
-    avg = f.sum() / len(f)
-    diff = np.where(f > avg, f - avg, avg - f) / ((f + avg) / 2.0) * 100.0
-    max_diff = float(diff.max()) if len(f) else 0.0
-    ok = not (max_diff > 6.0)
-    msg = ("PASS:: Fluence is homogenous across cells with 6% tolerance" if ok else
-           "FAIL:: Fluence not homogenous across cells within 6% tolerance\n"
+    local_sum = float(np.cumsum(f)[-1]) if len(f) else 0.0
+    average = _c_div(local_sum, len(f))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        diff = (np.where(f > average, f - average, average - f) / ((f + average) / 2.0)) * 100
+    max_diff = 0.0
+    for d in diff.tolist():
+        max_diff = max_diff if max_diff > d else d
+    percent_tolerance = 6.0
+    ok = not (max_diff > percent_tolerance)
+    msg = ("PASS:: Fluence is homogenous across cells with %g%% tolerance" % percent_tolerance if ok else
+           "FAIL:: Fluence not homogenous across cells within %g%% tolerance\n"
            "\tTry running more particles or more cycles to see if Max Percent Difference goes down.\n"
-           f"\tCurrent Max Percent Diff: {max_diff:4.1f}%")
+           "\tCurrent Max Percent Diff: %4.1f%%" % (percent_tolerance, max_diff))
     return ok, msg, max_diff
 
 

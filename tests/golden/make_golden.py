@@ -35,7 +35,12 @@ With ``--spectrum`` it stores the census energy spectrum file the reference
 prints for ``-e <stem>`` (EnergySpectrum.cc:38-59) after all cycles of a few
 decks in ``spectrum_out.npz``.
 
-Usage: python tests/golden/make_golden.py [--exponential-tally | --echo | --xsec | --spectrum] [deck ...]
+With ``--coral`` it stores what the reference's coralBenchmarkCorrectness
+prints (CoralBenchmark.cc:17-228) after the cycles of t_coral1 and of t_homog /
+t_fission run with coralBenchmark 1 / 2 (failing checks included) in
+``coral_out.npz``.
+
+Usage: python tests/golden/make_golden.py [--exponential-tally | --echo | --xsec | --spectrum | --coral]
 """
 from __future__ import annotations
 
@@ -229,8 +234,34 @@ def make_spectrum(names: list[str], workdir: Path) -> None:
     print(f"spectrum_out.npz: {len(out)} decks")
 
 
+CORAL_RUNS = {"t_coral1": None, "t_homog": 1, "t_fission": 2}   # deck -> coralBenchmark set here (None: the deck's)
+
+
+def make_coral(workdir: Path) -> None:
+    out = {}
+    for name, level in CORAL_RUNS.items():
+        text = (DECKS / f"{name}.inp").read_text()
+        if level is not None:
+            text = text.replace("Simulation:\n", f"Simulation:\n   coralBenchmark: {level}\n", 1)
+        deck = workdir / f"{name}.inp"
+        deck.write_text(text)
+        env = dict(os.environ, QS_CORAL="1", OMP_NUM_THREADS="8")
+        res = subprocess.run([str(HARNESS), "-i", str(deck)], env=env, cwd=workdir, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise SystemExit(f"reference run failed on {deck}:\n{res.stderr[-4000:]}")
+        k = res.stdout.index("\nTesting Ratios")
+        out[name] = np.array(res.stdout[k:])
+    np.savez_compressed(HERE / "coral_out.npz", **out)
+    print(f"coral_out.npz: {len(out)} runs")
+
+
 def main(argv: list[str]) -> None:
     import tempfile
+    if "--coral" in argv:
+        ensure_harness("ref")
+        with tempfile.TemporaryDirectory() as tmp:
+            make_coral(Path(tmp))
+        return
     if "--spectrum" in argv:
         ensure_harness("ref")
         names = [a for a in argv if a != "--spectrum"] or ["t_homog", "t_fission", "t_nonflat"]
