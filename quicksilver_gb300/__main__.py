@@ -55,10 +55,7 @@ def main(argv=None) -> int:
     out.write(deck.text() + "\n")
     if deck.cross_sections_out:   # written by initMC in the reference (initMC.cc:392-490)
         write_cross_sections(deck.cross_sections_out, mc.problem, deck.material_names)
-    # Tallies::PrintSummary's layout (Tallies.cc:122-144, Tallies.hh:60-76)
-    out.write("%-8s " % "cycle" + " ".join("%12s" % h for h in HEADER) +
-              "%14s %14s %14s %14s" % ("scalar_flux", "cycleInit", "cycleTracking", "cycleFinalize") +
-              (" %14s" % "cell_tally" if args.exponential_tally else "") + "\n")
+    out.write(summary_header() + (" %14s" % "cell_tally" if args.exponential_tally else "") + "\n")
     track_s = 0.0
     clock = {name: [0, 0.0] for name in TIMERS}   # calls, seconds
     for cycle in range(sim.n_steps):
@@ -80,8 +77,7 @@ def main(argv=None) -> int:
             clock[name][0] += 1
             clock[name][1] += dt
         bal = row.balance[0]
-        out.write("%8d " % cycle + " ".join("%12d" % int(bal[N.BAL[c]]) for c in COLUMNS) +
-                  "%14e %14e %14e %14e" % (row.flux_total[0], t1 - t0, t2 - t1, t3 - t2) +
+        out.write(summary_line(cycle, bal, row.flux_total[0], (t1 - t0, t2 - t1, t3 - t2)) +
                   (" %14e" % cell_total if cell_total is not None else "") + "\n")
     flags = mc.device_status()
     if flags:
@@ -97,6 +93,20 @@ def main(argv=None) -> int:
         coral_benchmark_correctness(cum, mc.fluence(), sim.coral_benchmark, out)
     mc.close()
     return 0
+
+
+def summary_header() -> str:
+    """Tallies::PrintSummary's header (Tallies.cc:126-131, Balance::PrintHeader, Tallies.hh:60-67)."""
+    return ("%-8s " % "cycle" + " ".join("%12s" % h for h in HEADER) +
+            "%14s %14s %14s %14s" % ("scalar_flux", "cycleInit", "cycleTracking", "cycleFinalize"))
+
+
+def summary_line(cycle: int, balance, flux_total: float, times) -> str:
+    """Tallies::PrintSummary's line for one cycle (Tallies.cc:133-140,
+    Balance::Print, Tallies.hh:69-76): counters, scalar-flux sum, and the
+    cycleInit / cycleTracking / cycleFinalize seconds."""
+    return ("%8d " % cycle + " ".join("%12d" % int(balance[N.BAL[c]]) for c in COLUMNS) +
+            "%14e %14e %14e %14e" % (flux_total, times[0], times[1], times[2]))
 
 
 # MC_Fast_Timer's timers (MC_Fast_Timer.hh:31-41, MC_Fast_Timer.cc:8-17); one

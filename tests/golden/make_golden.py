@@ -40,7 +40,12 @@ prints (CoralBenchmark.cc:17-228) after the cycles of t_coral1 and of t_homog /
 t_fission run with coralBenchmark 1 / 2 (failing checks included) in
 ``coral_out.npz``.
 
-Usage: python tests/golden/make_golden.py [--exponential-tally | --echo | --xsec | --spectrum | --coral]
+With ``--summary`` it stores the reference's per-cycle summary lines
+(Tallies::PrintSummary, Tallies.cc:122-144: header and one line per cycle,
+as printed to stdout) for a few decks in ``summary_out.npz``.
+
+Usage: python tests/golden/make_golden.py [--exponential-tally | --echo | --xsec | --spectrum | --coral |
+                                           --summary]
 """
 from __future__ import annotations
 
@@ -255,8 +260,29 @@ def make_coral(workdir: Path) -> None:
     print(f"coral_out.npz: {len(out)} runs")
 
 
+def make_summary(names: list[str], workdir: Path) -> None:
+    out = {}
+    for name in names:
+        deck = DECKS / f"{name}.inp"
+        env = dict(os.environ, OMP_NUM_THREADS="8")
+        res = subprocess.run([str(HARNESS), "-i", str(deck)], env=env, cwd=workdir, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise SystemExit(f"reference run failed on {deck}:\n{res.stderr[-4000:]}")
+        lines = res.stdout.splitlines()
+        k = next(i for i, l in enumerate(lines) if l.startswith("cycle "))
+        out[name] = np.array("\n".join(l for l in lines[k:] if l.startswith("cycle ") or l[:8].strip().isdigit()))
+    np.savez_compressed(HERE / "summary_out.npz", **out)
+    print(f"summary_out.npz: {len(out)} decks")
+
+
 def main(argv: list[str]) -> None:
     import tempfile
+    if "--summary" in argv:
+        ensure_harness("ref")
+        names = [a for a in argv if a != "--summary"] or ["t_homog", "t_fission", "config1"]
+        with tempfile.TemporaryDirectory() as tmp:
+            make_summary(names, Path(tmp))
+        return
     if "--coral" in argv:
         ensure_harness("ref")
         with tempfile.TemporaryDirectory() as tmp:
