@@ -1,4 +1,4 @@
-"""``python -m quicksilver_gb300 DECK [--nSteps N] [--key value ...]``
+"""``python -m quicksilver_gb300 [-i] DECK [-n 1e5 | --nParticles 1e5 ...] [--exponential-tally]``
 
 Runs a Quicksilver input deck with every cycle on the GPU, the way the
 reference's driver does (main.cc:38-85): the deck echoed with every default
@@ -9,14 +9,16 @@ Tallies::PrintSummary, Tallies.cc:122-144, Tallies.hh:60-76), then the
 figure of merit (segments per second of tracking), the census energy
 spectrum file when the deck names one (EnergySpectrum.cc:38-59) and the
 CORAL2 checks when the deck sets coralBenchmark (CoralBenchmark.cc:17-44).
-Simulation keys may be overridden on the command line (``--nParticles 1e5``),
-as the reference's flags do (Parameters.cc:230-255).  ``--exponential-tally``
+The command line takes the reference's flags (Parameters.cc:230-255: short
+``-n 1e5`` or long ``--nParticles 1e5`` / ``--nParticles=1e5``, ``-i DECK`` or
+the deck as the first argument, no deck for the default problem) with its
+precedence (Parameters.cc:80-95): a Simulation key the deck sets wins over
+the flag, except energySpectrum and crossSectionsOut.  ``--exponential-tally``
 runs as the reference built with -DEXPONENTIAL_TALLY (CycleTracking.cc:48-50)
 and adds each cycle's exponential cell-tally total to its line.
 """
 from __future__ import annotations
 
-import argparse
 import ctypes as C
 import sys
 import time
@@ -32,30 +34,98 @@ HEADER = ["start", "source", "rr", "split", "absorb", "scatter", "fission", "pro
           "census", "num_seg"]
 
 
+# The reference's flags (Parameters.cc:230-255): short letter -> long name;
+# loadBalance (-l) takes no value.
+SHORT_FLAGS = {"D": "dt", "f": "fMax", "i": "inputFile", "e": "energySpectrum", "S": "crossSectionsOut",
+               "l": "loadBalance", "c": "cycleTimers", "t": "debugThreads", "X": "lx", "Y": "ly", "Z": "lz",
+               "n": "nParticles", "g": "batchSize", "b": "nBatches", "N": "nSteps", "x": "nx", "y": "ny", "z": "nz",
+               "s": "seed", "I": "xDom", "J": "yDom", "K": "zDom", "B": "bTally", "F": "fTally", "C": "cTally"}
+COMMAND_LINE_WINS = ("energySpectrum", "crossSectionsOut")   # Parameters.cc:88-90
+
+
+def parse_command_line(argv) -> tuple:
+    """(deck path or None, {Simulation key: value} from the flags, exponential tally?)."""
+    path, values, exp_tally = None, {}, False
+    args = list(argv)
+    k = 0
+    while k < len(args):
+        a = args[k]
+        k += 1
+        if a == "--exponential-tally":
+            exp_tally = True
+            continue
+        if a.startswith("--"):
+            name, eq, val = a[2:].partition("=")
+        elif a.startswith("-") and len(a) == 2 and a[1] in SHORT_FLAGS:
+            name, eq, val = SHORT_FLAGS[a[1]], "", ""
+        elif path is None and not a.startswith("-"):
+            path = a   # the deck as a positional argument
+            continue
+        else:
+            raise SystemExit(f"unexpected argument {a!r}")
+        if name == "loadBalance" and not eq:
+            val = "1"
+        elif not eq:
+            if k >= len(args):
+                raise SystemExit(f"flag {a!r} needs a value")
+            val = args[k]
+            k += 1
+        if name == "inputFile":
+            path = val
+        else:
+            values[name] = val
+    return path, values, exp_tally
+
+
+def deck_simulation_keys(text: str) -> set:
+    """Keys the deck's Simulation block sets (they win over the flags)."""
+    keys, block = set(), None
+    for line in text.splitlines():
+        stripped = line.split("//")[0].split("#")[0].rstrip()
+        if not stripped:
+            continue
+        if not line[0].isspace():
+            block = stripped.rstrip(":").strip()
+        elif block == "Simulation" and ":" in stripped:
+            keys.add(stripped.split(":", 1)[0].strip())
+    return keys
+
+
+def deck_from_command_line(argv) -> tuple:
+    """getParameters (Parameters.cc:80-95): flags first, then the deck's own
+    Simulation keys over them (but not over energySpectrum and
+    crossSectionsOut), then the defaults.  Returns (Deck, exponential tally?)."""
+    path, values, exp_tally = parse_command_line(argv)
+    if path is None:
+        deck, deck_keys = Deck.from_string(""), set()
+    else:
+        deck = Deck.from_file(path)
+        with open(path) as fh:
+            deck_keys = deck_simulation_keys(fh.read())
+    for key, val in values.items():
+        if key in COMMAND_LINE_WINS or key not in deck_keys:
+            deck.set(key, val)
+    return deck, exp_tally
+
+
 def main(argv=None) -> int:
     t_main = time.perf_counter()   # MC_Fast_Timer::main covers the whole run
-    ap = argparse.ArgumentParser(prog="python -m quicksilver_gb300", description=__doc__.split("\n\n")[1])
-    ap.add_argument("deck")
-    ap.add_argument("--exponential-tally", action="store_true",
-                    help="behave as the reference built with -DEXPONENTIAL_TALLY")
-    args, extra = ap.parse_known_args(argv)
-    deck = Deck.from_file(args.deck)
-    it = iter(extra)
-    for flag in it:
-        if not flag.startswith("--"):
-            ap.error(f"unexpected argument {flag!r}")
-        deck.set(flag[2:], next(it))
+    argv = sys.argv[1:] if argv is None else argv
+    if "-h" in argv or "--help" in argv:
+        sys.stdout.write(__doc__)
+        return 0
+    deck, exponential_tally = deck_from_command_line(argv)
     sim = deck.simulation
     mc = MonteCarlo(deck)
     spectrum_stem = deck.energy_spectrum
     mc.observe(fluence=bool(sim.coral_benchmark), spectrum=bool(spectrum_stem))
-    if args.exponential_tally:
+    if exponential_tally:
         mc.exponential_tally(True)
     out = sys.stdout
     out.write(deck.text() + "\n")
     if deck.cross_sections_out:   # written by initMC in the reference (initMC.cc:392-490)
         write_cross_sections(deck.cross_sections_out, mc.problem, deck.material_names)
-    out.write(summary_header() + (" %14s" % "cell_tally" if args.exponential_tally else "") + "\n")
+    out.write(summary_header() + (" %14s" % "cell_tally" if exponential_tally else "") + "\n")
     track_s = 0.0
     clock = {name: [0, 0.0] for name in TIMERS}   # calls, seconds
     for cycle in range(sim.n_steps):
@@ -67,7 +137,7 @@ def main(argv=None) -> int:
         mc.cycle_tracking()
         mc_sync(h)
         t2 = time.perf_counter()
-        cell_total = mc.cell_tally().sum() if args.exponential_tally else None   # finalize resets it
+        cell_total = mc.cell_tally().sum() if exponential_tally else None   # finalize resets it
         mc.cycle_finalize()
         row = mc.history(cycle, 1)
         t3 = time.perf_counter()

@@ -197,8 +197,25 @@ def make_exp(deck: Path, workdir: Path) -> None:
           f"cell tally total {out['cell_tally'].sum():.6e}")
 
 
+# command lines whose echo pins the flags' meaning and precedence (Parameters.cc:80-95, 230-255)
+ECHO_COMMAND_LINES = {
+    "cli_default": ["-n", "100", "-N", "1", "-x", "2", "-y", "2", "-z", "2", "-X", "2", "-Y", "2", "-Z", "2",
+                    "-l", "-B", "2", "-C", "3"],
+    "cli_deck_and_flags": ["-i", "quicksilver_gb300/decks/t_homog.inp", "-n", "123", "-g", "50", "-D", "2e-08",
+                           "-e", "spec", "-S", "xs", "-s", "17"],
+}
+
+
 def make_echo(names: list[str], workdir: Path) -> None:
     out = {}
+    for name, args in ECHO_COMMAND_LINES.items():
+        echo = workdir / f"{name}.echo"
+        env = dict(os.environ, QS_ECHO=str(echo), QS_ECHO_ONLY="1")
+        res = subprocess.run([str(HARNESS)] + args, env=env, cwd=ROOT, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise SystemExit(f"reference run failed on {args}:\n{res.stderr[-4000:]}")
+        out[name] = np.array(echo.read_text())
+        out[name + "_args"] = np.array(args)
     for name in names:
         deck = (DECKS / f"{name}.inp").relative_to(ROOT)   # the echo records the path it was given
         echo = workdir / f"{name}.echo"

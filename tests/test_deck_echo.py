@@ -26,10 +26,25 @@ def _normalise(text: str) -> str:
     return "\n".join(out)
 
 
-@pytest.mark.parametrize("name", sorted(ECHO.keys()))
+DECK_NAMES = sorted(k for k in ECHO.keys() if not k.startswith("cli_"))
+COMMAND_LINES = sorted(k for k in ECHO.keys() if k.startswith("cli_") and not k.endswith("_args"))
+
+
+@pytest.mark.parametrize("name", DECK_NAMES)
 def test_echo_matches_reference(name):
     got = Deck.from_file(DECKS / f"{name}.inp").text()
     assert _normalise(got) == _normalise(str(ECHO[name]))
+
+
+@pytest.mark.parametrize("name", COMMAND_LINES)
+def test_command_line_matches_reference(name, monkeypatch):
+    """The driver's flags, their precedence over / under the deck's keys and
+    the default problem without a deck, as getParameters gives them: the
+    echo of the same command line, text for text."""
+    from quicksilver_gb300.__main__ import deck_from_command_line
+    monkeypatch.chdir(DECKS.parent.parent)   # the command lines name decks relative to the repository
+    deck, _ = deck_from_command_line([str(a) for a in ECHO[name + "_args"]])
+    assert _normalise(deck.text()) == _normalise(str(ECHO[name]))
 
 
 @pytest.mark.parametrize("name", ["t_homog", "t_fission", "t_nonflat", "config2"])
