@@ -1434,9 +1434,6 @@ int configure_track_grid(QsgHandle* h)
         const size_t ps = track_pool_smem_bytes(h->block_size, h->num_problems, sens ? h->sens.K : 0, pool);
         const void* fn = h->block_size == 256 ? pool_kernel_fn<256>(sens, pool) : pool_kernel_fn<128>(sens, pool);
         QSG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps));
-#ifdef QSG_CARVEOUT
-        QSG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, QSG_CARVEOUT));
-#endif
         per_sm = 0;
         QSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, h->block_size, ps));
         (sens ? h->pool_sens_blocks : h->pool_blocks) = h->num_sms * (per_sm > 0 ? per_sm : 1);
