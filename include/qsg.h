@@ -153,7 +153,9 @@ typedef struct QsgOptions {
     uint64_t particle_capacity;  /* per store (0 = grow on demand)             */
     uint64_t max_segments;       /* per history per launch guard (0 = 2^40)    */
     int32_t max_passes;          /* fission passes per asynchronous cycle (0 = 8) */
-    int32_t collision_batch;     /* parked collisions per warp collision step (0 = 16) */
+    int32_t collision_batch;     /* one-history-per-lane kernel: parked collisions per
+                                    warp collision step (0 = 16); the default pool
+                                    kernel's thresholds are qsg_set_pool_tuning's */
 } QsgOptions;
 
 typedef struct QsgHandle QsgHandle;
@@ -212,7 +214,8 @@ int qsg_track_cycle_async(QsgHandle* h, void* stream);
 /* Balance counters summed over replicas (13 x u64, QSG_BAL_* order) and the
  * scalar flux [num_cells*G] summed over replicas (Tallies.cc:16-23,75-96). */
 int qsg_read_tallies(QsgHandle* h, uint64_t* balance, double* flux);
-/* Zero counters and flux (Tallies::CycleFinalize reset, Tallies.cc:63-96). */
+/* Zero counters, flux and, when on, the exponential cell tally
+ * (Tallies::CycleFinalize reset, Tallies.cc:63-96). */
 int qsg_reset_tallies(QsgHandle* h);
 /* Device error flag bits (QSG_DEV_*) raised since the last reset, and clear. */
 int qsg_device_status(QsgHandle* h, uint32_t* flags, int clear);
