@@ -242,7 +242,8 @@ int qsg_configure_cycle(QsgHandle* h, const QsgCycleConfig* config);
 int qsg_cycle_init(QsgHandle* h, void* stream);
 /* cycleFinalize (main.cc:310-324), asynchronous: the cycle's 13 counters
  * (END = census count) and scalar-flux total are appended to a device-resident
- * history, then counters and flux are zeroed (Tallies.cc:25-98). */
+ * history, then counters, flux and (when on) the exponential cell tally are
+ * zeroed (Tallies.cc:25-98). */
 int qsg_cycle_finalize(QsgHandle* h, void* stream);
 /* Copy history rows [first, first+n): balance [n*13] and flux totals [n]
  * (either may be NULL).  Synchronous. */
@@ -333,8 +334,9 @@ int qsg_configure_cycle_batch(QsgHandle* h, const QsgCycleConfig* configs, const
  * permutation of the three particle stores). */
 int qsg_run_cycles(QsgHandle* h, int32_t n_cycles, int32_t use_graph, void* stream);
 /* Kernel-shape knobs picked by the autotuner: threads per block of the
- * tracking kernel (128 or 256), collisions batched per warp step (1-32),
- * particles claimed per work-queue atomic (1-1024); 0 keeps a value. */
+ * tracking kernel (128 or 256) and, for the one-history-per-lane kernel,
+ * collisions batched per warp step (1-32) and particles claimed per
+ * work-queue atomic (1-1024); 0 keeps a value. */
 int qsg_set_tuning(QsgHandle* h, int32_t block_size, int32_t collision_batch, int32_t queue_chunk);
 /* Tracking kernel: 1 (default) = each warp keeps a pool of 64 particles in
  * shared memory and hands 32 of one kind (segment or collision) to its lanes
