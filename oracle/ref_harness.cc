@@ -27,6 +27,9 @@
 //                         (QS_ECHO_ONLY=1: then stop)
 //   QS_PRINT_SPECTRUM=1   print the energy spectrum file after the last cycle
 //   QS_CORAL=1            run coralBenchmarkCorrectness after the last cycle
+//   QS_TIMERS=1           print the reference's timer reports to stdout: the
+//                         last-cycle table after every cycle (when the deck or
+//                         -c sets cycleTimers 1) and the cumulative table
 //   QS_INIT_ONLY=1        stop after initMC (which writes the crossSectionsOut
 //                         file when the deck or -S names one)
 //   Built with -DEXPONENTIAL_TALLY (make -C oracle ref_exp) it also writes,
@@ -60,6 +63,10 @@
 #include "MC_Time_Info.hh"
 #include "utilsMpi.hh"
 #include "CoralBenchmark.hh"
+#include "MC_Fast_Timer.hh"
+#include "MC_Processor_Info.hh"
+#include "utilsMpi.hh"
+#include <omp.h>
 
 extern MonteCarlo* mcco;
 void cycleInit(bool loadBalance);
@@ -321,6 +328,13 @@ int main(int argc, char** argv)
    if (want_tables) dump_tables(params);
    dump_rng_kat();
 
+   // the reference's timer reports as main.cc prints them: main timed from
+   // here (main.cc:51), Last_Cycle_Report after every cycle (main.cc:61-65,
+   // prints only when cycleTimers is 1), Cumulative_Report at the end
+   // (main.cc:87-91)
+   const bool want_timers = env_on("QS_TIMERS");
+   if (want_timers) MC_FASTTIMER_START(MC_Fast_Timer::main);
+
    const int G = mcco->_nuclearData->_numEnergyGroups;
    const int64_t NC = total_cells(params);
    const int nSteps = params.simulationParams.nSteps;
@@ -384,6 +398,17 @@ int main(int argc, char** argv)
       if (want_particles) dump_particles("census_c" + std::to_string(cyc), false);
 
       cycleFinalize();
+      if (want_timers)
+         mcco->fast_timer->Last_Cycle_Report(params.simulationParams.cycleTimers, mcco->processor_info->rank,
+                                             mcco->processor_info->num_processors,
+                                             mcco->processor_info->comm_mc_world);
+   }
+   if (want_timers)
+   {
+      MC_FASTTIMER_STOP(MC_Fast_Timer::main);
+      mcco->fast_timer->Cumulative_Report(mcco->processor_info->rank, mcco->processor_info->num_processors,
+                                          mcco->processor_info->comm_mc_world,
+                                          mcco->_tallies->_balanceCumulative._numSegments);
    }
    write_d("track_seconds", track_seconds);
    // the census energy spectrum file (EnergySpectrum.cc:38-59), which the

@@ -6,7 +6,10 @@ filled in (printParameters, Parameters.cc:97-215), nSteps cycles of cycleInit /
 cycleTracking / cycleFinalize, one summary line per cycle with the balance
 counters, the scalar-flux total and the three phase times (the columns of
 Tallies::PrintSummary, Tallies.cc:122-144, Tallies.hh:60-76), then the
-figure of merit (segments per second of tracking), the census energy
+figure of merit (segments per second of tracking) after the cumulative
+timer table (MC_Fast_Timer.cc:58-104) -- with cycleTimers 1 (``-c 1``) also
+the last-cycle table after every summary line (MC_Fast_Timer.cc:106-152) --,
+the census energy
 spectrum file when the deck names one (EnergySpectrum.cc:38-59) and the
 CORAL2 checks when the deck sets coralBenchmark (CoralBenchmark.cc:17-44).
 The command line takes the reference's flags (Parameters.cc:230-255: short
@@ -109,14 +112,15 @@ def deck_from_command_line(argv) -> tuple:
 
 
 def main(argv=None) -> int:
-    t_main = time.perf_counter()   # MC_Fast_Timer::main covers the whole run
     argv = sys.argv[1:] if argv is None else argv
     if "-h" in argv or "--help" in argv:
         sys.stdout.write(__doc__)
         return 0
     deck, exponential_tally = deck_from_command_line(argv)
     sim = deck.simulation
+    cycle_timers = int(deck._echo_values("Simulation", "cycleTimers")[0])
     mc = MonteCarlo(deck)
+    t_main = time.perf_counter()   # MC_Fast_Timer::main starts once the problem is set up (main.cc:51)
     spectrum_stem = deck.energy_spectrum
     mc.observe(fluence=bool(sim.coral_benchmark), spectrum=bool(spectrum_stem))
     if exponential_tally:
@@ -142,13 +146,19 @@ def main(argv=None) -> int:
         row = mc.history(cycle, 1)
         t3 = time.perf_counter()
         track_s += t2 - t1
-        for name, dt in (("cycleInit", t1 - t0), ("cycleTracking", t2 - t1), ("cycleTracking_Kernel", t2 - t1),
-                         ("cycleFinalize", t3 - t2)):
-            clock[name][0] += 1
+        # the reference stops its finalize timer for the summary line and
+        # starts it again after (Tallies.cc:125, 143): two calls a cycle,
+        # the second one empty here
+        last = {"cycleInit": (1, t1 - t0), "cycleTracking": (1, t2 - t1), "cycleTracking_Kernel": (1, t2 - t1),
+                "cycleFinalize": (2, t3 - t2)}
+        for name, (calls, dt) in last.items():
+            clock[name][0] += calls
             clock[name][1] += dt
         bal = row.balance[0]
         out.write(summary_line(cycle, bal, row.flux_total[0], (t1 - t0, t2 - t1, t3 - t2)) +
                   (" %14e" % cell_total if cell_total is not None else "") + "\n")
+        if cycle_timers == 1:   # Last_Cycle_Report: cumulative calls, this cycle's time (main.cc:61-65)
+            timer_table(out, "Last Cycle", {name: (clock[name][0], dt) for name, (_, dt) in last.items()})
     flags = mc.device_status()
     if flags:
         raise N.QsgError(N.QSG_ERR_DEVICE, f"device flags 0x{flags:x} raised during the run")
@@ -179,27 +189,35 @@ def summary_line(cycle: int, balance, flux_total: float, times) -> str:
             "%14e %14e %14e %14e" % (flux_total, times[0], times[1], times[2]))
 
 
-# MC_Fast_Timer's timers (MC_Fast_Timer.hh:31-41, MC_Fast_Timer.cc:8-17); one
-# process and one domain: no particle exchange, so the MPI and test-for-done
-# timers are never started
+# MC_Fast_Timer's timers (MC_Fast_Timer.hh:31-41, MC_Fast_Timer.cc:8-17).
+# cycleTracking_Kernel counts one call per cycle (the reference: one per
+# particle vault processed); cycleTracking_MPI and cycleTracking_Test_Done
+# stay at zero, as one GPU exchanges no particles (the reference times its
+# vault bookkeeping under cycleTracking_MPI even on one rank, main.cc:243-292)
 TIMERS = ["main", "cycleInit", "cycleTracking", "cycleTracking_Kernel", "cycleTracking_MPI",
           "cycleTracking_Test_Done", "cycleFinalize"]
 
 
-def timer_report(out, clock: dict, num_segments: int) -> None:
-    """MC_Fast_Timer_Container::Cumulative_Report (MC_Fast_Timer.cc:45-104)
-    for one rank: microseconds per timer (min = avg = max, no spread) and the
-    figure of merit, segments per second of cycleTracking."""
-    out.write("\n%-25s %12s %12s %12s %12s %12s %12s\n" % ("Timer", "Cumulative", "Cumulative", "Cumulative",
-                                                          "Cumulative", "Cumulative", "Cumulative"))
+def timer_table(out, kind: str, clock: dict) -> None:
+    """Print_Cumulative_Heading / Print_Last_Cycle_Heading and the timer
+    lines (MC_Fast_Timer.cc:31-56, 81-95, 133-146) for one rank:
+    {name: (calls, seconds)}, whole microseconds, min = avg = max, no spread."""
+    out.write("\n%-25s %12s %12s %12s %12s %12s %12s\n" % (("Timer",) + (kind,) * 6))
     out.write("%-25s %12s %12s %12s %12s %12s %12s\n" % ("Name", "number", "microSecs", "microSecs", "microSecs",
                                                         "microSecs", "Efficiency"))
     out.write("%-25s %12s %12s %12s %12s %12s %12s\n" % ("", "of calls", "min", "avg", "max", "stddev", "Rating"))
     for name in TIMERS:
-        calls, secs = clock.get(name, [0, 0.0])
+        calls, secs = clock.get(name, (0, 0.0))
         us = float(int(secs * 1e6))   # the reference keeps whole microseconds
         out.write("%-25s %12d %12.3e %12.3e %12.3e %12.3e %12.2f\n" %
                   (name, calls, us, us, us, 0.0, 100.0 * us / (us + 1.0e-80)))
+
+
+def timer_report(out, clock: dict, num_segments: int) -> None:
+    """MC_Fast_Timer_Container::Cumulative_Report (MC_Fast_Timer.cc:58-104)
+    for one rank: the timer table and the figure of merit, segments per
+    second of cycleTracking."""
+    timer_table(out, "Cumulative", clock)
     track_us = float(int(clock["cycleTracking"][1] * 1e6))
     out.write("%-25s %12.3e %-25s\n" % ("Figure Of Merit", num_segments / (track_us * 1e-6),
                                          "[Num Segments / Cycle Tracking Time]"))

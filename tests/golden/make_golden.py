@@ -44,8 +44,14 @@ With ``--summary`` it stores the reference's per-cycle summary lines
 (Tallies::PrintSummary, Tallies.cc:122-144: header and one line per cycle,
 as printed to stdout) for a few decks in ``summary_out.npz``.
 
+With ``--timers`` it stores what the reference prints from its first
+summary line on for t_homog run with ``-c 1`` (cycleTimers): per cycle the
+summary line and the last-cycle timer table (MC_Fast_Timer.cc:106-152), then
+the cumulative table and the figure of merit (MC_Fast_Timer.cc:58-104), in
+``timers_out.npz``.
+
 Usage: python tests/golden/make_golden.py [--exponential-tally | --echo | --xsec | --spectrum | --coral |
-                                           --summary]
+                                           --summary | --timers]
 """
 from __future__ import annotations
 
@@ -292,8 +298,25 @@ def make_summary(names: list[str], workdir: Path) -> None:
     print(f"summary_out.npz: {len(out)} decks")
 
 
+def make_timers(workdir: Path) -> None:
+    deck = DECKS / "t_homog.inp"
+    env = dict(os.environ, QS_TIMERS="1", OMP_NUM_THREADS="8")
+    res = subprocess.run([str(HARNESS), "-i", str(deck), "-c", "1"], env=env, cwd=workdir, capture_output=True,
+                         text=True)
+    if res.returncode != 0:
+        raise SystemExit(f"reference run failed on {deck}:\n{res.stderr[-4000:]}")
+    k = res.stdout.index("cycle ")
+    np.savez_compressed(HERE / "timers_out.npz", t_homog=np.array(res.stdout[k:]))
+    print("timers_out.npz: t_homog")
+
+
 def main(argv: list[str]) -> None:
     import tempfile
+    if "--timers" in argv:
+        ensure_harness("ref")
+        with tempfile.TemporaryDirectory() as tmp:
+            make_timers(Path(tmp))
+        return
     if "--summary" in argv:
         ensure_harness("ref")
         names = [a for a in argv if a != "--summary"] or ["t_homog", "t_fission", "config1"]

@@ -90,3 +90,23 @@ def test_gpu_command_line_driver_exponential_tally(gpu):
             assert int(r[1 + k]) == int(gold["balance"][c][N.BAL[name]]), (c, name)
         want = gold["cell_tally"][c].sum()
         assert abs(float(r[-1]) - want) <= 1e-6 * want   # printed with 7 significant digits
+
+
+def test_gpu_command_line_driver_cycle_timers(gpu):
+    """-c 1 (cycleTimers): after every summary line the driver prints the
+    reference's last-cycle timer table, then the cumulative one; the lines
+    line up with the reference's own printout of the same run
+    (tests/golden/timers_out.npz), and so do the call counts of the timers
+    both sides time alike (main, cycleInit, cycleTracking, cycleFinalize and
+    the done test)."""
+    res = subprocess.run([sys.executable, "-m", "quicksilver_gb300", str(DECKS / "t_homog.inp"), "-c", "1"],
+                         cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr
+    got = res.stdout[res.stdout.index("cycle "):].split("\n")
+    want = str(np.load(ROOT / "tests" / "golden" / "timers_out.npz")["t_homog"]).split("\n")
+    assert len(got) == len(want)
+    for g, w in zip(got, want):
+        assert len(g) == len(w) and g.split()[:1] == w.split()[:1], (g, w)
+        if g.split()[:1] and g.split()[0] in ("main", "cycleInit", "cycleTracking", "cycleFinalize",
+                                              "cycleTracking_Test_Done"):
+            assert g.split()[1] == w.split()[1], (g, w)
