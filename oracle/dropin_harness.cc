@@ -11,10 +11,16 @@
 //   * validates the export with qsg_problem_check (no GPU needed);
 //   * writes every exported array, named after its QsgProblem field, to the
 //     file QS_DUMP names (records as oracle/ref_harness.cc writes them), so
-//     the tests can compare it with the library's own deck reader.
+//     the tests can compare it with the library's own deck reader;
+//   * with QS_VAULTS=1, checks the vault and tally halves of the cycle
+//     adapter (qsgGather / qsgScatterCensus / qsgAddTallies) around the
+//     reference's own first cycleInit, and dumps the gathered processing
+//     particles (p_<field>) and the vault size.
 //
-// Exit status: 0 when qsg_problem_check accepts the export, else 2 (the
-// library's message on stderr).
+// The library calls that need a GPU (qsgAttach, qsgCycleTracking) are
+// compiled and linked here but not run.  Exit status: 0 when everything
+// passes, 2 when qsg_problem_check rejects the export (the library's message
+// on stderr), 3 when a vault or tally check fails.
 
 #include <algorithm>
 #include <cstdint>
@@ -31,11 +37,16 @@
 #include "MaterialDatabase.hh"
 #include "MC_Domain.hh"
 #include "MC_Time_Info.hh"
+#include "MC_Base_Particle.hh"
+#include "ParticleVault.hh"
+#include "ParticleVaultContainer.hh"
+#include "Tallies.hh"
 #include "utilsMpi.hh"
 
 #include "qsg.h"
 
 extern MonteCarlo* mcco;
+void cycleInit(bool loadBalance);
 
 // ---- the adapter ----------------------------------------------------------
 
@@ -116,6 +127,122 @@ void qsgExport(MonteCarlo* mc, QsgExport& e)
     p.time_step = mc->time_info->time_step;
 }
 
+static QsgHandle* g_qsg = nullptr;
+static QsgExport g_export;   // qsg_create copies the tables; the cycle code below reads the counts
+
+void qsgAttach(MonteCarlo* mc)
+{
+    qsgExport(mc, g_export);
+    QsgOptions o{};
+    o.flux_replicas = mc->_params.simulationParams.fluxTallyReplications;
+    if (qsg_create(&g_export.problem, &o, &g_qsg) != QSG_OK) {
+        char e[512]; qsg_last_error(e, sizeof e); printf("%s\n", e);
+    }
+}
+
+// MC_Base_Particle records (MC_Base_Particle.hh:75-92) as host columns, and
+// the QsgParticleSoA view of them.
+struct QsgColumns {
+    std::vector<double> d[12];
+    std::vector<uint64_t> q[2];
+    std::vector<int32_t> i[6];
+    QsgParticleSoA soa{};
+    void resize(size_t n)
+    {
+        for (auto& v : d) v.resize(n);
+        for (auto& v : q) v.resize(n);
+        for (auto& v : i) v.resize(n);
+        soa = QsgParticleSoA{d[0].data(), d[1].data(), d[2].data(), d[3].data(), d[4].data(), d[5].data(),
+                             d[6].data(), d[7].data(), d[8].data(), d[9].data(), d[10].data(), d[11].data(),
+                             q[0].data(), q[1].data(), i[0].data(), i[1].data(), i[2].data(), i[3].data(),
+                             i[4].data(), i[5].data()};
+    }
+};
+
+// every particle of a list of vaults -> columns, in vault order
+size_t qsgGather(ParticleVaultContainer& pvc, bool processed, QsgColumns& cols)
+{
+    const uint64_t nv = processed ? pvc.processedSize() : pvc.processingSize();
+    cols.resize(processed ? pvc.sizeProcessed() : pvc.sizeProcessing());
+    size_t k = 0;
+    for (uint64_t v = 0; v < nv; ++v) {
+        ParticleVault& vault = *(processed ? pvc.getTaskProcessedVault(v) : pvc.getTaskProcessingVault(v));
+        for (size_t j = 0; j < vault.size(); ++j, ++k) {
+            const MC_Base_Particle& b = vault[j];
+            const double dd[12] = {b.coordinate.x, b.coordinate.y, b.coordinate.z, b.velocity.x, b.velocity.y,
+                                   b.velocity.z, b.kinetic_energy, b.weight, b.time_to_census, b.age,
+                                   b.num_mean_free_paths, b.num_segments};
+            const int32_t ii[6] = {b.last_event, b.num_collisions, b.breed, b.species, b.domain, b.cell};
+            for (int f = 0; f < 12; ++f) cols.d[f][k] = dd[f];
+            for (int f = 0; f < 6; ++f) cols.i[f][k] = ii[f];
+            cols.q[0][k] = b.random_number_seed;
+            cols.q[1][k] = b.identifier;
+        }
+    }
+    return k;
+}
+
+// n census particles -> the processed vaults, each filled to the vault size
+// (getFirstEmptyProcessedVault, ParticleVaultContainer.cc:111-128)
+void qsgScatterCensus(const QsgColumns& cols, size_t n, ParticleVaultContainer& pvc)
+{
+    size_t k = 0;
+    while (k < n) {
+        ParticleVault& vault = *pvc.getTaskProcessedVault(pvc.getFirstEmptyProcessedVault());
+        for (; k < n && vault.size() < pvc.getVaultSize(); ++k) {
+            MC_Base_Particle b;
+            b.coordinate = MC_Vector(cols.d[0][k], cols.d[1][k], cols.d[2][k]);
+            b.velocity = MC_Vector(cols.d[3][k], cols.d[4][k], cols.d[5][k]);
+            b.kinetic_energy = cols.d[6][k];        b.weight = cols.d[7][k];
+            b.time_to_census = cols.d[8][k];        b.age = cols.d[9][k];
+            b.num_mean_free_paths = cols.d[10][k];  b.num_segments = cols.d[11][k];
+            b.random_number_seed = cols.q[0][k];    b.identifier = cols.q[1][k];
+            b.last_event = (MC_Tally_Event::Enum)cols.i[0][k];
+            b.num_collisions = cols.i[1][k];  b.breed = cols.i[2][k];   b.species = cols.i[3][k];
+            b.domain = cols.i[4][k];          b.cell = cols.i[5][k];
+            vault.pushBaseParticle(b);
+        }
+    }
+}
+
+// one cycle's counters (QSG_BAL_* order) and flux [cell][group] -> the
+// first balance and flux replicas, which the reference sums over replicas
+// at cycle finalize (Tallies.cc:16-23, 146-171)
+void qsgAddTallies(MonteCarlo* mc, const uint64_t* bal, const double* flux)
+{
+    Balance& b = mc->_tallies->_balanceTask[0];
+    b._absorb += bal[QSG_BAL_ABSORB];       b._census += bal[QSG_BAL_CENSUS];
+    b._escape += bal[QSG_BAL_ESCAPE];       b._collision += bal[QSG_BAL_COLLISION];
+    b._fission += bal[QSG_BAL_FISSION];     b._produce += bal[QSG_BAL_PRODUCE];
+    b._scatter += bal[QSG_BAL_SCATTER];     b._numSegments += bal[QSG_BAL_NUM_SEGMENTS];
+    ScalarFluxTask& t = mc->_tallies->_scalarFluxDomain[0]._task[0];
+    const int C = g_export.problem.num_cells, G = g_export.problem.num_groups;
+    for (int c = 0; c < C; ++c)
+        for (int g = 0; g < G; ++g) t._cell[c]._group[g] += flux[(size_t)c * G + g];
+}
+
+// replaces cycleTracking (main.cc:138-307): the processing vaults tracked in
+// one call, fission products included; census particles land in the
+// processed vaults and the cycle's tallies in the reference's Tallies
+void qsgCycleTracking(MonteCarlo* mc)
+{
+    static QsgColumns in, census;
+    ParticleVaultContainer& pvc = *mc->_particleVaultContainer;
+    const size_t n = qsgGather(pvc, false, in);
+    uint64_t n_processing = 0, n_census = 0, bal[QSG_BAL_COUNT];
+    std::vector<double> flux((size_t)g_export.problem.num_cells * g_export.problem.num_groups);
+    int rc = qsg_set_particles(g_qsg, &in.soa, n);
+    if (rc == QSG_OK) rc = qsg_track_cycle_sync(g_qsg);
+    if (rc == QSG_OK) rc = qsg_sizes(g_qsg, &n_processing, &n_census);
+    if (rc == QSG_OK) { census.resize(n_census); rc = qsg_get_census(g_qsg, &census.soa, n_census, &n_census); }
+    if (rc == QSG_OK) rc = qsg_read_tallies(g_qsg, bal, flux.data());
+    if (rc == QSG_OK) rc = qsg_reset_tallies(g_qsg);
+    if (rc != QSG_OK) { char e[512]; qsg_last_error(e, sizeof e); printf("%s\n", e); return; }
+    for (uint64_t v = 0; v < pvc.processingSize(); ++v) pvc.getTaskProcessingVault(v)->clear();
+    qsgScatterCensus(census, n_census, pvc);
+    qsgAddTallies(mc, bal, flux.data());
+}
+
 // ---- the check ------------------------------------------------------------
 
 namespace {
@@ -137,6 +264,60 @@ void put(const char* name, char dtype, const void* data, uint64_t count)
 
 }  // namespace
 
+// The vault and tally halves of qsgCycleTracking on the CPU (the tracking
+// call between them needs a GPU): after the reference's own cycleInit, the
+// processing vaults gathered into columns, scattered into the processed
+// vaults and gathered back must be the same records, no vault above the
+// vault size; and counters / flux added through qsgAddTallies must be what
+// the reference's Tallies then hold.  Returns the number of failures.
+int check_vaults_and_tallies(MonteCarlo* mc, const Parameters& params)
+{
+    int bad = 0;
+    cycleInit(bool(params.simulationParams.loadBalance));
+    ParticleVaultContainer& pvc = *mc->_particleVaultContainer;
+    QsgColumns in, back;
+    const size_t n = qsgGather(pvc, false, in);
+    if (n == 0 || pvc.sizeProcessed() != 0) { fprintf(stderr, "unexpected vault sizes\n"); return 1; }
+    qsgScatterCensus(in, n, pvc);
+    for (uint64_t v = 0; v < pvc.processedSize(); ++v)
+        if (pvc.getTaskProcessedVault(v)->size() > pvc.getVaultSize()) { fprintf(stderr, "vault %d over size\n", (int)v); ++bad; }
+    if (qsgGather(pvc, true, back) != n) { fprintf(stderr, "census count differs\n"); return bad + 1; }
+    for (int f = 0; f < 12; ++f) bad += memcmp(in.d[f].data(), back.d[f].data(), n * 8) != 0;
+    for (int f = 0; f < 2; ++f) bad += memcmp(in.q[f].data(), back.q[f].data(), n * 8) != 0;
+    for (int f = 0; f < 6; ++f) bad += memcmp(in.i[f].data(), back.i[f].data(), n * 4) != 0;
+    if (bad) fprintf(stderr, "vault round trip differs\n");
+    put("vault_size", 'q', std::vector<uint64_t>{pvc.getVaultSize()}.data(), 1);
+    const char* dnames[12] = {"x", "y", "z", "vx", "vy", "vz", "kinetic_energy", "weight", "time_to_census", "age",
+                              "num_mean_free_paths", "num_segments"};
+    const char* inames[6] = {"last_event", "num_collisions", "breed", "species", "domain", "cell"};
+    for (int f = 0; f < 12; ++f) put((std::string("p_") + dnames[f]).c_str(), 'd', in.d[f].data(), n);
+    put("p_random_number_seed", 'q', in.q[0].data(), n);
+    put("p_identifier", 'q', in.q[1].data(), n);
+    for (int f = 0; f < 6; ++f) put((std::string("p_") + inames[f]).c_str(), 'i', in.i[f].data(), n);
+
+    const int C = g_export.problem.num_cells, G = g_export.problem.num_groups;
+    Balance before = mc->_tallies->_balanceTask[0];
+    uint64_t bal[QSG_BAL_COUNT];
+    for (int k = 0; k < QSG_BAL_COUNT; ++k) bal[k] = 1000 + 17 * k;
+    std::vector<double> flux((size_t)C * G);
+    double want = mc->_tallies->ScalarFluxSum(mc);
+    for (size_t k = 0; k < flux.size(); ++k) { flux[k] = (double)(k % 13); want += flux[k]; }
+    qsgAddTallies(mc, bal, flux.data());
+    const Balance& b = mc->_tallies->_balanceTask[0];
+    const uint64_t got[8] = {b._absorb - before._absorb, b._census - before._census, b._escape - before._escape,
+                             b._collision - before._collision, b._fission - before._fission,
+                             b._produce - before._produce, b._scatter - before._scatter,
+                             b._numSegments - before._numSegments};
+    const int slot[8] = {QSG_BAL_ABSORB, QSG_BAL_CENSUS, QSG_BAL_ESCAPE, QSG_BAL_COLLISION, QSG_BAL_FISSION,
+                         QSG_BAL_PRODUCE, QSG_BAL_SCATTER, QSG_BAL_NUM_SEGMENTS};
+    for (int k = 0; k < 8; ++k)
+        if (got[k] != bal[slot[k]]) { fprintf(stderr, "counter slot %d differs\n", slot[k]); ++bad; }
+    if (b._start != before._start || b._source != before._source || b._rr != before._rr ||
+        b._split != before._split || b._end != before._end) { fprintf(stderr, "population counters touched\n"); ++bad; }
+    if (mc->_tallies->ScalarFluxSum(mc) != want) { fprintf(stderr, "flux sum differs\n"); ++bad; }
+    return bad;
+}
+
 int main(int argc, char** argv)
 {
     mpiInit(&argc, &argv);
@@ -146,9 +327,9 @@ int main(int argc, char** argv)
         fprintf(stderr, "dropin_harness: %d domains; the export covers one\n", (int)mcco->domain.size());
         return 2;
     }
-    QsgExport e;
-    qsgExport(mcco, e);
-    const QsgProblem& p = e.problem;
+    qsgExport(mcco, g_export);
+    const QsgProblem& p = g_export.problem;
+    const QsgExport& e = g_export;
     const int rc = qsg_problem_check(&p);
     if (rc != QSG_OK) {
         char msg[1024];
@@ -160,31 +341,36 @@ int main(int argc, char** argv)
     if (path && path[0]) {
         g_out = fopen(path, "wb");
         if (!g_out) { fprintf(stderr, "cannot open %s\n", path); return 1; }
-        const uint64_t G = p.num_groups, C = p.num_cells;
-        put("energies", 'd', p.energies, G + 1);
-        put("isotope_reaction_offset", 'i', p.isotope_reaction_offset, e.iso_off.size());
-        put("reaction_type", 'i', p.reaction_type, e.rtype.size());
-        put("reaction_nubar", 'd', p.reaction_nubar, e.nubar.size());
-        put("reaction_xs", 'd', p.reaction_xs, e.xs.size());
-        put("material_isotope_offset", 'i', p.material_isotope_offset, e.mat_off.size());
-        put("material_isotope_gid", 'i', p.material_isotope_gid, e.mat_gid.size());
-        put("material_atom_fraction", 'd', p.material_atom_fraction, e.af.size());
-        put("material_mass", 'd', p.material_mass, e.mass.size());
-        put("nodes", 'd', p.nodes, e.nodes.size());
-        put("cell_points", 'i', p.cell_points, C * 14);
-        put("facet_local_points", 'i', p.facet_local_points, 72);
-        put("facet_planes", 'd', p.facet_planes, C * 96);
-        put("facet_event", 'i', p.facet_event, C * 24);
-        put("facet_adjacent_cell", 'i', p.facet_adjacent_cell, C * 24);
-        put("facet_adjacent_facet", 'i', p.facet_adjacent_facet, C * 24);
-        put("cell_material", 'i', p.cell_material, C);
-        put("cell_number_density", 'd', p.cell_number_density, C);
-        put("cell_volume", 'd', p.cell_volume, C);
-        put("cell_id", 'q', p.cell_id, C);
-        put("time_step", 'd', &p.time_step, 1);
-        fclose(g_out);
     }
+    const uint64_t G = p.num_groups, C = p.num_cells;
+    put("energies", 'd', p.energies, G + 1);
+    put("isotope_reaction_offset", 'i', p.isotope_reaction_offset, e.iso_off.size());
+    put("reaction_type", 'i', p.reaction_type, e.rtype.size());
+    put("reaction_nubar", 'd', p.reaction_nubar, e.nubar.size());
+    put("reaction_xs", 'd', p.reaction_xs, e.xs.size());
+    put("material_isotope_offset", 'i', p.material_isotope_offset, e.mat_off.size());
+    put("material_isotope_gid", 'i', p.material_isotope_gid, e.mat_gid.size());
+    put("material_atom_fraction", 'd', p.material_atom_fraction, e.af.size());
+    put("material_mass", 'd', p.material_mass, e.mass.size());
+    put("nodes", 'd', p.nodes, e.nodes.size());
+    put("cell_points", 'i', p.cell_points, C * 14);
+    put("facet_local_points", 'i', p.facet_local_points, 72);
+    put("facet_planes", 'd', p.facet_planes, C * 96);
+    put("facet_event", 'i', p.facet_event, C * 24);
+    put("facet_adjacent_cell", 'i', p.facet_adjacent_cell, C * 24);
+    put("facet_adjacent_facet", 'i', p.facet_adjacent_facet, C * 24);
+    put("cell_material", 'i', p.cell_material, C);
+    put("cell_number_density", 'd', p.cell_number_density, C);
+    put("cell_volume", 'd', p.cell_volume, C);
+    put("cell_id", 'q', p.cell_id, C);
+    put("time_step", 'd', &p.time_step, 1);
     printf("dropin_harness: export accepted (%d cells, %d groups, %d isotopes, %d materials)\n",
            p.num_cells, p.num_groups, p.num_isotopes, p.num_materials);
-    return 0;
+    int bad = 0;
+    if (getenv("QS_VAULTS")) {
+        bad = check_vaults_and_tallies(mcco, params);
+        printf("dropin_harness: vault round trip and tally hand-over %s\n", bad ? "FAILED" : "ok");
+    }
+    if (g_out) fclose(g_out);
+    return bad ? 3 : 0;
 }
