@@ -150,13 +150,19 @@ class _Driver:
 
 
 class MonteCarlo(_Driver):
-    def __init__(self, deck: Deck, flux_replicas: int = 1, balance_replicas: int = 1, max_passes: int = 8,
-                 store_capacity: int = 0, device: int = 0, problem: HostProblem | None = None,
+    def __init__(self, deck: Deck, flux_replicas: int | None = None, balance_replicas: int | None = None,
+                 max_passes: int = 8, store_capacity: int = 0, device: int = 0, problem: HostProblem | None = None,
                  block_size: int = 0, collision_batch: int = 0, seed_offset: int = 0):
-        """seed_offset (0 = the reference's seeding) is added to every source
+        """flux_replicas / balance_replicas default to the deck's fTally /
+        bTally, the reference's tally replication counts (Tallies.cc:173-238).
+        seed_offset (0 = the reference's seeding) is added to every source
         seed, giving an independent replica of the same problem."""
         self.deck = deck
         self.params = deck.simulation
+        if flux_replicas is None:
+            flux_replicas = max(1, self.params.flux_replications)
+        if balance_replicas is None:
+            balance_replicas = max(1, self.params.balance_replications)
         self.problem = problem if problem is not None else deck.build()
         self.tracker = Tracker(self.problem, flux_replicas=flux_replicas, balance_replicas=balance_replicas,
                                device=device, max_passes=max_passes, block_size=block_size,

@@ -83,6 +83,29 @@ def test_gpu_flux_replicas(gpu):
     run_parity("t_homog", cycles=2, flux_replicas=4)
 
 
+def test_gpu_deck_tally_replications(gpu):
+    """fTally / bTally in a deck size MonteCarlo's flux and balance
+    replicas, as they size the reference's (Tallies.cc:173-238): whole device
+    cycles keep the reference's counters bit for bit, and the flux totals
+    agree with a one-replica run to summation order."""
+    from quicksilver_gb300 import Deck
+    from quicksilver_gb300.monte_carlo import MonteCarlo
+    gold = np.load(DECKS.parent.parent / "tests" / "golden" / "t_homog.npz")["balance"]
+    deck = Deck.from_file(DECKS / "t_homog.inp")
+    deck.set("fTally", "3")
+    deck.set("bTally", "2")
+    runs = []
+    for d in (deck, Deck.from_file(DECKS / "t_homog.inp")):
+        mc = MonteCarlo(d)
+        try:
+            runs.append(mc.run(3))
+            assert mc.device_status() == 0
+        finally:
+            mc.close()
+    np.testing.assert_array_equal(runs[0].balance, gold[:3])
+    np.testing.assert_allclose(runs[0].flux_total, runs[1].flux_total, rtol=1e-12)
+
+
 def test_gpu_empty_vault(gpu):
     _, sim, hp = load_problem("t_homog.inp")
     trk = Tracker(hp)
