@@ -2,8 +2,6 @@
 validation errors surface through the C ABI before any device work."""
 import ctypes
 
-import pytest
-
 from helpers import DECKS
 from quicksilver_gb300 import Deck
 from quicksilver_gb300 import _native as N
