@@ -167,8 +167,8 @@ def main(argv=None) -> int:
     clock["main"] = [1, time.perf_counter() - t_main]
     timer_report(out, clock, cum["num_segments"])
     if spectrum_stem:
-        path = write_energy_spectrum(spectrum_stem, mc.problem.array("energies"), mc.energy_spectrum()[0])
-        out.write(f"energy spectrum written to {path}\n")
+        # written silently, as the reference's PrintSpectrum does (EnergySpectrum.cc:38-59)
+        write_energy_spectrum(spectrum_stem, mc.problem.array("energies"), mc.energy_spectrum()[0])
     if sim.coral_benchmark:
         coral_benchmark_correctness(cum, mc.fluence(), sim.coral_benchmark, out)
     mc.close()

@@ -50,8 +50,13 @@ summary line and the last-cycle timer table (MC_Fast_Timer.cc:106-152), then
 the cumulative table and the figure of merit (MC_Fast_Timer.cc:58-104), in
 ``timers_out.npz``.
 
+With ``--transcript`` it stores, for t_coral1 run with ``-e spectrum``, what
+the reference prints from its first summary line to its CORAL2 checks
+(summary lines, cumulative timer table, figure of merit, checks) and the
+spectrum file it writes, in ``transcript_out.npz``.
+
 Usage: python tests/golden/make_golden.py [--exponential-tally | --echo | --xsec | --spectrum | --coral |
-                                           --summary | --timers]
+                                           --summary | --timers | --transcript]
 """
 from __future__ import annotations
 
@@ -310,8 +315,26 @@ def make_timers(workdir: Path) -> None:
     print("timers_out.npz: t_homog")
 
 
+def make_transcript(workdir: Path) -> None:
+    deck = DECKS / "t_coral1.inp"
+    env = dict(os.environ, QS_TIMERS="1", QS_CORAL="1", QS_PRINT_SPECTRUM="1", OMP_NUM_THREADS="8")
+    res = subprocess.run([str(HARNESS), "-i", str(deck), "-e", "spectrum"], env=env, cwd=workdir,
+                         capture_output=True, text=True)
+    if res.returncode != 0:
+        raise SystemExit(f"reference run failed on {deck}:\n{res.stderr[-4000:]}")
+    k = res.stdout.index("cycle ")
+    np.savez_compressed(HERE / "transcript_out.npz", stdout=np.array(res.stdout[k:]),
+                        spectrum=np.array((workdir / "spectrum.dat").read_text()))
+    print("transcript_out.npz: t_coral1")
+
+
 def main(argv: list[str]) -> None:
     import tempfile
+    if "--transcript" in argv:
+        ensure_harness("ref")
+        with tempfile.TemporaryDirectory() as tmp:
+            make_transcript(Path(tmp))
+        return
     if "--timers" in argv:
         ensure_harness("ref")
         with tempfile.TemporaryDirectory() as tmp:

@@ -50,3 +50,64 @@ def assert_flux_close(got: np.ndarray, want: np.ndarray, rel: float = 1e-12, sca
     assert worst <= 1.0, (f"flux error {worst:.3e} x tolerance (max relative "
                           f"{float((np.abs(got[nz] - want[nz]) / denom[nz]).max()):.3e})")
     return worst
+
+
+class OracleMonteCarlo:
+    """Stands in for MonteCarlo under the command-line driver's loop on the
+    CPU (its product path needs a GPU): the same cycles run by the oracle,
+    with the reference's observers restated on the oracle's tallies --
+    fluence per cell (Tallies.cc:100-118, each group added in order) and the
+    census energy spectrum (EnergySpectrum.cc:12-36, the group search of
+    NuclearData.cc:207-228)."""
+
+    def __init__(self, deck):
+        self.problem = deck.build()
+        self.run = oracle_run(self.problem, deck.simulation)
+        self.tracker = None
+        self.rows = []
+        self._fluence = self._spectrum = None
+
+    def observe(self, fluence=False, spectrum=False):
+        G = self.problem.num_groups
+        self._fluence = np.zeros(self.problem.num_cells) if fluence else None
+        self._spectrum = np.zeros(G + 1, dtype=np.uint64) if spectrum else None
+
+    def cycle_init(self):
+        self.run.cycle_init()
+
+    def cycle_tracking(self):
+        self.run.cycle_tracking(8)
+        flux = self.run.flux()
+        self.flux_total = flux.sum()
+        if self._fluence is not None:
+            for g in range(flux.shape[1]):
+                self._fluence += flux[:, g]
+        if self._spectrum is not None:
+            en = self.problem.array("energies")
+            G = self.problem.num_groups
+            e = self.run.processed()["kinetic_energy"]
+            grp = np.minimum(np.searchsorted(en, e, side="right") - 1, G - 1)
+            grp[e <= en[0]] = 0
+            grp[e > en[-1]] = G
+            np.add.at(self._spectrum, grp, 1)
+
+    def cycle_finalize(self):
+        self.run.cycle_finalize()
+        self.rows.append((self.run.last_balance(), self.flux_total))
+
+    def history(self, first, n):
+        from quicksilver_gb300.monte_carlo import CycleHistory
+        rows = self.rows[first:first + n]
+        return CycleHistory(np.array([r[0] for r in rows]), np.array([r[1] for r in rows]))
+
+    def fluence(self):
+        return self._fluence
+
+    def energy_spectrum(self):
+        return [self._spectrum]
+
+    def device_status(self):
+        return 0
+
+    def close(self):
+        pass

@@ -10,7 +10,7 @@ import io
 
 import numpy as np
 
-from helpers import DECKS
+from helpers import DECKS, OracleMonteCarlo
 from quicksilver_gb300.__main__ import TIMERS, timer_report, timer_table
 
 TEXT = str(np.load(DECKS.parent.parent / "tests" / "golden" / "timers_out.npz")["t_homog"])
@@ -56,43 +56,6 @@ def test_cumulative_table_and_figure_of_merit_match_reference():
     timer_report(buf, {k: list(v) for k, v in clock.items()}, num_segments)
     fom = next(l for l in TEXT.split("\n") if l.startswith("Figure Of Merit"))
     assert buf.getvalue() == want + fom + "\n"
-
-
-class OracleMonteCarlo:
-    """Stands in for MonteCarlo under the driver's loop on the CPU: the same
-    cycles run by the oracle (the driver's product path needs a GPU)."""
-
-    def __init__(self, deck):
-        from helpers import oracle_run
-        from quicksilver_gb300.monte_carlo import CycleHistory
-        self.problem = deck.build()
-        self.run = oracle_run(self.problem, deck.simulation)
-        self.tracker = None
-        self.rows, self._history = [], CycleHistory
-
-    def observe(self, fluence=False, spectrum=False):
-        assert not fluence and not spectrum
-
-    def cycle_init(self):
-        self.run.cycle_init()
-
-    def cycle_tracking(self):
-        self.run.cycle_tracking(8)
-        self.flux_total = self.run.flux().sum()
-
-    def cycle_finalize(self):
-        self.run.cycle_finalize()
-        self.rows.append((self.run.last_balance(), self.flux_total))
-
-    def history(self, first, n):
-        rows = self.rows[first:first + n]
-        return self._history(np.array([r[0] for r in rows]), np.array([r[1] for r in rows]))
-
-    def device_status(self):
-        return 0
-
-    def close(self):
-        pass
 
 
 def test_driver_prints_reference_layout(monkeypatch, capsys):
