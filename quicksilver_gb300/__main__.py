@@ -37,13 +37,51 @@ HEADER = ["start", "source", "rr", "split", "absorb", "scatter", "fission", "pro
           "census", "num_seg"]
 
 
-# The reference's flags (Parameters.cc:230-255): short letter -> long name;
-# loadBalance (-l) takes no value.
-SHORT_FLAGS = {"D": "dt", "f": "fMax", "i": "inputFile", "e": "energySpectrum", "S": "crossSectionsOut",
-               "l": "loadBalance", "c": "cycleTimers", "t": "debugThreads", "X": "lx", "Y": "ly", "Z": "lz",
-               "n": "nParticles", "g": "batchSize", "b": "nBatches", "N": "nSteps", "x": "nx", "y": "ny", "z": "nz",
-               "s": "seed", "I": "xDom", "J": "yDom", "K": "zDom", "B": "bTally", "F": "fTally", "C": "cTally"}
+# The reference's flags in its order (Parameters.cc:230-255): long name,
+# short letter, takes a value, value type, help text.  help (-h) and
+# loadBalance (-l) take no value.
+ARGUMENTS = [
+    ("help", "h", 0, "i", "print this message"),
+    ("dt", "D", 1, "d", "time step (seconds)"),
+    ("fMax", "f", 1, "d", "max random mesh node displacement"),
+    ("inputFile", "i", 1, "s", "name of input file"),
+    ("energySpectrum", "e", 1, "s", "name of energy spectrum output file"),
+    ("crossSectionsOut", "S", 1, "s", "name of cross section output file"),
+    ("loadBalance", "l", 0, "i", "enable/disable load balancing"),
+    ("cycleTimers", "c", 1, "i", "enable/disable cycle timers"),
+    ("debugThreads", "t", 1, "i", "set thread debug level to 1, 2, 3"),
+    ("lx", "X", 1, "d", "x-size of simulation (cm)"),
+    ("ly", "Y", 1, "d", "y-size of simulation (cm)"),
+    ("lz", "Z", 1, "d", "z-size of simulation (cm)"),
+    ("nParticles", "n", 1, "u", "number of particles"),
+    ("batchSize", "g", 1, "u", "number of particles in a vault/batch"),
+    ("nBatches", "b", 1, "u", "number of vault/batch to start (sets batchSize automaticaly)"),
+    ("nSteps", "N", 1, "i", "number of time steps"),
+    ("nx", "x", 1, "i", "number of mesh elements in x"),
+    ("ny", "y", 1, "i", "number of mesh elements in y"),
+    ("nz", "z", 1, "i", "number of mesh elements in z"),
+    ("seed", "s", 1, "i", "random number seed"),
+    ("xDom", "I", 1, "i", "number of MPI ranks in x"),
+    ("yDom", "J", 1, "i", "number of MPI ranks in y"),
+    ("zDom", "K", 1, "i", "number of MPI ranks in z"),
+    ("bTally", "B", 1, "i", "number of balance tally replications"),
+    ("fTally", "F", 1, "i", "number of scalar flux tally replications"),
+    ("cTally", "C", 1, "i", "number of scalar cell tally replications"),
+]
+SHORT_FLAGS = {short: name for name, short, _, _, _ in ARGUMENTS if name != "help"}
 COMMAND_LINE_WINS = ("energySpectrum", "crossSectionsOut")   # Parameters.cc:88-90
+
+
+def help_text() -> str:
+    """The reference's argument list as its -h prints it (printArgs,
+    cmdLineParser.cc:123-142: long names padded to the longest), then this
+    driver's own flag."""
+    width = max(len(name) for name, *_ in ARGUMENTS)
+    lines = ["", "  Arguments are: "]
+    lines += [f"   --{name:<{width}} -{short}  arg={arg} type={kind}  {text}" for name, short, arg, kind, text in ARGUMENTS]
+    lines += ["", "", "  --exponential-tally: run as the reference built with -DEXPONENTIAL_TALLY "
+              "(one extra random number per segment, exp of it tallied per cell)", ""]
+    return "\n".join(lines)
 
 
 def parse_command_line(argv) -> tuple:
@@ -113,9 +151,9 @@ def deck_from_command_line(argv) -> tuple:
 
 def main(argv=None) -> int:
     argv = sys.argv[1:] if argv is None else argv
-    if "-h" in argv or "--help" in argv:
-        sys.stdout.write(__doc__)
-        return 0
+    if "-h" in argv or "--help" in argv:   # the reference prints its list and stops (Parameters.cc:263-271)
+        sys.stdout.write(help_text())
+        return 2
     deck, exponential_tally = deck_from_command_line(argv)
     sim = deck.simulation
     cycle_timers = int(deck._echo_values("Simulation", "cycleTimers")[0])

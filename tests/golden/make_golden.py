@@ -53,7 +53,8 @@ the cumulative table and the figure of merit (MC_Fast_Timer.cc:58-104), in
 With ``--transcript`` it stores, for t_coral1 run with ``-e spectrum``, what
 the reference prints from its first summary line to its CORAL2 checks
 (summary lines, cumulative timer table, figure of merit, checks) and the
-spectrum file it writes, in ``transcript_out.npz``.
+spectrum file it writes, and what it prints for ``-h`` (printArgs,
+cmdLineParser.cc:123-142), in ``transcript_out.npz``.
 
 Usage: python tests/golden/make_golden.py [--exponential-tally | --echo | --xsec | --spectrum | --coral |
                                            --summary | --timers | --transcript]
@@ -323,8 +324,11 @@ def make_transcript(workdir: Path) -> None:
     if res.returncode != 0:
         raise SystemExit(f"reference run failed on {deck}:\n{res.stderr[-4000:]}")
     k = res.stdout.index("cycle ")
+    helped = subprocess.run([str(HARNESS), "-h"], cwd=workdir, capture_output=True, text=True)
+    if helped.returncode != 2 or not helped.stdout.startswith("\n  Arguments are: "):
+        raise SystemExit(f"unexpected -h behaviour: rc={helped.returncode}")
     np.savez_compressed(HERE / "transcript_out.npz", stdout=np.array(res.stdout[k:]),
-                        spectrum=np.array((workdir / "spectrum.dat").read_text()))
+                        spectrum=np.array((workdir / "spectrum.dat").read_text()), help=np.array(helped.stdout))
     print("transcript_out.npz: t_coral1")
 
 

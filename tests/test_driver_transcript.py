@@ -7,7 +7,8 @@ cycle the counters and scalar-flux total as the reference prints them, the
 cumulative timer table line for line (times and the reference's per-vault
 call counts aside), the figure-of-merit line, and the four CORAL2 checks
 text for text, fluence verdict and percentage included -- and the energy
-spectrum file byte for byte."""
+spectrum file byte for byte; and ``-h`` printing the reference's argument
+list text for text and stopping with its exit status."""
 import numpy as np
 
 from helpers import DECKS, OracleMonteCarlo
@@ -41,3 +42,10 @@ def test_driver_transcript_matches_reference(monkeypatch, capsys, tmp_path):
         elif not timers and not g.startswith(("cycle ", "Figure Of Merit")):
             assert g == w                                   # the CORAL2 check text
     assert (tmp_path / "spectrum.dat").read_text() == str(GOLD["spectrum"])
+
+
+def test_help_lists_the_reference_arguments(capsys):
+    import quicksilver_gb300.__main__ as M
+    assert M.main(["-h"]) == 2
+    out = capsys.readouterr().out
+    assert out.startswith(str(GOLD["help"])) and "--exponential-tally" in out[len(str(GOLD["help"])):]
