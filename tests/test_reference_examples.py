@@ -78,16 +78,20 @@ def _scaled_copy(deck: Path, tmp_path: Path, **keys) -> Path:
 @pytest.mark.parametrize("deck", DECKS, ids=[str(d.relative_to(EXAMPLES)) for d in DECKS])
 def test_oracle_counters_match_reference_on_its_example_decks(deck, tmp_path):
     """The C oracle against the unmodified reference on its own example decks,
-    scaled to 3000 particles, 2 cycles and a 6^3 mesh in one domain (the
-    counters do not depend on the domain count): all 13 counters bit for bit
-    every cycle."""
+    scaled to 3000 particles, 2 cycles and a 6^3 mesh: all 13 counters bit for
+    bit every cycle.  A deck's own xDom = yDom = zDom = 0 (the reference's four
+    random domains on one rank) is kept; an explicit decomposition, which the
+    reference runs only with one MPI rank per domain, becomes one domain."""
     import numpy as np
     import sys
     sys.path.insert(0, str(ROOT / "tests" / "golden"))
     from make_golden import read_dump
     from helpers import oracle_run
 
-    keys = dict(nParticles=3000, nSteps=2, nx=6, ny=6, nz=6, xDom=1, yDom=1, zDom=1)
+    keys = dict(nParticles=3000, nSteps=2, nx=6, ny=6, nz=6)
+    doms = [int(Deck.from_file(deck)._echo_values("Simulation", k)[0]) for k in ("xDom", "yDom", "zDom")]
+    if any(doms):
+        keys.update(xDom=1, yDom=1, zDom=1)
     if deck.stem == "NonFlatXC":
         # supercritical (fission ratio 1 against absorption 6e-3, nuBar 2.4): within a
         # time step of 1e-8 s the fission chains grow without bound; 1e-10 s keeps them short
@@ -97,6 +101,7 @@ def test_oracle_counters_match_reference_on_its_example_decks(deck, tmp_path):
     env = dict(os.environ, QS_DUMP=str(dump), OMP_NUM_THREADS="4")
     res = subprocess.run([str(HARNESS), "-i", str(small)], env=env, capture_output=True, text=True, timeout=300)
     assert res.returncode == 0, res.stderr[-2000:]
+    assert res.stdout.count("Building partition") == (1 if any(doms) else 4)
     ref = read_dump(dump)
     d = Deck.from_file(small)
     sim, hp = d.simulation, d.build()
