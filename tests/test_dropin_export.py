@@ -1,14 +1,21 @@
 """The drop-in adapter a maintainer adds to the reference
-(oracle/dropin_harness.cc, the code the integration guide shows), compiled
-with the unmodified reference's sources and linked against libqsg.so:
+(oracle/dropin_adapter.hh, the code the integration guide shows), compiled
+with the unmodified reference's sources:
 
-* the table export after initMC: for every bundled deck it passes
+* the table export after initMC, linked against libqsg.so
+  (oracle/dropin_harness.cc): for every bundled deck it passes
   qsg_problem_check (the reference's mesh self-test included), and every
   table it hands the library is, bit for bit, the table this library's own
   deck reader builds (node numbering aside: the reference shares nodes
   between cells, so cell corners are compared as coordinates) -- so what the
   GPU tests prove for deck-built problems holds for a problem exported from
   the reference's own MonteCarlo object;
+* the reference's own main loop with the adapter in place
+  (oracle/dropin_cycle.cc), the library's calls answered on the CPU by a
+  stand-in built on the oracle (oracle/qsg_cpu_standin.c; the GPU tests
+  show the library's tracking is the oracle's): its whole printout --
+  per-cycle counters and flux totals, timer tables, figure of merit, CORAL2
+  checks -- and spectrum file are the unmodified reference's;
 * the cycle adapter's vault and tally halves around the reference's own
   first cycleInit: the particles it gathers from the processing vaults are
   the oracle's, bit for bit; scattering them into the processed vaults and
@@ -31,6 +38,7 @@ from quicksilver_gb300 import Deck
 
 ROOT = Path(__file__).resolve().parent.parent
 HARNESS = ROOT / "oracle" / "_ref" / "qs_dropin_harness"
+CYCLE = ROOT / "oracle" / "_ref" / "qs_dropin_cycle"
 sys.path.insert(0, str(ROOT / "tests" / "golden"))
 from make_golden import read_dump   # noqa: E402
 
@@ -94,5 +102,49 @@ def _block(text: str, name: str) -> str:
                                   "qsgScatterCensus", "qsgAddTallies", "qsgCycleTracking"])
 def test_integration_guide_shows_the_compiled_adapter(name):
     guide = (ROOT / "INTEGRATION.md").read_text()
-    code = (ROOT / "oracle" / "dropin_harness.cc").read_text()
+    code = (ROOT / "oracle" / "dropin_adapter.hh").read_text()
     assert _block(guide, name) == _block(code, name)
+
+
+GOLDEN = ROOT / "tests" / "golden"
+
+
+@pytest.mark.skipif(not CYCLE.exists(), reason="the adapter's main-loop harness is absent")
+def test_reference_main_loop_through_adapter(tmp_path):
+    gold = np.load(GOLDEN / "transcript_out.npz")
+    res = subprocess.run([str(CYCLE), "-i", str(DECKS / "t_coral1.inp"), "-e", "spectrum"], cwd=tmp_path,
+                         capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr[-2000:]
+    got = res.stdout[res.stdout.index("cycle "):].split("\n")
+    want = str(gold["stdout"]).split("\n")
+    assert len(got) == len(want)
+    timers = False
+    for g, w in zip(got, want):
+        gf, wf = g.split(), w.split()
+        assert gf[:1] == wf[:1] and len(g) == len(w), (g, w)
+        if g.startswith("Timer"):
+            timers = True
+        elif g.startswith("Figure Of Merit"):
+            timers = False
+        elif not timers and g[:8].strip().isdigit():
+            assert gf[:14] == wf[:14], (g, w)           # counters and scalar-flux total
+        elif timers and gf and gf[0] in ("main", "cycleInit", "cycleTracking", "cycleFinalize"):
+            assert gf[1] == wf[1], (g, w)                # call counts
+        elif not timers and not g.startswith(("cycle ", "Figure Of Merit")):
+            assert g == w                                # CORAL2 check text
+    assert (tmp_path / "spectrum.dat").read_text() == str(gold["spectrum"])
+
+
+@pytest.mark.skipif(not CYCLE.exists(), reason="the adapter's main-loop harness is absent")
+@pytest.mark.parametrize("name", ["t_homog", "t_fission", "config1"])
+def test_reference_summary_through_adapter(name, tmp_path):
+    want = str(np.load(GOLDEN / "summary_out.npz")[name]).split("\n")
+    res = subprocess.run([str(CYCLE), "-i", str(DECKS / f"{name}.inp")], cwd=tmp_path, capture_output=True,
+                         text=True, timeout=600)
+    assert res.returncode == 0, res.stderr[-2000:]
+    lines = res.stdout.split("\n")
+    k = next(i for i, line in enumerate(lines) if line.startswith("cycle "))
+    got = [line for line in lines[k:] if line.startswith("cycle ") or line[:8].strip().isdigit()]
+    assert got[0] == want[0] and len(got) == len(want)
+    for g, w in zip(got[1:], want[1:]):
+        assert g.split()[:14] == w.split()[:14], (g, w)
