@@ -14,7 +14,8 @@ import numpy as np
 import os
 
 # QSG_LIB=<name> loads lib/libqsg_<name>.so instead of lib/libqsg.so, e.g.
-# QSG_LIB=verify for the screen-verification build (build.py --verify-screen)
+# QSG_LIB=verify for the screen-verification build (build.py --verify-screen),
+# QSG_LIB=nvtx for the build with NVTX ranges (build.py --nvtx)
 _variant = os.environ.get("QSG_LIB", "")
 LIB_PATH = Path(__file__).resolve().parent / "lib" / (f"libqsg_{_variant}.so" if _variant else "libqsg.so")
 
@@ -189,7 +190,7 @@ def lib() -> C.CDLL:
     if _lib is None:
         if not LIB_PATH.exists():
             from . import build as _build
-            _build.build(verify_screen=LIB_PATH.name == "libqsg_verify.so")
+            _build.build(verify_screen=LIB_PATH.name == "libqsg_verify.so", nvtx=LIB_PATH.name == "libqsg_nvtx.so")
         handle = C.CDLL(str(LIB_PATH))
         for name, (args, res) in _SIGNATURES.items():
             fn = getattr(handle, name)

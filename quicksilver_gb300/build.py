@@ -64,15 +64,21 @@ def _run(cmd: list[str]) -> None:
         sys.stderr.write(res.stderr)
 
 
-def build(verbose: bool = False, ptxas_verbose: bool = False, verify_screen: bool = False) -> Path:
+def build(verbose: bool = False, ptxas_verbose: bool = False, verify_screen: bool = False,
+          nvtx: bool = False) -> Path:
     """Compile every translation unit and link ``libqsg.so``; returns its path.
 
     ``verify_screen`` builds ``libqsg_verify.so`` instead: the facet search also
     evaluates every facet the FP32 screen skipped and raises QSG_DEV_SCREEN_MISS
-    if FP64 would have accepted one (a test build; slower).
+    if FP64 would have accepted one (a test build; slower).  ``nvtx`` builds
+    ``libqsg_nvtx.so``: the same library with NVTX ranges around its phases
+    (-DQSG_NVTX).  Either loads with QSG_LIB=verify / QSG_LIB=nvtx.
     """
-    obj_dir = OBJ / ("verify" if verify_screen else "")
-    lib = OUT / ("libqsg_verify.so" if verify_screen else "libqsg.so")
+    if verify_screen and nvtx:
+        raise ValueError("one variant at a time")
+    variant = "verify" if verify_screen else "nvtx" if nvtx else ""
+    obj_dir = OBJ / variant
+    lib = OUT / (f"libqsg_{variant}.so" if variant else "libqsg.so")
     obj_dir.mkdir(parents=True, exist_ok=True)
     nvcc = _nvcc()
     jobs = []
@@ -93,6 +99,8 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, verify_screen: boo
                 flags += ["-Xptxas", "-v"]
             if verify_screen:
                 flags += ["-DQSG_VERIFY_SCREEN"]
+            if nvtx:
+                flags += ["-DQSG_NVTX"]
             jobs.append([nvcc, *NVCC_ARCH, *flags, f"-I{INCLUDE}", f"-I{CSRC}", f"-I{CSRC / 'host'}",
                          "-c", str(src), "-o", str(obj)])
     if jobs:
@@ -112,4 +120,5 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, verify_screen: boo
 
 
 if __name__ == "__main__":
-    build(verbose=True, ptxas_verbose="-v" in sys.argv, verify_screen="--verify-screen" in sys.argv)
+    build(verbose=True, ptxas_verbose="-v" in sys.argv, verify_screen="--verify-screen" in sys.argv,
+          nvtx="--nvtx" in sys.argv)

@@ -667,6 +667,7 @@ extern "C" int qsg_configure_cycle(QsgHandle* h, const QsgCycleConfig* cfg)
 extern "C" int qsg_cycle_init(QsgHandle* h, void* stream)
 {
     QSG_API_BEGIN
+    QSG_RANGE("cycleInit");
     if (!h) return fail(QSG_ERR_INVALID, "qsg_cycle_init: null handle");
     if (!h->cycle_configured) return fail(QSG_ERR_INVALID, "qsg_cycle_init: call qsg_configure_cycle first");
     int st = set_device(h);
@@ -679,6 +680,7 @@ extern "C" int qsg_cycle_init(QsgHandle* h, void* stream)
 extern "C" int qsg_cycle_finalize(QsgHandle* h, void* stream)
 {
     QSG_API_BEGIN
+    QSG_RANGE("cycleFinalize");
     if (!h) return fail(QSG_ERR_INVALID, "qsg_cycle_finalize: null handle");
     if (!h->cycle_configured) return fail(QSG_ERR_INVALID, "qsg_cycle_finalize: call qsg_configure_cycle first");
     int st = set_device(h);
@@ -699,6 +701,7 @@ static bool same_roles(const QsgHandle* h, const QsgHandle::GraphEntry& g)
 extern "C" int qsg_run_cycles(QsgHandle* h, int32_t n_cycles, int32_t use_graph, void* stream)
 {
     QSG_API_BEGIN
+    QSG_RANGE("qsg_run_cycles");
     if (!h || n_cycles < 0) return fail(QSG_ERR_INVALID, "qsg_run_cycles: bad argument");
     if (!h->cycle_configured) return fail(QSG_ERR_INVALID, "qsg_run_cycles: call qsg_configure_cycle first");
     int st = set_device(h);

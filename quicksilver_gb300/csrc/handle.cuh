@@ -12,6 +12,24 @@
 #include "status.h"
 #include "track_device.cuh"
 
+// NVTX ranges around the phases, named as the reference's -DUSE_NVTX build
+// names them (NVTX_Range.hh; main.cc:175), for profilers that filter or
+// group by range.  Off unless built with -DQSG_NVTX
+// (python -m quicksilver_gb300.build --nvtx): then QSG_RANGE opens a range
+// that closes at the end of the enclosing scope.
+#ifdef QSG_NVTX
+#include <nvtx3/nvToolsExt.h>
+struct QsgNvtxRange {
+    explicit QsgNvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~QsgNvtxRange() { nvtxRangePop(); }
+    QsgNvtxRange(const QsgNvtxRange&) = delete;
+    QsgNvtxRange& operator=(const QsgNvtxRange&) = delete;
+};
+#define QSG_RANGE(name) QsgNvtxRange qsg_nvtx_range_(name)
+#else
+#define QSG_RANGE(name) ((void)0)
+#endif
+
 namespace qsg {
 
 #define QSG_CUDA(call)                                                                      \

@@ -2157,6 +2157,7 @@ extern "C" int qsg_track_host(QsgHandle* h, const QsgParticleSoA* particles, uin
                               uint64_t census_capacity, uint64_t* n_census, void* stream)
 {
     QSG_API_BEGIN
+    QSG_RANGE("cycleTracking_TrackingKernel");
     if (!h || !n_census) return fail(QSG_ERR_INVALID, "qsg_track_host: null argument");
     *n_census = 0;
     if (h->sens.K > 0)
@@ -2215,6 +2216,7 @@ extern "C" int qsg_track_host(QsgHandle* h, const QsgParticleSoA* particles, uin
 extern "C" int qsg_track_cycle(QsgHandle* h, void* stream)
 {
     QSG_API_BEGIN
+    QSG_RANGE("cycleTracking_TrackingKernel");
     if (!h) return fail(QSG_ERR_INVALID, "qsg_track_cycle: null handle");
     int st = set_device(h);
     if (st) return st;
@@ -2225,6 +2227,7 @@ extern "C" int qsg_track_cycle(QsgHandle* h, void* stream)
 extern "C" int qsg_track_cycle_async(QsgHandle* h, void* stream)
 {
     QSG_API_BEGIN
+    QSG_RANGE("cycleTracking_TrackingKernel");
     if (!h) return fail(QSG_ERR_INVALID, "qsg_track_cycle_async: null handle");
     int st = set_device(h);
     if (st) return st;
@@ -2235,6 +2238,7 @@ extern "C" int qsg_track_cycle_async(QsgHandle* h, void* stream)
 extern "C" int qsg_track_cycle_sync(QsgHandle* h)
 {
     QSG_API_BEGIN
+    QSG_RANGE("cycleTracking_TrackingKernel");
     if (!h) return fail(QSG_ERR_INVALID, "qsg_track_cycle_sync: null handle");
     int st = set_device(h);
     if (st) return st;
@@ -2494,6 +2498,7 @@ extern "C" int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* p
                                            double* flux, uint64_t* balance, void* stream)
 {
     QSG_API_BEGIN
+    QSG_RANGE("cycleTracking_TrackingKernel");
     if (!h || !n_census) return fail(QSG_ERR_INVALID, "qsg_track_particles_noalloc: null handle or n_census");
     int st = set_device(h);
     if (st) return st;

@@ -26,6 +26,17 @@ def test_library_exports_every_declared_symbol(native_lib):
         assert hasattr(native_lib, name), f"{name} declared in qsg.h but not exported"
 
 
+def test_nvtx_build_exports_the_same_abi():
+    """The variant with NVTX ranges around its phases (build.py --nvtx,
+    -DQSG_NVTX, as the reference's -DUSE_NVTX) builds and exports the same
+    functions."""
+    from quicksilver_gb300 import build
+    lib = ctypes.CDLL(str(build.build(nvtx=True)))
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    assert lib.qsg_abi_version() == 1
+
+
 def test_abi_version(native_lib):
     assert native_lib.qsg_abi_version() == 1
 
