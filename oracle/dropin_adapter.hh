@@ -115,6 +115,10 @@ static QsgExport g_export;   // qsg_create copies the tables; the cycle code bel
 
 void qsgAttach(MonteCarlo* mc)
 {
+    if (mc->domain.size() != 1) {   // xDom = yDom = zDom = 1 tracks the same histories as the 4-domain default
+        printf("qsgAttach: %d domains; the library tracks one (set xDom = yDom = zDom = 1)\n", (int)mc->domain.size());
+        return;
+    }
     qsgExport(mc, g_export);
     QsgOptions o{};
     o.flux_replicas = mc->_params.simulationParams.fluxTallyReplications;

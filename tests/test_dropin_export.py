@@ -148,3 +148,16 @@ def test_reference_summary_through_adapter(name, tmp_path):
     assert got[0] == want[0] and len(got) == len(want)
     for g, w in zip(got[1:], want[1:]):
         assert g.split()[:14] == w.split()[:14], (g, w)
+
+
+@pytest.mark.skipif(not CYCLE.exists(), reason="the adapter's main-loop harness is absent")
+def test_adapter_refuses_more_than_one_domain(tmp_path):
+    """The reference's one-rank default (xDom = yDom = zDom = 0) builds four
+    domains; the adapter hands the library one and says so instead."""
+    text = (DECKS / "t_homog.inp").read_text()
+    for key in ("xDom", "yDom", "zDom"):
+        text = text.replace(f"   {key}: 1\n", f"   {key}: 0\n")
+    deck = tmp_path / "four_domains.inp"
+    deck.write_text(text)
+    res = subprocess.run([str(CYCLE), "-i", str(deck)], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert res.returncode == 2 and "qsgAttach: 4 domains" in res.stdout
