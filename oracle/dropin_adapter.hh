@@ -125,6 +125,13 @@ void qsgAttach(MonteCarlo* mc)
     if (qsg_create(&g_export.problem, &o, &g_qsg) != QSG_OK) {
         char e[512]; qsg_last_error(e, sizeof e); printf("%s\n", e);
     }
+#ifdef EXPONENTIAL_TALLY   // the reference built with it: the library draws and tallies the same (CycleTracking.cc:48-50)
+    if (g_qsg && qsg_set_exponential_tally(g_qsg, 1) != QSG_OK) {
+        char e[512]; qsg_last_error(e, sizeof e); printf("%s\n", e);
+        qsg_destroy(g_qsg);
+        g_qsg = nullptr;
+    }
+#endif
 }
 
 // MC_Base_Particle records (MC_Base_Particle.hh:75-92) as host columns, and
@@ -208,6 +215,16 @@ void qsgAddTallies(MonteCarlo* mc, const uint64_t* bal, const double* flux)
         for (int g = 0; g < G; ++g) t._cell[c]._group[g] += flux[(size_t)c * G + g];
 }
 
+#ifdef EXPONENTIAL_TALLY
+// the cycle's exponential cell tally [cell] -> the first cell-tally replica
+// (Tallies.hh:126-165), which cycleFinalize resets (Tallies.cc:91)
+void qsgAddCellTally(MonteCarlo* mc, const double* cell_tally)
+{
+    CellTallyTask& t = mc->_tallies->_cellTallyDomain[0]._task[0];
+    for (int c = 0; c < g_export.problem.num_cells; ++c) t._cell[c] += cell_tally[c];
+}
+#endif
+
 // replaces cycleTracking (main.cc:138-307): the processing vaults tracked in
 // one call, fission products included; census particles land in the
 // processed vaults and the cycle's tallies in the reference's Tallies
@@ -225,6 +242,10 @@ void qsgCycleTracking(MonteCarlo* mc)
     if (rc == QSG_OK) rc = qsg_sizes(g_qsg, &n_processing, &n_census);
     if (rc == QSG_OK) { census.resize(n_census); rc = qsg_get_census(g_qsg, &census.soa, n_census, &n_census); }
     if (rc == QSG_OK) rc = qsg_read_tallies(g_qsg, bal, flux.data());
+#ifdef EXPONENTIAL_TALLY
+    std::vector<double> cell_tally(g_export.problem.num_cells);
+    if (rc == QSG_OK) rc = qsg_read_cell_tally(g_qsg, cell_tally.data());
+#endif
     if (rc == QSG_OK) rc = qsg_reset_tallies(g_qsg);
     MC_FASTTIMER_STOP(MC_Fast_Timer::cycleTracking_Kernel);
     if (rc != QSG_OK) { char e[512]; qsg_last_error(e, sizeof e); printf("%s\n", e); }
@@ -232,6 +253,9 @@ void qsgCycleTracking(MonteCarlo* mc)
     if (rc == QSG_OK) {
         qsgScatterCensus(census, n_census, pvc);
         qsgAddTallies(mc, bal, flux.data());
+#ifdef EXPONENTIAL_TALLY
+        qsgAddCellTally(mc, cell_tally.data());
+#endif
     }
     MC_FASTTIMER_STOP(MC_Fast_Timer::cycleTracking);
 }

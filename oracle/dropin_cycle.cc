@@ -8,7 +8,11 @@
 // reference's sources, the adapter (oracle/dropin_adapter.hh) and the CPU
 // stand-in for libqsg's tracking calls (oracle/qsg_cpu_standin.c, answered
 // by the C oracle), so it runs without a GPU; the tests compare its printout
-// with the unmodified reference's.  Exit status 2 when qsgAttach fails.
+// with the unmodified reference's.  Built with -DEXPONENTIAL_TALLY
+// (`make dropin_cycle_exp`) it also prints, after each cycle's tracking, the
+// cell tally the adapter handed to the reference's Tallies
+// ("cell_tally_total <sum>", summed in cell order).  Exit status 2 when
+// qsgAttach fails.
 
 #include <cstdio>
 
@@ -33,6 +37,12 @@ int main(int argc, char** argv)
     for (int ii = 0; ii < params.simulationParams.nSteps; ++ii) {
         cycleInit(bool(params.simulationParams.loadBalance));
         qsgCycleTracking(mcco);
+#ifdef EXPONENTIAL_TALLY
+        double total = 0.0;
+        const CellTallyTask& t = mcco->_tallies->_cellTallyDomain[0]._task[0];
+        for (int c = 0; c < t._cell.size(); ++c) total += t._cell[c];
+        printf("cell_tally_total %.17g\n", total);
+#endif
         cycleFinalize();
         mcco->fast_timer->Last_Cycle_Report(params.simulationParams.cycleTimers, mcco->processor_info->rank,
                                             mcco->processor_info->num_processors,

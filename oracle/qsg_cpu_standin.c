@@ -30,6 +30,7 @@ struct QsgHandle {
     uint64_t n_census;
     uint64_t balance[QSG_BAL_COUNT];
     double* flux;
+    double* cell_tally;   /* NULL unless qsg_set_exponential_tally turned it on */
 };
 
 static char g_error[512];
@@ -69,7 +70,7 @@ int qsg_create(const QsgProblem* problem, const QsgOptions* options, QsgHandle**
 
 int qsg_destroy(QsgHandle* h)
 {
-    if (h) { free(h->in); free(h->census); free(h->flux); free(h); }
+    if (h) { free(h->in); free(h->census); free(h->flux); free(h->cell_tally); free(h); }
     return QSG_OK;
 }
 
@@ -105,7 +106,12 @@ int qsg_track_cycle_sync(QsgHandle* h)
         if (!census) { free(flux); return fail(QSG_ERR_CAPACITY, "qsg_track_cycle_sync: out of host memory"); }
         uint64_t bal[QSG_BAL_COUNT] = {0}, n_census = 0;
         memset(flux, 0, (nf ? nf : 1) * sizeof(double));
-        const int rc = oracle_track(h->problem, h->in, h->n_in, census, cap, &n_census, bal, flux, 8);
+        const size_t nc = h->cell_tally ? (size_t)h->problem->num_cells : 0;
+        double* cell = nc ? (double*)calloc(nc, sizeof(double)) : NULL;
+        if (nc && !cell) { free(census); free(flux); return fail(QSG_ERR_CAPACITY, "out of host memory"); }
+        const int rc = oracle_track_cell_tally(h->problem, h->in, h->n_in, census, cap, &n_census, bal, flux, cell, 8);
+        for (size_t k = 0; k < nc && rc == 0; ++k) h->cell_tally[k] += cell[k];
+        free(cell);
         if (rc == -3) {   /* fission grew the census past its room: again, with room for all of it */
             free(census);
             cap = n_census + 16;
@@ -165,5 +171,23 @@ int qsg_reset_tallies(QsgHandle* h)
     if (!h) return fail(QSG_ERR_INVALID, "qsg_reset_tallies: null handle");
     memset(h->balance, 0, sizeof h->balance);
     memset(h->flux, 0, flux_size(h) * sizeof(double));
+    if (h->cell_tally) memset(h->cell_tally, 0, (size_t)h->problem->num_cells * sizeof(double));
+    return QSG_OK;
+}
+
+/* The -DEXPONENTIAL_TALLY build's draw and cell tally (oracle_track_cell_tally). */
+int qsg_set_exponential_tally(QsgHandle* h, int32_t enabled)
+{
+    if (!h || (enabled != 0 && enabled != 1)) return fail(QSG_ERR_INVALID, "qsg_set_exponential_tally: bad argument");
+    free(h->cell_tally);
+    h->cell_tally = enabled ? (double*)calloc((size_t)h->problem->num_cells + 1, sizeof(double)) : NULL;
+    return enabled && !h->cell_tally ? fail(QSG_ERR_CAPACITY, "out of host memory") : QSG_OK;
+}
+
+int qsg_read_cell_tally(QsgHandle* h, double* cell_tally)
+{
+    if (!h || !cell_tally) return fail(QSG_ERR_INVALID, "qsg_read_cell_tally: null argument");
+    if (!h->cell_tally) return fail(QSG_ERR_INVALID, "qsg_read_cell_tally: the exponential tally is off");
+    memcpy(cell_tally, h->cell_tally, (size_t)h->problem->num_cells * sizeof(double));
     return QSG_OK;
 }

@@ -39,6 +39,7 @@ from quicksilver_gb300 import Deck
 ROOT = Path(__file__).resolve().parent.parent
 HARNESS = ROOT / "oracle" / "_ref" / "qs_dropin_harness"
 CYCLE = ROOT / "oracle" / "_ref" / "qs_dropin_cycle"
+CYCLE_EXP = ROOT / "oracle" / "_ref_exp" / "qs_dropin_cycle"
 sys.path.insert(0, str(ROOT / "tests" / "golden"))
 from make_golden import read_dump   # noqa: E402
 
@@ -161,3 +162,30 @@ def test_adapter_refuses_more_than_one_domain(tmp_path):
     deck.write_text(text)
     res = subprocess.run([str(CYCLE), "-i", str(deck)], cwd=tmp_path, capture_output=True, text=True, timeout=300)
     assert res.returncode == 2 and "qsgAttach: 4 domains" in res.stdout
+
+
+@pytest.mark.skipif(not CYCLE_EXP.exists(), reason="the adapter's main-loop harness for -DEXPONENTIAL_TALLY is absent")
+@pytest.mark.parametrize("name", ["t_homog", "t_fission"])
+def test_exponential_tally_build_through_adapter(name, tmp_path):
+    """The reference built with -DEXPONENTIAL_TALLY, the adapter switching the
+    library's exponential tally on: every cycle's counters are that build's
+    (tests/golden/exp_<deck>.npz, from the unmodified reference built with the
+    define) and the cell tally handed to its Tallies sums to that build's
+    within 1e-12."""
+    from quicksilver_gb300 import _native as N
+    gold = np.load(GOLDEN / f"exp_{name}.npz")
+    res = subprocess.run([str(CYCLE_EXP), "-i", str(DECKS / f"{name}.inp")], cwd=tmp_path, capture_output=True,
+                         text=True, timeout=600)
+    assert res.returncode == 0, res.stderr[-2000:]
+    lines = res.stdout.split("\n")
+    totals = [float(line.split()[1]) for line in lines if line.startswith("cell_tally_total ")]
+    k = next(i for i, line in enumerate(lines) if line.startswith("cycle "))
+    rows = [line.split() for line in lines[k + 1:] if line[:8].strip().isdigit()]
+    cols = ["start", "source", "rr", "split", "absorb", "scatter", "fission", "produce", "collision", "escape",
+            "census", "num_segments"]
+    assert len(rows) == len(totals) == len(gold["balance"])
+    for c, row in enumerate(rows):
+        for j, col in enumerate(cols):
+            assert int(row[1 + j]) == int(gold["balance"][c][N.BAL[col]]), (c, col)
+        want = gold["cell_tally"][c].sum()
+        assert abs(totals[c] - want) <= 1e-12 * want, c
