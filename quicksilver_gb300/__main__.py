@@ -165,6 +165,10 @@ def main(argv=None) -> int:
         mc.exponential_tally(True)
     out = sys.stdout
     out.write(deck.text() + "\n")
+    # initMC's progress lines for the one domain tracked here (initMC.cc:295-319);
+    # the mesh self-test they bracket ran in qsg_create (initMC.cc:202-234)
+    out.write("Building partition 0\ndone building\nBuilding MC_Domain 0\n"
+              "Starting Consistency Check\nFinished Consistency Check\nFinished initMesh\n")
     if deck.cross_sections_out:   # written by initMC in the reference (initMC.cc:392-490)
         write_cross_sections(deck.cross_sections_out, mc.problem, deck.material_names)
     out.write(summary_header() + (" %14s" % "cell_tally" if exponential_tally else "") + "\n")

@@ -51,8 +51,8 @@ the cumulative table and the figure of merit (MC_Fast_Timer.cc:58-104), in
 ``timers_out.npz``.
 
 With ``--transcript`` it stores, for t_coral1 run with ``-e spectrum``, what
-the reference prints from its first summary line to its CORAL2 checks
-(summary lines, cumulative timer table, figure of merit, checks) and the
+the reference prints after its deck echo (initMC's progress lines, summary
+lines, cumulative timer table, figure of merit, CORAL2 checks) and the
 spectrum file it writes, and what it prints for ``-h`` (printArgs,
 cmdLineParser.cc:123-142), in ``transcript_out.npz``.
 
@@ -323,7 +323,7 @@ def make_transcript(workdir: Path) -> None:
                          capture_output=True, text=True)
     if res.returncode != 0:
         raise SystemExit(f"reference run failed on {deck}:\n{res.stderr[-4000:]}")
-    k = res.stdout.index("cycle ")
+    k = res.stdout.index("Building partition 0")
     helped = subprocess.run([str(HARNESS), "-h"], cwd=workdir, capture_output=True, text=True)
     if helped.returncode != 2 or not helped.stdout.startswith("\n  Arguments are: "):
         raise SystemExit(f"unexpected -h behaviour: rc={helped.returncode}")

@@ -2,7 +2,8 @@
 the reference's own (tests/golden/transcript_out.npz, make_golden.py
 --transcript: t_coral1 run with ``-e spectrum``), with the oracle standing
 in for the GPU under the driver's loop (tests/helpers.OracleMonteCarlo):
-from the first summary line on, the same lines in the same order -- per
+after the deck echo, the same lines in the same order -- initMC's progress
+lines text for text, per
 cycle the counters and scalar-flux total as the reference prints them, the
 cumulative timer table line for line (times and the reference's per-vault
 call counts aside), the figure-of-merit line, and the four CORAL2 checks
@@ -24,7 +25,7 @@ def test_driver_transcript_matches_reference(monkeypatch, capsys, tmp_path):
     stem = tmp_path / "spectrum"
     assert M.main([str(DECKS / "t_coral1.inp"), "-e", str(stem)]) == 0
     out = capsys.readouterr().out
-    got = out[out.index("cycle "):].split("\n")
+    got = out[out.index("Building partition 0"):].split("\n")
     want = str(GOLD["stdout"]).split("\n")
     assert len(got) == len(want)
     timers = False

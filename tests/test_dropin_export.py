@@ -116,7 +116,7 @@ def test_reference_main_loop_through_adapter(tmp_path):
     res = subprocess.run([str(CYCLE), "-i", str(DECKS / "t_coral1.inp"), "-e", "spectrum"], cwd=tmp_path,
                          capture_output=True, text=True, timeout=600)
     assert res.returncode == 0, res.stderr[-2000:]
-    got = res.stdout[res.stdout.index("cycle "):].split("\n")
+    got = res.stdout[res.stdout.index("Building partition 0"):].split("\n")
     want = str(gold["stdout"]).split("\n")
     assert len(got) == len(want)
     timers = False
