@@ -15,7 +15,9 @@ with the unmodified reference's sources:
   stand-in built on the oracle (oracle/qsg_cpu_standin.c; the GPU tests
   show the library's tracking is the oracle's): its whole printout --
   per-cycle counters and flux totals, timer tables, figure of merit, CORAL2
-  checks -- and spectrum file are the unmodified reference's;
+  checks -- and spectrum file are the unmodified reference's; with the
+  reference built with -DEXPONENTIAL_TALLY, that build's counters and cell
+  tally; a four-domain MonteCarlo is refused with a message;
 * the cycle adapter's vault and tally halves around the reference's own
   first cycleInit: the particles it gathers from the processing vaults are
   the oracle's, bit for bit; scattering them into the processed vaults and
