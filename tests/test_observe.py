@@ -3,7 +3,7 @@ on balances with known verdicts, on the oracle's run of a CORAL-style deck,
 and the energy-spectrum file format (EnergySpectrum.cc:38-59)."""
 import numpy as np
 
-from helpers import load_problem, oracle_run
+from helpers import OracleMonteCarlo, load_problem
 from quicksilver_gb300 import _native as N
 from quicksilver_gb300.observe import (balance_event_test, balance_ratio_test, coral_benchmark_correctness,
                                        cumulative_balance, fluence_test, missing_particle_test,
@@ -45,30 +45,18 @@ def test_fluence_verdicts():
 
 
 def oracle_observe(name, cycles=None):
-    """The oracle's run with the reference's observers restated: fluence per
-    cell (Tallies.cc:100-118: each group added in order), the census energy
-    spectrum (EnergySpectrum.cc:12-36, NuclearData.cc:207-228 group search)."""
-    _, sim, hp = load_problem(name)
-    run = oracle_run(hp, sim)
-    en = hp.array("energies")
-    G = hp.num_groups
-    fluence = np.zeros(hp.num_cells)
-    spectrum = np.zeros(G + 1, dtype=np.uint64)
-    hist = []
-    for _ in range(sim.n_steps if cycles is None else cycles):
-        run.cycle_init()
-        run.cycle_tracking(0)
-        flux = run.flux()
-        for g in range(G):
-            fluence += flux[:, g]
-        e = run.processed()["kinetic_energy"]
-        grp = np.minimum(np.searchsorted(en, e, side="right") - 1, G - 1)
-        grp[e <= en[0]] = 0
-        grp[e > en[-1]] = G
-        np.add.at(spectrum, grp, 1)
-        run.cycle_finalize()
-        hist.append(run.last_balance())
-    return np.array(hist), fluence, spectrum, en
+    """The oracle's run with the reference's observers restated
+    (helpers.OracleMonteCarlo): cumulative counters per cycle, fluence per
+    cell, census energy spectrum, group edges."""
+    deck, sim, _ = load_problem(name)
+    mc = OracleMonteCarlo(deck)
+    mc.observe(fluence=True, spectrum=True)
+    n = sim.n_steps if cycles is None else cycles
+    for _ in range(n):
+        mc.cycle_init()
+        mc.cycle_tracking()
+        mc.cycle_finalize()
+    return mc.history(0, n).balance, mc.fluence(), mc.energy_spectrum()[0], mc.problem.array("energies")
 
 
 def test_coral_checks_on_oracle_run(tmp_path):
