@@ -47,7 +47,10 @@ WORKLOAD = ("config2: 40^3-cell 40 cm cube, 3 materials in spherical shells (r=8
             "3 reactions each, polynomial cross sections, 230 groups, 1e6 particles, FP64")
 METRIC = "segments/s per cycle on 1 GB300; batched+adjoint vs plain at matched tally error"
 B_ALG_PER_SEGMENT = 288          # algorithmic HBM bytes per segment (136-B record read+write + 16-B flux RMW)
-PROFILE_SUMMARY = ROOT / "profiles" / "track_pool_kernel_config2.md"
+# per-segment ncu figures of the tracking kernel on this workload, with the
+# hash of the kernel sources they were captured from
+PROFILE_DATA = ROOT / "profiles" / "track_pool_kernel_config2.json"
+KERNEL_SOURCES = [ROOT / "quicksilver_gb300" / "csrc" / "track.cu", ROOT / "quicksilver_gb300" / "csrc" / "track_device.cuh"]
 
 
 def dist_env():
@@ -118,22 +121,22 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def profile_value(key: str):
-    """A per-segment figure (``key: value`` line) of the committed ncu summary."""
-    if not PROFILE_SUMMARY.exists():
-        return None
-    for line in PROFILE_SUMMARY.read_text().splitlines():
-        if line.strip().startswith(key + ":"):
-            try:
-                return float(line.split(":", 1)[1].strip().split()[0])
-            except ValueError:
-                return None
-    return None
+def kernel_source_hash() -> str:
+    import hashlib
+    h = hashlib.sha256()
+    for p in KERNEL_SOURCES:
+        h.update(p.read_bytes())
+    return h.hexdigest()
 
 
-def profile_traffic_per_segment():
-    """DRAM bytes per segment of the tracking kernel from the committed ncu summary."""
-    return profile_value("traffic_bytes_per_segment")
+def profile_figures():
+    """(figures, matches): the committed ncu per-segment figures and whether
+    they were captured from the kernel sources as they are now.  Figures
+    from other sources are reported as stale and not used."""
+    if not PROFILE_DATA.exists():
+        return None, False
+    data = json.loads(PROFILE_DATA.read_text())
+    return data, data.get("kernel_source_sha256") == kernel_source_hash()
 
 
 def fp64_roofline(fp64_per_segment, segments_per_s_per_gpu, peak):
@@ -146,11 +149,15 @@ def fp64_roofline(fp64_per_segment, segments_per_s_per_gpu, peak):
     return {"achieved": achieved, "peak": peak, "unit": "FP64 warp instructions/s", "frac": achieved / peak,
             "fp64_warp_instructions_per_segment": fp64_per_segment,
             "peak_source": "measured in this run (qsg_measure_fp64_rate: independent DFMA chains, 16 warps/SM)",
-            "per_segment_source": "ncu sm__inst_executed_pipe_fp64.sum / segments, " + PROFILE_SUMMARY.name}
+            "per_segment_source": "ncu sm__inst_executed_pipe_fp64.sum / segments, " + PROFILE_DATA.name}
 
 
-def cpu_port_rate(deck_path: Path, cycles: int, threads: int):
-    """The CPU port (oracle) timed on the host cores: (segments/s, segments, seconds)."""
+def cpu_port_rate(deck_path: Path, warmup: int, steps: int, threads: int):
+    """The CPU port (oracle) on the host cores, timed as the reference arm
+    times it: `warmup` whole cycles, then the tracking of `steps` cycles
+    with `threads` OpenMP threads, then one more cycle on one core.  Returns
+    (segments/s, segments, seconds, 1-core segments/s, 1-core segments,
+    1-core seconds)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle_py
     from quicksilver_gb300 import Deck
@@ -159,17 +166,26 @@ def cpu_port_rate(deck_path: Path, cycles: int, threads: int):
     hp = deck.build()
     run = oracle_py.OracleRun(hp.ptr, hp.num_cells, hp.num_groups, hp.source_rates(), sim.n_particles,
                               sim.e_min, sim.e_max, sim.low_weight_cutoff, sim.load_balance, keepalive=hp)
-    seg = 0
-    secs = 0.0
-    for _ in range(cycles):
+
+    def one(nthreads):
         run.cycle_init()
         t0 = time.perf_counter()
-        run.cycle_tracking(threads)
-        secs += time.perf_counter() - t0
-        seg += int(run.balance()[12])
+        run.cycle_tracking(nthreads)
+        dt = time.perf_counter() - t0
+        n = int(run.balance()[12])
         run.cycle_finalize()
+        return n, dt
+
+    for _ in range(warmup):
+        one(threads)
+    seg, secs = 0, 0.0
+    for _ in range(steps):
+        n, dt = one(threads)
+        seg += n
+        secs += dt
+    seg1, secs1 = one(1)
     run.close()
-    return seg / secs, seg, secs
+    return seg / secs, seg, secs, seg1 / secs1, seg1, secs1
 
 
 def _sync():
@@ -216,6 +232,7 @@ def measure_batched(tune_space=None):
         bmc.close()
     # the plain path, problem by problem, from the same starting state (one warm-up cycle)
     t_plain, seg_plain, same = 0.0, 0, True
+    per_problem = []
     for p, (d, hp, off) in enumerate(zip(decks, problems, offs)):
         mc = MonteCarlo(d, problem=hp, seed_offset=off)
         try:
@@ -224,12 +241,48 @@ def measure_batched(tune_space=None):
             t0 = time.perf_counter()
             h = mc.run(cycles)
             _sync()
-            t_plain += time.perf_counter() - t0
+            dt = time.perf_counter() - t0
+            t_plain += dt
             seg_plain += h.segments()
+            per_problem.append((dt, h.segments()))
             same &= bool(np.array_equal(h.balance, hb.balance[:, p, :]))
         finally:
             mc.close()
     seg_b = hb.segments()
+    # breakdown: per mesh edge, the plain path's time and rate beside the same
+    # problems batched on their own; per particle-count decade, the plain rate
+    edges = [int(d.simulation.nx) for d in decks]
+    npart = [int(d.simulation.n_particles) for d in decks]
+    by_edge = {}
+    for e in sorted(set(edges)):
+        idx = [p for p in range(len(decks)) if edges[p] == e]
+        tp = sum(per_problem[p][0] for p in idx)
+        sp = sum(per_problem[p][1] for p in idx)
+        sub = BatchMonteCarlo([decks[p] for p in idx], problems=[problems[p] for p in idx],
+                              seed_offsets=[offs[p] for p in idx], flux_replicas=best["flux_replicas"])
+        try:
+            sub.tune(**{k: best[k] for k in ("block_size", "pool_collision_step", "pool_refill") if k in best})
+            sub.run(1, use_graph=True)
+            f0 = sub.cycles
+            _sync()
+            t0 = time.perf_counter()
+            sub.run_cycles(cycles, use_graph=True)
+            _sync()
+            tb = time.perf_counter() - t0
+            sb = sub.history(f0, cycles).segments()
+        finally:
+            sub.close()
+        by_edge[str(e)] = {"problems": len(idx), "empty_problems": sum(1 for p in idx if per_problem[p][1] == 0),
+                           "segments": sp, "plain_s": tp, "plain_segments_per_s": sp / tp if tp else None,
+                           "batched_alone_s": tb, "batched_alone_segments_per_s": sb / tb if tb else None,
+                           "speedup_batched_alone": (tp / tb) if tb else None}
+    by_particles = {}
+    for lo, hi in ((1e4, 1e5), (1e5, 1e6), (1e6, 2e6 + 1)):
+        idx = [p for p in range(len(decks)) if lo <= npart[p] < hi]
+        tp = sum(per_problem[p][0] for p in idx)
+        sp = sum(per_problem[p][1] for p in idx)
+        by_particles[f"{lo:.0e}-{min(hi, 2e6):.0e}"] = {"problems": len(idx), "segments": sp, "plain_s": tp,
+                                                        "plain_segments_per_s": sp / tp if tp else None}
     for hp in problems:
         hp.close()
     return {"workload": "64 independent problems (mesh edge from {8,16,24,32,48} cm, 1e4-2e6 particles "
@@ -238,6 +291,7 @@ def measure_batched(tune_space=None):
             "plain_problem_by_problem_segments_per_s": seg_plain / t_plain, "plain_s": t_plain,
             "speedup_at_equal_tally_error": (seg_b / t_batch) / (seg_plain / t_plain),
             "segments": seg_b, "balance_bit_exact_vs_plain": same, "device_flags": flags,
+            "by_mesh_edge": by_edge, "by_particle_count": by_particles,
             "tuning": {k: best[k] for k in ("block_size", "pool_collision_step", "pool_refill", "flux_replicas")},
             "tune_s": tune_s, "timing": "wall clock, whole cycles, synchronised"}
 
@@ -316,7 +370,12 @@ def measure_adjoint(replicas=6):
         res[h] = (float(np.median(ratio)), float(ratio.min()), float(ratio.max()))
     rate_plain = seg_plain / t_plain
     rate_sens = seg_sens / t_sens
+    # plain runs needed per sensitivity run at equal standard error, per
+    # component: the median component is the headline, the worst and best
+    # beside it
     speedup = 2 * K * res[1e-2][0] * (t_plain / t_sens)
+    speedups = {"min": 2 * K * res[1e-2][1] * (t_plain / t_sens), "median": speedup,
+                "max": 2 * K * res[1e-2][2] * (t_plain / t_sens)}
     return {"workload": "config4: 10^3 cells, 10 cm box, 3 materials (spheres r=2, 4 cm), escape boundaries, "
                         "230 groups, 1e6 particles, 20 cycles; 12 scale parameters",
             "params": K, "replicas": replicas,
@@ -326,6 +385,7 @@ def measure_adjoint(replicas=6):
                                                               "max": res[1e-2][2]},
             "variance_ratio_fd_step_1e-4": {"median": res[1e-4][0], "min": res[1e-4][1], "max": res[1e-4][2]},
             "speedup_at_equal_tally_error": speedup,
+            "speedup_at_equal_tally_error_over_components": speedups,
             "effective_segments_per_s": speedup * rate_plain,
             "timing": "wall clock of MonteCarlo.run (20 whole cycles), synchronised; handle set-up excluded"}
 
@@ -607,7 +667,9 @@ def main():
     peak, peak_kind = measured_peak_hbm()
     seg_per_launch = segments / world / args.steps
     achieved = B_ALG_PER_SEGMENT * seg_per_launch / (track_s / args.steps) / 1e9
-    tps = profile_traffic_per_segment()
+    prof, prof_current = profile_figures()
+    tps = prof.get("dram_bytes_per_segment") if (prof and prof_current) else None
+    fp64_ps = prof.get("fp64_warp_instructions_per_segment") if (prof and prof_current) else None
     line = {
         "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * track_s / args.steps, "higher_is_better": True,
@@ -622,8 +684,9 @@ def main():
                      "traffic": (tps * seg_per_launch) if tps else None,
                      "algorithmic_bytes_per_segment": B_ALG_PER_SEGMENT,
                      "note": "not HBM-bound: the binding roof is FP64 issue (fp64_issue)",
-                     "fp64_issue": fp64_roofline(profile_value("fp64_warp_instructions_per_segment"),
-                                                 seg_per_launch / (track_s / args.steps), fp64_peak)},
+                     "profile": {"file": str(PROFILE_DATA.relative_to(ROOT)), "matches_kernel_source": prof_current,
+                                 "captured": prof.get("captured") if prof else None},
+                     "fp64_issue": fp64_roofline(fp64_ps, seg_per_launch / (track_s / args.steps), fp64_peak)},
         "e2e": {"value": e2e_seg / e2e_s, "unit": "segments/s", "h2d_bytes_per_step": h2d // e2e_steps,
                 "d2h_bytes_per_step": d2h // e2e_steps,
                 "path": "qsg_track_host (the tracking launch reads the vault from and appends the census to "
@@ -640,13 +703,16 @@ def main():
         # the forms compare single-GPU paths; replica runs (N > 1) report the plain line only
         line["forms"] = {"batched": measure_batched(), "adjoint": measure_adjoint()}
     if not args.no_cpu_baseline:
-        rate, seg, secs = cpu_port_rate(DECK, 2, os.cpu_count() or 1)
-        rate1, seg1, secs1 = cpu_port_rate(DECK, 1, 1)
-        line["cpu_baseline"] = {"value": rate, "unit": "segments/s", "cores": os.cpu_count(), "kind": "port",
-                                "sample": f"config2 cycles 0-1 ({seg} segments, {secs:.1f} s tracking) with "
-                                          f"{os.cpu_count()} OpenMP threads",
+        threads = os.cpu_count() or 1
+        rate, seg, secs, rate1, seg1, secs1 = cpu_port_rate(DECK, args.warmup, args.steps, threads)
+        w, k = args.warmup, args.steps
+        line["cpu_baseline"] = {"value": rate, "unit": "segments/s", "cores": threads, "kind": "port",
+                                "sample": f"config2 cycles {w}-{w + k - 1} ({seg} segments, {secs:.1f} s tracking) "
+                                          f"after {w} warm-up cycles, {threads} OpenMP threads: the cycles the "
+                                          f"reference arm times",
                                 "value_1_thread": rate1,
-                                "sample_1_thread": f"config2 cycle 0 ({seg1} segments, {secs1:.1f} s) on one core"}
+                                "sample_1_thread": f"config2 cycle {w + k} ({seg1} segments, {secs1:.1f} s) on one "
+                                                   f"core"}
     print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()

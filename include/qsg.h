@@ -359,15 +359,19 @@ int qsg_set_pool_tuning(QsgHandle* h, int32_t collision_step, int32_t refill);
  *
  * Tracks the n particles of `particles` (device arrays, read only) through
  * the handle's tables exactly as qsg_track_cycle_sync does, fission passes
- * included.  Census particles go to `census` (device arrays with room for
- * census_capacity particles; *n_census receives the count); scalar flux is
- * ADDED into `flux` (device, [num_cells * G], the handle's cell numbering) and
- * the balance counters into `balance` (device, [problems * 13], QSG_BAL_*
- * order), so zero them first for fresh tallies.  The handle's own stores and
- * tallies are left alone, except the exponential cell tally: with
- * qsg_set_exponential_tally on, the per-segment draw happens here too and
- * its tally adds to the handle's (allocated when it was switched on).  The call returns when the work on `stream` (a
- * cudaStream_t, or NULL) has finished.
+ * included, with the tracking kernel qsg_set_track_kernel selects and
+ * without sensitivity scores.  Census particles go to `census` (device
+ * arrays with room for census_capacity particles; *n_census receives the
+ * count); scalar flux is ADDED into `flux` (device, [num_cells * G], the
+ * handle's cell numbering) and the balance counters into `balance` (device,
+ * [problems * 13], QSG_BAL_* order), so zero them first for fresh tallies.
+ * No output may share memory with `particles` or with another output
+ * (QSG_ERR_INVALID).  The handle's own stores and tallies are left alone,
+ * except the exponential cell tally: with qsg_set_exponential_tally on, the
+ * per-segment draw happens here too and its tally adds to the handle's
+ * (allocated when it was switched on).  n == 0 returns at once with
+ * *n_census = 0.  The call returns when the work on `stream` (a cudaStream_t,
+ * or NULL) has finished.
  *
  * Allocates nothing: the fission products handed from one pass to the next
  * live in a fixed array inside the library, two stores of
@@ -375,9 +379,14 @@ int qsg_set_pool_tuning(QsgHandle* h, int32_t collision_step, int32_t refill);
  * every GPU that loads libqsg.so holds until the process exits.  A pass that
  * makes more fission products than that, or a census beyond census_capacity,
  * ends the call with QSG_ERR_CAPACITY and a message naming the limit; the
- * outputs of that call are then incomplete.  The first call on a device looks
- * up the array's device address (cudaGetSymbolAddress), so make that first
- * call before any stream capture begins.  Every call on a device shares the
+ * outputs of that call are then incomplete.  The array's memory is reserved
+ * by the CUDA driver when it loads this library's device code on a device
+ * (with the default lazy loading: at the first use of the library's kernels
+ * there, which qsg_create already makes), never by this call.  The first
+ * call in each CUDA context looks up the array's device address
+ * (cudaGetSymbolAddress) and later calls reuse it, so make that first call
+ * before any stream capture begins -- also after a cudaDeviceReset, which
+ * replaces the context and reloads the device code.  Every call on a device shares the
  * one array, and each call clears the parts that must start at zero: calls
  * whose work overlaps on the GPU (other threads, other streams) race on it and
  * must be serialised by the caller. */
@@ -398,6 +407,15 @@ int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* particles, u
  * of the conversion, the quotient, the comparisons and the sample (all zero
  * on a correct build). */
 int qsg_check_arithmetic(int32_t device, uint64_t n, uint64_t seed, uint64_t* mismatches);
+
+/* No reference counterpart: log, sin and cos of the n host values x by the
+ * portable elementary functions (quicksilver_gb300/csrc/portable_math.h)
+ * evaluated on CUDA device `device`, into host arrays.  Those functions use
+ * only correctly rounded IEEE operations, so the results must equal a CPU's
+ * bit for bit; the library built with them (build.py --portable-math,
+ * libqsg_pm.so) then tracks the trajectories the reference tracks when it is
+ * linked with the same functions. */
+int qsg_portable_math_eval(int32_t device, const double* x, uint64_t n, double* lg, double* sn, double* cs);
 
 /* No reference counterpart: the FP64 issue rate of CUDA device `device`, in
  * FP64 warp instructions per second, measured with independent multiply-add

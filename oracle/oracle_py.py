@@ -67,6 +67,12 @@ def lib() -> C.CDLL:
                                     C.c_double, C.c_int]
         h.oracle_create.restype = vp
         h.oracle_destroy.argtypes = [vp]
+        h.oracle_set_seed_offset.argtypes = [vp, C.c_uint64]
+        h.oracle_set_seed_offset.restype = None
+        h.oracle_use_portable_math.argtypes = [C.c_int]
+        h.oracle_use_portable_math.restype = None
+        h.oracle_pm_eval.argtypes = [vp, C.c_uint64, vp, vp, vp]
+        h.oracle_pm_eval.restype = None
         h.oracle_destroy.restype = None
         for name in ("oracle_cycle_init", "oracle_cycle_finalize"):
             getattr(h, name).argtypes = [vp]
@@ -126,6 +132,11 @@ class OracleRun:
                                       n_particles, e_min, e_max, low_weight_cutoff, load_balance)
         if not self._h:
             raise MemoryError("oracle_create failed")
+
+    def set_seed_offset(self, offset: int):
+        """Add `offset` to every source seed (before the first cycle): the
+        oracle's side of the library's per-problem seed offsets."""
+        lib().oracle_set_seed_offset(self._h, int(offset) & 0xFFFFFFFFFFFFFFFF)
 
     def close(self):
         if self._h:
@@ -290,6 +301,20 @@ def track_sens(problem_ptr, num_cells: int, num_groups: int, particles: np.ndarr
     return {"census": census[:m].copy(), "census_scores": census_sc[:m].copy(),
             "balance": np.array(bal, dtype=np.uint64), "flux": flux.reshape(num_cells, num_groups),
             "flux_cell": fc, "dflux": df.reshape(num_cells, K), "leak": float(lk[0]), "dleak": dl}
+
+
+def use_portable_math(on: bool):
+    """Process-wide: the tracking path's log / sin / cos become the portable
+    functions (quicksilver_gb300/csrc/portable_math.h) or, off, libm's."""
+    lib().oracle_use_portable_math(int(bool(on)))
+
+
+def pm_eval(x: np.ndarray):
+    """(log, sin, cos) of x by the portable functions."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = [np.empty_like(x) for _ in range(3)]
+    lib().oracle_pm_eval(x.ctypes.data, len(x), *(o.ctypes.data for o in out))
+    return tuple(out)
 
 
 def rng_sample(seed: int):

@@ -5,8 +5,10 @@
  * domain.  Every routine names the reference lines it follows.  Floating
  * point expressions keep the reference's operation order; the file is built
  * with -ffp-contract=off so no fused multiply-add changes a rounding.
- * libm's log/sin/cos/sqrt are used exactly where the reference uses them.
+ * libm's log/sin/cos/sqrt are used exactly where the reference uses them
+ * (log/sin/cos: or the portable functions, oracle_use_portable_math).
  */
+#include "../quicksilver_gb300/csrc/portable_math.h"
 #include "qs_oracle.h"
 
 #include <math.h>
@@ -16,6 +18,34 @@
 #ifdef _OPENMP
 #include <omp.h>
 #endif
+
+/* Elementary functions of the tracking path: the host libm's (the
+ * reference's), or, after oracle_use_portable_math(1), the portable
+ * functions that the GPU library's portable-math build and the reference
+ * built by `make -C oracle ref_pm` also use. */
+static int g_portable_math = 0;
+
+void oracle_use_portable_math(int on) { g_portable_math = on != 0; }
+
+static inline double ora_log(double x) { return g_portable_math ? qsg_log(x) : log(x); }
+
+static inline void ora_sincos(double x, double* s, double* c)
+{
+    if (g_portable_math) {
+        qsg_sincos(x, s, c);
+    } else {
+        *s = sin(x);
+        *c = cos(x);
+    }
+}
+
+void oracle_pm_eval(const double* x, uint64_t n, double* lg, double* sn, double* cs)
+{
+    for (uint64_t i = 0; i < n; i++) {
+        lg[i] = qsg_log(x[i]);
+        qsg_sincos(x[i], &sn[i], &cs[i]);
+    }
+}
 
 /* PhysicalConstants.hh:9-16 */
 #define QS_NEUTRON_REST_MASS_ENERGY 9.395656981095e+2
@@ -375,7 +405,7 @@ static int segment_outcome(TrackCtx* ctx, WorkParticle* w)
     else w->mean_free_path = 1.0 / sigma;
     if (w->num_mean_free_paths == 0.0) {
         double r = oracle_rng_sample(&w->seed);
-        w->num_mean_free_paths = -1.0 * log(r);
+        w->num_mean_free_paths = -1.0 * ora_log(r);
     }
     if (force_collision) distance[OUT_COLLISION] = QS_SMALL_DOUBLE;
     else distance[OUT_COLLISION] = w->num_mean_free_paths * w->mean_free_path;
@@ -504,8 +534,8 @@ static void update_trajectory(double energy, double angle, WorkParticle* w)
     double cosTheta = angle;
     double r = oracle_rng_sample(&w->seed);
     double phi = 2 * 3.14159265 * r;
-    double sinPhi = sin(phi);
-    double cosPhi = cos(phi);
+    double sinPhi, cosPhi;
+    ora_sincos(phi, &sinPhi, &cosPhi);
     double sinTheta = sqrt((1.0 - (cosTheta * cosTheta)));
     rotate3d(w, sinTheta, cosTheta, sinPhi, cosPhi);
     const double m = QS_NEUTRON_REST_MASS_ENERGY;
@@ -514,7 +544,7 @@ static void update_trajectory(double energy, double angle, WorkParticle* w)
     w->vy = speed * w->beta;
     w->vz = speed * w->gamma;
     r = oracle_rng_sample(&w->seed);
-    w->num_mean_free_paths = -1.0 * log(r);
+    w->num_mean_free_paths = -1.0 * ora_log(r);
 }
 
 /* CollisionEvent, CollisionEvent.cc:48-148 (with NuclearDataReaction::
@@ -758,6 +788,7 @@ struct OracleRun {
     OracleSens sens;            /* sens.K == 0: off */
     int has_sens;
     double* cell_tally;         /* [C] exponential cell tally, NULL: off */
+    uint64_t seed_offset;       /* added to every source seed (0: the reference's seeding) */
 };
 
 OracleRun* oracle_create(const QsgProblem* pb, const double* source_rate, uint64_t n_particles,
@@ -777,6 +808,8 @@ OracleRun* oracle_create(const QsgProblem* pb, const double* source_rate, uint64
     if (!r->flux || !r->source_tally) { oracle_destroy(r); return NULL; }
     return r;
 }
+
+void oracle_set_seed_offset(OracleRun* r, uint64_t offset) { r->seed_offset = offset; }
 
 void oracle_destroy(OracleRun* r)
 {
@@ -881,6 +914,7 @@ static int source_now(OracleRun* run)
         for (int k = 0; k < n; k++) {
             uint64_t seed0 = run->source_tally[c]++;
             seed0 += pb->cell_id[c];
+            seed0 += run->seed_offset;
             WorkParticle w;
             memset(&w, 0, sizeof(w));
             w.seed = oracle_rng_spawn(&seed0);
@@ -892,8 +926,10 @@ static int source_now(OracleRun* run)
             w.gamma = 1.0 - 2.0 * oracle_rng_sample(&w.seed);
             double sine_gamma = sqrt((1.0 - (w.gamma * w.gamma)));
             double phi = QS_PI * (2.0 * oracle_rng_sample(&w.seed) - 1.0);
-            w.alpha = sine_gamma * cos(phi);
-            w.beta = sine_gamma * sin(phi);
+            double sin_phi, cos_phi;
+            ora_sincos(phi, &sin_phi, &cos_phi);
+            w.alpha = sine_gamma * cos_phi;
+            w.beta = sine_gamma * sin_phi;
             w.kinetic_energy = (run->e_max - run->e_min) * oracle_rng_sample(&w.seed) + run->e_min;
             /* Get_Speed_From_Energy, MC_SourceNow.cc:169-177 */
             const double m = QS_NEUTRON_REST_MASS_ENERGY;
@@ -906,7 +942,7 @@ static int source_now(OracleRun* run)
             w.cell = c;
             w.weight = spw;
             double rn = oracle_rng_sample(&w.seed);
-            w.num_mean_free_paths = -1.0 * log(rn);
+            w.num_mean_free_paths = -1.0 * ora_log(rn);
             rn = oracle_rng_sample(&w.seed);
             w.time_to_census = dt * rn;
             w.last_event = QSG_EVENT_CENSUS; /* MC_Particle default */

@@ -36,6 +36,18 @@ OracleRun* oracle_create(const QsgProblem* problem, const double* source_rate,
                          uint64_t n_particles, double e_min, double e_max,
                          double low_weight_cutoff, int load_balance);
 void oracle_destroy(OracleRun* run);
+/* An offset added to every source seed (MC_SourceNow.cc:90-97 adds the cell's
+ * _id to its source tally; this adds `offset` on top), giving an independent
+ * replica of the same problem as the library's per-problem seed offsets do.
+ * 0, the default, is the reference's seeding.  Call before the first cycle. */
+void oracle_set_seed_offset(OracleRun* run, uint64_t offset);
+/* Process-wide: 1 = the tracking path's log / sin / cos are the portable
+ * functions of quicksilver_gb300/csrc/portable_math.h (as in the GPU
+ * library's portable-math build and the reference built with `make -C oracle
+ * ref_pm`); 0 (default) = the host libm's, as the reference uses them. */
+void oracle_use_portable_math(int on);
+/* log, sin and cos of x[0..n) by the portable functions. */
+void oracle_pm_eval(const double* x, uint64_t n, double* lg, double* sn, double* cs);
 
 /* cycleInit (main.cc:96-121): swap census into processing, MC_SourceNow,
  * PopulationControl, RouletteLowWeightParticles. */

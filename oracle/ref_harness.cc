@@ -35,6 +35,12 @@
 //   Built with -DEXPONENTIAL_TALLY (make -C oracle ref_exp) it also writes,
 //   per cycle, the reference's exponential cell tally.
 //
+//   QS_PORTABLE_MATH=1    (harness built by `make -C oracle ref_pm` only)
+//                         from the first cycle on, the reference's log / sin
+//                         / cos / sincos calls go to the portable functions
+//                         of quicksilver_gb300/csrc/portable_math.h through
+//                         the linker's --wrap (oracle/pm_wrap.c); initMC's
+//                         table construction keeps the host libm
 //   QS_THETA=<file>       cross-section scale factors applied after initMC;
 //                         lines "material reactionType gLo gHi factor" with
 //                         reactionType 1=scatter 2=absorption 3=fission and
@@ -69,6 +75,8 @@
 #include <omp.h>
 
 extern MonteCarlo* mcco;
+// defined only by oracle/pm_wrap.c (the ref_pm build)
+extern "C" __attribute__((weak)) int qs_portable_math_on;
 void cycleInit(bool loadBalance);
 void cycleTracking(MonteCarlo* monteCarlo);
 void cycleFinalize();
@@ -313,6 +321,10 @@ int main(int argc, char** argv)
    }
    mcco = initMC(params);
    if (getenv("QS_INIT_ONLY")) return 0;   // e.g. for initMC's crossSectionsOut file only
+   if (getenv("QS_PORTABLE_MATH")) {
+      if (!&qs_portable_math_on) { fprintf(stderr, "QS_PORTABLE_MATH: this harness was not built with pm_wrap.c\n"); return 2; }
+      qs_portable_math_on = 1;
+   }
 
    const char* theta = getenv("QS_THETA");
    if (theta && theta[0]) apply_theta(theta);

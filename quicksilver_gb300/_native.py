@@ -38,6 +38,7 @@ QSG_DEV_STORE_OVERFLOW = 1 << 4
 QSG_DEV_BAD_FACET = 1 << 5
 QSG_DEV_NEGATIVE_DISTANCE = 1 << 6
 QSG_DEV_PASS_LIMIT = 1 << 7
+QSG_DEV_SCREEN_MISS = 1 << 8   # verification build only
 
 # NuclearDataReaction::Enum (NuclearData.hh:33-40), QSG_REACT_* in qsg.h
 QSG_REACT_SCATTER, QSG_REACT_ABSORPTION, QSG_REACT_FISSION = 1, 2, 3
@@ -131,6 +132,7 @@ _SIGNATURES = {
     "qsg_problem_check": ([C.POINTER(QsgProblem)], C.c_int),
     "qsg_check_arithmetic": ([C.c_int32, C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)], C.c_int),
     "qsg_measure_fp64_rate": ([C.c_int32, C.POINTER(C.c_double)], C.c_int),
+    "qsg_portable_math_eval": ([C.c_int32, _VP, C.c_uint64, _VP, _VP, _VP], C.c_int),
     "qsg_create": ([C.POINTER(QsgProblem), C.POINTER(QsgOptions), C.POINTER(_VP)], C.c_int),
     "qsg_destroy": ([_VP], C.c_int),
     "qsg_set_particles": ([_VP, C.POINTER(QsgParticleSoA), C.c_uint64], C.c_int),
@@ -224,6 +226,15 @@ def check_arithmetic(n: int, seed: int = 1, device: int = 0) -> tuple:
     out = (C.c_uint64 * 4)()
     check(lib().qsg_check_arithmetic(device, n, seed, out))
     return tuple(int(v) for v in out)
+
+
+def portable_math_eval(x, device: int = 0):
+    """(log, sin, cos) of x by the portable elementary functions on the GPU
+    (qsg_portable_math_eval)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = [np.empty_like(x) for _ in range(3)]
+    check(lib().qsg_portable_math_eval(device, x.ctypes.data, len(x), *(o.ctypes.data for o in out)))
+    return tuple(out)
 
 
 def measure_fp64_rate(device: int = 0) -> float:

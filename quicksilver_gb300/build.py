@@ -65,18 +65,22 @@ def _run(cmd: list[str]) -> None:
 
 
 def build(verbose: bool = False, ptxas_verbose: bool = False, verify_screen: bool = False,
-          nvtx: bool = False) -> Path:
+          nvtx: bool = False, portable_math: bool = False) -> Path:
     """Compile every translation unit and link ``libqsg.so``; returns its path.
 
     ``verify_screen`` builds ``libqsg_verify.so`` instead: the facet search also
     evaluates every facet the FP32 screen skipped and raises QSG_DEV_SCREEN_MISS
     if FP64 would have accepted one (a test build; slower).  ``nvtx`` builds
     ``libqsg_nvtx.so``: the same library with NVTX ranges around its phases
-    (-DQSG_NVTX).  Either loads with QSG_LIB=verify / QSG_LIB=nvtx.
+    (-DQSG_NVTX).  ``portable_math`` builds ``libqsg_pm.so``: the tracking
+    path's log / sin / cos are the portable functions of
+    csrc/portable_math.h (-DQSG_PORTABLE_MATH), the ones the oracle and the
+    reference can be switched to, so that all three track bit-identical
+    trajectories.  Each loads with QSG_LIB=verify / nvtx / pm.
     """
-    if verify_screen and nvtx:
+    if verify_screen + nvtx + portable_math > 1:
         raise ValueError("one variant at a time")
-    variant = "verify" if verify_screen else "nvtx" if nvtx else ""
+    variant = "verify" if verify_screen else "nvtx" if nvtx else "pm" if portable_math else ""
     obj_dir = OBJ / variant
     lib = OUT / (f"libqsg_{variant}.so" if variant else "libqsg.so")
     obj_dir.mkdir(parents=True, exist_ok=True)
@@ -101,6 +105,8 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, verify_screen: boo
                 flags += ["-DQSG_VERIFY_SCREEN"]
             if nvtx:
                 flags += ["-DQSG_NVTX"]
+            if portable_math:
+                flags += ["-DQSG_PORTABLE_MATH"]
             jobs.append([nvcc, *NVCC_ARCH, *flags, f"-I{INCLUDE}", f"-I{CSRC}", f"-I{CSRC / 'host'}",
                          "-c", str(src), "-o", str(obj)])
     if jobs:
@@ -121,4 +127,4 @@ def build(verbose: bool = False, ptxas_verbose: bool = False, verify_screen: boo
 
 if __name__ == "__main__":
     build(verbose=True, ptxas_verbose="-v" in sys.argv, verify_screen="--verify-screen" in sys.argv,
-          nvtx="--nvtx" in sys.argv)
+          nvtx="--nvtx" in sys.argv, portable_math="--portable-math" in sys.argv)

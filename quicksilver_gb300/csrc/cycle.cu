@@ -179,8 +179,8 @@ __global__ void __launch_bounds__(kInitBlock) source_kernel(SourceArgs a)
     p.gamma = 1.0 - 2.0 * rng_sample(p.seed);
     double sine_gamma = sqrt((1.0 - (p.gamma * p.gamma)));
     double phi = kPi * (2.0 * rng_sample(p.seed) - 1.0);
-    p.alpha = sine_gamma * cos(phi);
-    p.beta = sine_gamma * sin(phi);
+    p.alpha = sine_gamma * QSG_COS(phi);
+    p.beta = sine_gamma * QSG_SIN(phi);
     // energy uniform in [eMin, eMax]; Get_Speed_From_Energy (MC_SourceNow.cc:169-177)
     p.kinetic_energy = (a.c.e_max[prob] - a.c.e_min[prob]) * rng_sample(p.seed) + a.c.e_min[prob];
     const double m = kNeutronRestMassEnergy;
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(kInitBlock) source_kernel(SourceArgs a)
     p.domain = 0;
     p.cell = cell;
     p.weight = a.c.weight[prob];
-    p.num_mean_free_paths = -1.0 * log(rng_sample(p.seed));
+    p.num_mean_free_paths = -1.0 * QSG_LOG(rng_sample(p.seed));
     p.time_to_census = tb.time_step * rng_sample(p.seed);
     p.age = 0.0;
     p.num_segments = 0.0;

@@ -482,7 +482,7 @@ __device__ __forceinline__ int segment_outcome(const DevTables& t, const DevTall
     }
     if (f64_eq0(p.num_mean_free_paths)) {
         double r = rng_sample(p.seed);
-        p.num_mean_free_paths = -1.0 * log(r);
+        p.num_mean_free_paths = -1.0 * QSG_LOG(r);
     }
     d_coll = force_collision ? kSmallDouble : p.num_mean_free_paths * p.mean_free_path;
     d_census = speed * p.time_to_census;
@@ -543,7 +543,7 @@ __device__ __forceinline__ void update_trajectory(double energy, double angle, P
     double r = rng_sample(p.seed);
     double phi = 2 * 3.14159265 * r;
     double sinPhi, cosPhi;
-    sincos(phi, &sinPhi, &cosPhi);
+    QSG_SINCOS(phi, &sinPhi, &cosPhi);
     double sinTheta = sqrt((1.0 - (cosTheta * cosTheta)));
     double cos_theta = p.gamma;
     double sin_theta = sqrt((1.0 - (cos_theta * cos_theta)));
@@ -568,7 +568,7 @@ __device__ __forceinline__ void update_trajectory(double energy, double angle, P
     p.vz = speed * p.gamma;
     p.speed = -1.0;   // |velocity| of the new velocity is recomputed when next needed
     r = rng_sample(p.seed);
-    p.num_mean_free_paths = -1.0 * log(r);
+    p.num_mean_free_paths = -1.0 * QSG_LOG(r);
 }
 
 // CollisionEvent (CollisionEvent.cc:48-148) with NuclearDataReaction::
@@ -1389,9 +1389,10 @@ void launch_pool_t(QsgHandle* h, int grid, size_t smem, cudaStream_t s, const De
 }
 
 template <int B>
-void launch_pool(QsgHandle* h, cudaStream_t s, const DevTally& tv, unsigned long long* cursor, const PassStores& ps)
+void launch_pool(QsgHandle* h, cudaStream_t s, const DevTally& tv, unsigned long long* cursor, const PassStores& ps,
+                 bool sens)
 {
-    if (h->sens.K == 0) {
+    if (!sens || h->sens.K == 0) {
         launch_pool_t<B, false, kPoolPlain>(h, h->pool_blocks,
                                             track_pool_smem_bytes(B, h->num_problems, 0, kPoolPlain), s, tv, cursor,
                                             ps);
@@ -1762,19 +1763,16 @@ int copy_soa(const DevStore& d, const QsgParticleSoA* h, uint64_t n, bool to_dev
 
 namespace {
 
-// One tracking pass over explicit stores: input -> census + fission
-// products.  The pass's particle count is read by the kernel from the input's
-// device counter, so nothing here waits for the device.
-int launch_pass_stores(QsgHandle* h, cudaStream_t s, const PassStores& ps)
+// The tracking kernel the handle selects (qsg_set_track_kernel, block size,
+// sensitivities when `sens` and enabled) over explicit stores, tallies and
+// work cursor.
+int launch_track_kernel(QsgHandle* h, cudaStream_t s, const DevTally& tv, unsigned long long* cursor,
+                        const PassStores& ps, bool sens)
 {
-    unsigned long long* cursor = &h->scalars.ptr->cursor;
-    QSG_CUDA(cudaMemsetAsync(ps.extra.count, 0, sizeof(unsigned long long), s));
-    QSG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s));
-    const DevTally tv = tally_view(h);
     if (h->kernel_kind == 1 && pool_kernel_usable(h)) {
-        if (h->block_size == 256) launch_pool<256>(h, s, tv, cursor, ps);
-        else launch_pool<128>(h, s, tv, cursor, ps);
-    } else if (h->sens.K > 0) {
+        if (h->block_size == 256) launch_pool<256>(h, s, tv, cursor, ps, sens);
+        else launch_pool<128>(h, s, tv, cursor, ps, sens);
+    } else if (sens && h->sens.K > 0) {
         const size_t smem = track_smem_bytes_sens(h);
         if (h->block_size == 256)
             track_kernel<256, true><<<h->sens_track_blocks, 256, smem, s>>>(h->tables, tv, ps.in, ps.census,
@@ -1793,6 +1791,17 @@ int launch_pass_stores(QsgHandle* h, cudaStream_t s, const PassStores& ps)
     }
     QSG_CUDA(cudaGetLastError());
     return QSG_OK;
+}
+
+// One tracking pass over explicit stores: input -> census + fission
+// products.  The pass's particle count is read by the kernel from the input's
+// device counter, so nothing here waits for the device.
+int launch_pass_stores(QsgHandle* h, cudaStream_t s, const PassStores& ps)
+{
+    unsigned long long* cursor = &h->scalars.ptr->cursor;
+    QSG_CUDA(cudaMemsetAsync(ps.extra.count, 0, sizeof(unsigned long long), s));
+    QSG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s));
+    return launch_track_kernel(h, s, tally_view(h), cursor, ps, true);
 }
 
 // One tracking pass over the handle's stores: processing -> processed +
@@ -2121,6 +2130,23 @@ bool soa_ranges_overlap(const QsgParticleSoA* a, uint64_t n, const QsgParticleSo
     return false;
 }
 
+bool ranges_overlap(const void* a, uint64_t a_bytes, const void* b, uint64_t b_bytes)
+{
+    const uintptr_t a0 = (uintptr_t)a, b0 = (uintptr_t)b;
+    return a0 < b0 + b_bytes && b0 < a0 + a_bytes;
+}
+
+// Whether any field array of `a` (n particles) overlaps [p, p + bytes).
+bool soa_overlaps_range(const QsgParticleSoA* a, uint64_t n, const void* p, uint64_t bytes)
+{
+    const void* fa[20] = {a->x, a->y, a->z, a->vx, a->vy, a->vz, a->kinetic_energy, a->weight, a->time_to_census,
+                          a->age, a->num_mean_free_paths, a->num_segments, a->random_number_seed, a->identifier,
+                          a->last_event, a->num_collisions, a->breed, a->species, a->domain, a->cell};
+    for (int i = 0; i < 20; i++)
+        if (ranges_overlap(fa[i], n * (i < 14 ? 8 : 4), p, bytes)) return true;
+    return false;
+}
+
 // Device view of a caller's particle arrays for qsg_track_host: each field
 // must be page-locked host memory (cudaHostAlloc / cudaHostRegister, which the
 // GPU reads and writes over the host link) or device memory.
@@ -2404,27 +2430,60 @@ static __device__ __align__(256) unsigned char qsg_noalloc_scratch[QSG_NOALLOC_S
 namespace qsg {
 namespace {
 
-constexpr int kNoallocMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-unsigned char* g_noalloc_address[kNoallocMaxDevices] = {};
+// Device address of the scratch in the current context (device `device`
+// current).  The lookup (cudaGetSymbolAddress) runs once per CUDA context and
+// is cached under the context's unique id, so a context that replaces one
+// destroyed by cudaDeviceReset -- which reloads this library's device code at
+// a new address -- gets a fresh lookup.  Where the driver cannot name the
+// context, every call looks the address up (no allocation either way once the
+// device code is loaded).
+using CtxGetCurrentFn = int (*)(void**);
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
 
-// Device address of the scratch on `device`, which must be current.  The first
-// call on each device performs the lookup; later calls reuse it.
+std::mutex g_noalloc_mutex;
+std::map<unsigned long long, unsigned char*> g_noalloc_address;   // context id -> address
+
+bool current_context_id(unsigned long long* id)
+{
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        looked_up = true;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1{}, q2{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 4000, cudaEnableDefault, &q1) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+            get_id = reinterpret_cast<CtxGetIdFn>(f2);
+        }
+        cudaGetLastError();
+    }
+    void* ctx = nullptr;
+    return get_current && get_id && get_current(&ctx) == 0 && ctx && get_id(ctx, id) == 0;
+}
+
 int noalloc_scratch_address(int device, unsigned char** out)
 {
-    if (device < 0 || device >= kNoallocMaxDevices)
-        return fail(QSG_ERR_INVALID, "qsg_track_particles_noalloc: device %d outside 0..%d", device,
-                    kNoallocMaxDevices - 1);
+    unsigned long long ctx_id = 0;
+    const bool named = current_context_id(&ctx_id);
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_address[device]) {
-        void* ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&ptr, qsg_noalloc_scratch);
-        if (e != cudaSuccess || !ptr)
-            return fail(QSG_ERR_CUDA, "qsg_track_particles_noalloc: cudaGetSymbolAddress of the scratch array on "
-                        "device %d failed: %s", device, cudaGetErrorString(e));
-        g_noalloc_address[device] = static_cast<unsigned char*>(ptr);
+    if (named) {
+        auto it = g_noalloc_address.find(ctx_id);
+        if (it != g_noalloc_address.end()) {
+            *out = it->second;
+            return QSG_OK;
+        }
     }
-    *out = g_noalloc_address[device];
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, qsg_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+        return fail(QSG_ERR_CUDA, "qsg_track_particles_noalloc: cudaGetSymbolAddress of the scratch array on "
+                    "device %d failed: %s", device, cudaGetErrorString(e));
+    if (named) g_noalloc_address[ctx_id] = static_cast<unsigned char*>(ptr);
+    *out = static_cast<unsigned char*>(ptr);
     return QSG_OK;
 }
 
@@ -2500,6 +2559,8 @@ extern "C" int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* p
     QSG_API_BEGIN
     QSG_RANGE("cycleTracking_TrackingKernel");
     if (!h || !n_census) return fail(QSG_ERR_INVALID, "qsg_track_particles_noalloc: null handle or n_census");
+    *n_census = 0;
+    if (n == 0) return QSG_OK;
     int st = set_device(h);
     if (st) return st;
     if ((st = noalloc_check_soa(particles, h->device, "particles")) ||
@@ -2507,6 +2568,18 @@ extern "C" int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* p
         (st = noalloc_check_pointer(flux, 8, h->device, "flux")) ||
         (st = noalloc_check_pointer(balance, 8, h->device, "balance")))
         return st;
+    // the kernels read the particles while other threads append census
+    // records and add tallies: no output may share memory with the input or
+    // with another output
+    const uint64_t flux_n = (uint64_t)h->num_cells * h->num_groups;
+    const uint64_t bal_n = (uint64_t)h->num_problems * QSG_BAL_COUNT;
+    if (soa_ranges_overlap(particles, n, census, census_capacity))
+        return fail(QSG_ERR_INVALID, "qsg_track_particles_noalloc: the census arrays overlap the particle arrays");
+    if (ranges_overlap(flux, flux_n * 8, balance, bal_n * 8) || soa_overlaps_range(particles, n, flux, flux_n * 8) ||
+        soa_overlaps_range(particles, n, balance, bal_n * 8) ||
+        soa_overlaps_range(census, census_capacity, flux, flux_n * 8) ||
+        soa_overlaps_range(census, census_capacity, balance, bal_n * 8))
+        return fail(QSG_ERR_INVALID, "qsg_track_particles_noalloc: flux or balance overlaps another argument");
     unsigned char* scratch = nullptr;
     if ((st = noalloc_scratch_address(h->device, &scratch))) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -2527,20 +2600,14 @@ extern "C" int qsg_track_particles_noalloc(QsgHandle* h, const QsgParticleSoA* p
 
     noalloc_begin_kernel<<<1, 1, 0, s>>>(header, prod[0].count, prod[1].count, (unsigned long long)n);
     QSG_CUDA(cudaGetLastError());
-    const size_t smem = track_smem_bytes(h);
     unsigned long long remaining = n, counts[3] = {0, 0, 0};
     for (int pass = 0; remaining != 0; pass++) {
         const DevStore in = pass == 0 ? in0 : prod[(pass + 1) & 1];
         const DevStore extra = prod[pass & 1];
         QSG_CUDA(cudaMemsetAsync(extra.count, 0, sizeof(unsigned long long), s));
         QSG_CUDA(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s));
-        if (h->block_size == 256)
-            track_kernel<256, false><<<h->track_blocks, 256, smem, s>>>(h->tables, tally, in, out, extra, cursor,
-                                                                        DevSens{});
-        else
-            track_kernel<128, false><<<h->track_blocks, 128, smem, s>>>(h->tables, tally, in, out, extra, cursor,
-                                                                        DevSens{});
-        QSG_CUDA(cudaGetLastError());
+        // the kernel qsg_set_track_kernel selects, without sensitivity scores
+        if ((st = launch_track_kernel(h, s, tally, cursor, PassStores{in, out, extra}, false))) return st;
         // products of this pass, census so far, device flags
         QSG_CUDA(cudaMemcpyAsync(&counts[0], extra.count, 8, cudaMemcpyDeviceToHost, s));
         QSG_CUDA(cudaMemcpyAsync(&counts[1], header + 2, 8, cudaMemcpyDeviceToHost, s));
@@ -2702,6 +2769,54 @@ extern "C" int qsg_check_arithmetic(int32_t device, uint64_t n, uint64_t seed, u
     bad.free();
     if (e != cudaSuccess) return fail(QSG_ERR_CUDA, "qsg_check_arithmetic: %s", cudaGetErrorString(e));
     for (int k = 0; k < 4; k++) mismatches[k] = host[k];
+    return QSG_OK;
+    QSG_API_END
+}
+
+// ------------------------------------------------------------------------
+// The portable elementary functions evaluated on the device, for the check
+// that the GPU gives the host's bits (portable_math.h).
+
+namespace qsg {
+namespace {
+
+__global__ void portable_math_kernel(const double* x, uint64_t n, double* lg, double* sn, double* cs)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        lg[i] = qsg_log(x[i]);
+        qsg_sincos(x[i], sn + i, cs + i);
+    }
+}
+
+}  // namespace
+}  // namespace qsg
+
+extern "C" int qsg_portable_math_eval(int32_t device, const double* x, uint64_t n, double* lg, double* sn,
+                                      double* cs)
+{
+    QSG_API_BEGIN
+    if (n > 0 && (!x || !lg || !sn || !cs)) return fail(QSG_ERR_INVALID, "qsg_portable_math_eval: null argument");
+    int ndev = 0;
+    qsg_device_count(&ndev);
+    if (ndev == 0) return fail(QSG_ERR_NO_DEVICE, "qsg_portable_math_eval: no CUDA device visible");
+    if (device < 0 || device >= ndev)
+        return fail(QSG_ERR_INVALID, "qsg_portable_math_eval: device %d of %d", (int)device, ndev);
+    if (n == 0) return QSG_OK;
+    QSG_CUDA(cudaSetDevice(device));
+    qsg::DevBuf<double> buf;
+    int st = buf.alloc(4 * n);
+    if (st) return st;
+    cudaError_t e = cudaMemcpy(buf.ptr, x, n * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        qsg::portable_math_kernel<<<4 * 152, 256>>>(buf.ptr, n, buf.ptr + n, buf.ptr + 2 * n, buf.ptr + 3 * n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(lg, buf.ptr + n, n * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(sn, buf.ptr + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(cs, buf.ptr + 3 * n, n * sizeof(double), cudaMemcpyDeviceToHost);
+    buf.free();
+    if (e != cudaSuccess) return fail(QSG_ERR_CUDA, "qsg_portable_math_eval: %s", cudaGetErrorString(e));
     return QSG_OK;
     QSG_API_END
 }

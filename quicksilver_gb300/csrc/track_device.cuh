@@ -10,7 +10,23 @@
 
 #include <cstdint>
 
+#include "portable_math.h"
 #include "qsg.h"
+
+// The tracking path's elementary functions: the CUDA math library's, or with
+// -DQSG_PORTABLE_MATH (build.py --portable-math, libqsg_pm.so) the portable
+// ones of portable_math.h, which the oracle and the reference can use too.
+#ifdef QSG_PORTABLE_MATH
+#define QSG_LOG(x) qsg_log(x)
+#define QSG_SINCOS(x, s, c) qsg_sincos((x), (s), (c))
+#define QSG_SIN(x) qsg_sin(x)
+#define QSG_COS(x) qsg_cos(x)
+#else
+#define QSG_LOG(x) log(x)
+#define QSG_SINCOS(x, s, c) sincos((x), (s), (c))
+#define QSG_SIN(x) sin(x)
+#define QSG_COS(x) cos(x)
+#endif
 
 namespace qsg {
 

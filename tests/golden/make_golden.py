@@ -1,6 +1,6 @@
 """Generate golden fixtures from the UNMODIFIED reference (test infrastructure).
 
-Needs the reference sources (default /root/reference/src) and builds
+Needs the reference sources ($QS_REF_SRC, default: a checkout beside the repository, ../reference/src) and builds
 ``oracle/_ref/qs_ref_harness`` with ``make -C oracle ref``.  For every deck in
 quicksilver_gb300/decks it runs the reference harness and stores in
 ``tests/golden/<deck>.npz``:
@@ -56,8 +56,16 @@ lines, cumulative timer table, figure of merit, CORAL2 checks) and the
 spectrum file it writes, and what it prints for ``-h`` (printArgs,
 cmdLineParser.cc:123-142), in ``transcript_out.npz``.
 
-Usage: python tests/golden/make_golden.py [--exponential-tally | --echo | --xsec | --spectrum | --coral |
-                                           --summary | --timers | --transcript]
+With ``--portable-math`` it runs the reference linked with the portable
+elementary functions (``make -C oracle ref_pm``, QS_PORTABLE_MATH=1: its
+tracking path's log / sin / cos are those of
+quicksilver_gb300/csrc/portable_math.h, initMC keeps libm) and stores, per
+deck, ``pm_<deck>.npz``: the counters, the flux (whole when small, otherwise
+per cell / per group / projections / total) and the sha256 of the sorted
+particle sets after each cycleInit and cycleTracking.
+
+Usage: python tests/golden/make_golden.py [--exponential-tally | --portable-math | --echo | --xsec |
+                                           --spectrum | --coral | --summary | --timers | --transcript]
 """
 from __future__ import annotations
 
@@ -75,7 +83,7 @@ ROOT = HERE.parent.parent
 DECKS = ROOT / "quicksilver_gb300" / "decks"
 HARNESS = ROOT / "oracle" / "_ref" / "qs_ref_harness"
 HARNESS_EXP = ROOT / "oracle" / "_ref_exp" / "qs_ref_harness"
-REF_SRC = os.environ.get("QS_REF_SRC", "/root/reference/src")
+REF_SRC = os.environ.get("QS_REF_SRC", str(Path(__file__).resolve().parents[3] / "reference" / "src"))
 FULL_FLUX_LIMIT = 20000   # store the whole flux array when cells*groups is at most this
 
 PARTICLE_DTYPE = np.dtype([
@@ -190,6 +198,35 @@ def make(deck: Path, workdir: Path) -> None:
         out[k] = d[k]
     np.savez_compressed(HERE / (deck.stem + ".npz"), **out)
     print(f"{deck.name}: cycles={cycles} cells={C} groups={G} segments={int(out['balance'][:, 12].sum())}")
+
+
+HARNESS_PM = ROOT / "oracle" / "_ref" / "qs_ref_harness_pm"
+PM_DECKS = ["t_homog", "t_escape", "t_scatter_octant", "t_fission", "t_nonflat", "config1"]
+PM_FULL_FLUX_LIMIT = 20000    # above this, the whole flux of the first cycle only
+
+
+def make_pm(deck: Path, workdir: Path) -> None:
+    dump = workdir / (deck.stem + ".pm.dump")
+    env = dict(os.environ, QS_DUMP=str(dump), QS_DUMP_PARTICLES="1", QS_DUMP_TABLES="1", QS_PORTABLE_MATH="1",
+               OMP_NUM_THREADS="8")
+    res = subprocess.run([str(HARNESS_PM), "-i", str(deck)], env=env, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise SystemExit(f"reference run failed on {deck}:\n{res.stderr[-4000:]}")
+    d = read_dump(dump)
+    cycles = sum(1 for k in d if k.startswith("balance_c"))
+    G = len(d["energies"]) - 1
+    C = len(d["cell_volume"])
+    flux = np.stack([d[f"flux_c{c}"] for c in range(cycles)])
+    out = {"balance": np.stack([d[f"balance_c{c}"] for c in range(cycles)])}
+    out["flux"] = flux.reshape(cycles, C, G) if C * G <= PM_FULL_FLUX_LIMIT else flux[:1].reshape(1, C, G)
+    out["flux_cell"] = flux.reshape(cycles, C, G).sum(axis=2)
+    out["flux_group"] = flux.reshape(cycles, C, G).sum(axis=1)
+    out["flux_total"] = flux.sum(axis=1)
+    out["init_sha"] = np.array([sha(sort_records(particles(d, f"init_c{c}"))) for c in range(cycles)])
+    out["census_sha"] = np.array([sha(sort_records(particles(d, f"census_c{c}"))) for c in range(cycles)])
+    out["census_n"] = np.array([len(particles(d, f"census_c{c}")) for c in range(cycles)], dtype=np.int64)
+    np.savez_compressed(HERE / f"pm_{deck.stem}.npz", **out)
+    print(f"pm_{deck.name}: cycles={cycles} segments={int(out['balance'][:, 12].sum())}")
 
 
 def make_exp(deck: Path, workdir: Path) -> None:
@@ -372,6 +409,14 @@ def main(argv: list[str]) -> None:
         names = [a for a in argv if a != "--echo"] or sorted(p.stem for p in DECKS.glob("*.inp"))
         with tempfile.TemporaryDirectory() as tmp:
             make_echo(names, Path(tmp))
+        return
+    if "--portable-math" in argv:
+        ensure_harness("ref_pm")
+        names = [a for a in argv if a != "--portable-math"] or PM_DECKS
+        import tempfile
+        with tempfile.TemporaryDirectory() as td:
+            for n in names:
+                make_pm(DECKS / f"{n}.inp", Path(td))
         return
     exp = "--exponential-tally" in argv
     argv = [a for a in argv if a != "--exponential-tally"]

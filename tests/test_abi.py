@@ -82,6 +82,7 @@ def test_new_entry_points_check_arguments_before_any_cuda_call(native_lib):
     assert lib.qsg_check_arithmetic(0, 16, 1, None) == N.QSG_ERR_INVALID
     out = (ctypes.c_uint64 * 4)()
     assert lib.qsg_check_arithmetic(-1, 16, 1, out) in (N.QSG_ERR_INVALID, N.QSG_ERR_NO_DEVICE)
+    assert lib.qsg_portable_math_eval(0, None, 4, None, None, None) == N.QSG_ERR_INVALID
 
 
 @pytest.mark.parametrize("name", ["t_homog.inp", "t_scatter_octant.inp", "t_nonflat.inp", "config1.inp"])

@@ -24,12 +24,21 @@ def test_reference_arm_json_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
 
 
-def test_profile_figures_and_fp64_roofline():
+def test_profile_figures_and_fp64_roofline(tmp_path, monkeypatch):
+    """The per-segment ncu figures come from a machine-readable profile that
+    records the hash of the kernel sources it was captured from; a capture of
+    other sources is reported as stale, not used."""
     sys.path.insert(0, str(ROOT))
     import bench
-    assert bench.profile_traffic_per_segment() > 0
-    per_seg = bench.profile_value("fp64_warp_instructions_per_segment")
-    assert 1.0 < per_seg < 50.0
+    data, _ = bench.profile_figures()
+    assert data["dram_bytes_per_segment"] > 0 and 1.0 < data["fp64_warp_instructions_per_segment"] < 50.0
+    fake = tmp_path / "p.json"
+    fake.write_text(json.dumps(dict(data, kernel_source_sha256=bench.kernel_source_hash())))
+    monkeypatch.setattr(bench, "PROFILE_DATA", fake)
+    assert bench.profile_figures()[1] is True
+    fake.write_text(json.dumps(dict(data, kernel_source_sha256="0" * 64)))
+    assert bench.profile_figures()[1] is False
+    per_seg = data["fp64_warp_instructions_per_segment"]
     r = bench.fp64_roofline(per_seg, 2.0e9, 1.5e10)
     assert abs(r["achieved"] - per_seg * 2.0e9) < 1.0 and abs(r["frac"] - r["achieved"] / 1.5e10) < 1e-12
     assert bench.fp64_roofline(None, 2.0e9, 1.5e10) is None

@@ -1,5 +1,5 @@
 """The drop-in adapter a maintainer adds to the reference
-(oracle/dropin_adapter.hh, the code the integration guide shows), compiled
+(oracle/dropin_adapter.hh), compiled
 with the unmodified reference's sources:
 
 * the table export after initMC, linked against libqsg.so
@@ -27,7 +27,6 @@ with the unmodified reference's sources:
 Runs where the reference's sources and the harness built from them are
 present, and skips elsewhere."""
 import os
-import re
 import subprocess
 import sys
 from pathlib import Path
@@ -91,22 +90,6 @@ def test_cycle_adapter_vaults_and_tallies(name, tmp_path):
     for field in want.dtype.names:
         size = a[field].dtype.itemsize
         np.testing.assert_array_equal(a[field].view(f"u{size}"), b[field].view(f"u{size}"), err_msg=field)
-
-
-def _block(text: str, name: str) -> str:
-    """One C++ function or struct (its first line to the closing brace at
-    column 0), whitespace collapsed."""
-    m = re.search(r"^(?:struct |[\w:<>*& ]+ )" + name + r"\b.*?^\};?", text, re.S | re.M)
-    assert m, name
-    return " ".join(m.group(0).split())
-
-
-@pytest.mark.parametrize("name", ["QsgExport", "qsgExport", "qsgAttach", "QsgColumns", "qsgGather",
-                                  "qsgScatterCensus", "qsgAddTallies", "qsgCycleTracking"])
-def test_integration_guide_shows_the_compiled_adapter(name):
-    guide = (ROOT / "INTEGRATION.md").read_text()
-    code = (ROOT / "oracle" / "dropin_adapter.hh").read_text()
-    assert _block(guide, name) == _block(code, name)
 
 
 GOLDEN = ROOT / "tests" / "golden"

@@ -1,0 +1,72 @@
+"""The FP32 facet screen and the tracking loop's other bit-exact replacements,
+checked in the GPU tests by the verification build (libqsg_verify.so,
+``python -m quicksilver_gb300.build --verify-screen``; __graft_entry__.build()
+makes it beside libqsg.so).
+
+In that build the tracking kernels also evaluate, in the reference's FP64
+arithmetic (MCT.cc:280-395, 549-621), every facet the screen skipped and
+every facet it accepted without the full test, and compare every integer-pipe
+double-to-float conversion and every corrected-reciprocal mean-free-path
+quotient with the FP64 operation; any disagreement raises
+QSG_DEV_SCREEN_MISS.  Run here on config1 (10 cycles) and two cycles of
+config2: no flag may be raised, and the counters and flux totals must equal
+those of the default build (and, for config1, the unmodified reference's
+golden counters).
+"""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from helpers import DECKS
+from quicksilver_gb300 import _native as N
+from quicksilver_gb300.monte_carlo import MonteCarlo
+
+pytestmark = pytest.mark.gpu
+
+ROOT = DECKS.parent.parent
+GOLDEN = ROOT / "tests" / "golden"
+VERIFY_LIB = N.LIB_PATH.parent / "libqsg_verify.so"
+
+
+@pytest.fixture(scope="module")
+def verify_lib():
+    if not VERIFY_LIB.exists():
+        from quicksilver_gb300 import build
+        build.build(verify_screen=True)
+    return VERIFY_LIB
+
+
+def _verify_run(deck, cycles):
+    env = dict(os.environ, QSG_LIB="verify")
+    res = subprocess.run([sys.executable, str(ROOT / "tests" / "verify_screen_run.py"), str(DECKS / deck),
+                          str(cycles)], env=env, capture_output=True, text=True, timeout=900)
+    assert res.returncode == 0, res.stderr[-4000:]
+    out = json.loads(res.stdout.strip().splitlines()[-1])
+    assert out["library"] == "libqsg_verify.so"
+    return out
+
+
+def _default_run(deck, cycles):
+    from quicksilver_gb300 import Deck
+    mc = MonteCarlo(Deck.from_file(DECKS / deck))
+    try:
+        hist = mc.run(cycles)
+    finally:
+        mc.close()
+    return hist
+
+
+@pytest.mark.parametrize("deck,cycles", [("config1.inp", 10), ("config2.inp", 2)])
+def test_verification_build_sees_no_screen_miss(gpu, verify_lib, deck, cycles):
+    got = _verify_run(deck, cycles)
+    assert got["flags"] & N.QSG_DEV_SCREEN_MISS == 0, "the FP32 screen disagreed with FP64"
+    assert got["flags"] == 0, f"device flags 0x{got['flags']:x}"
+    want = _default_run(deck, cycles)
+    np.testing.assert_array_equal(np.array(got["balance"], dtype=np.uint64), want.balance)
+    np.testing.assert_allclose(got["flux_total"], want.flux_total, rtol=1e-12, atol=0)
+    if deck == "config1.inp":
+        np.testing.assert_array_equal(np.array(got["balance"], dtype=np.uint64), np.load(GOLDEN / "config1.npz")["balance"])
