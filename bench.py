@@ -193,7 +193,7 @@ def _sync():
     torch.cuda.synchronize()
 
 
-def measure_batched(tune_space=None):
+def measure_batched(tune_space=None, n_problems=64, fixed_shape=None):
     """Batched form on the uneven ensemble (64 problems, mesh edge in
     {8..48}, 1e4-2e6 particles, 10 cycles): one persistent launch per pass
     for all problems, cycles replayed from CUDA graphs, kernel shape from the
@@ -206,7 +206,7 @@ def measure_batched(tune_space=None):
     from quicksilver_gb300.autotune import autotune
     from quicksilver_gb300.decks.make_decks import config3
     from quicksilver_gb300.monte_carlo import BatchMonteCarlo, MonteCarlo, seed_offset
-    texts = config3()
+    texts = config3()[:n_problems]
     decks = [Deck.from_string(t) for t in texts]
     problems = [d.build() for d in decks]
     offs = [seed_offset(d.simulation.seed) for d in decks]
@@ -214,7 +214,10 @@ def measure_batched(tune_space=None):
     t0 = time.perf_counter()
     space = tune_space or {"block_size": (128,), "pool_collision_step": (24, 32), "pool_refill": (8, 16, 32),
                            "flux_replicas": (1,)}
-    best = autotune(texts, scale=0.1, cycles=1, warmup=1, cache_path=None, space=space, problems=problems)
+    if fixed_shape is None:
+        best = autotune(texts, scale=0.1, cycles=1, warmup=1, cache_path=None, space=space, problems=problems)
+    else:
+        best = dict(fixed_shape)
     tune_s = time.perf_counter() - t0
     bmc = BatchMonteCarlo(decks, problems=problems, seed_offsets=offs, flux_replicas=best["flux_replicas"])
     try:
@@ -285,8 +288,8 @@ def measure_batched(tune_space=None):
                                                         "plain_segments_per_s": sp / tp if tp else None}
     for hp in problems:
         hp.close()
-    return {"workload": "64 independent problems (mesh edge from {8,16,24,32,48} cm, 1e4-2e6 particles "
-                        "log-uniform, 1-3 materials, 230 groups), 10 cycles each after 1 warm-up cycle",
+    return {"workload": f"{n_problems} independent problems (mesh edge from {{8,16,24,32,48}} cm, 1e4-2e6 "
+                        "particles log-uniform, 1-3 materials, 230 groups), 10 cycles each after 1 warm-up cycle",
             "batched_segments_per_s": seg_b / t_batch, "batched_s": t_batch,
             "plain_problem_by_problem_segments_per_s": seg_plain / t_plain, "plain_s": t_plain,
             "speedup_at_equal_tally_error": (seg_b / t_batch) / (seg_plain / t_plain),
@@ -388,6 +391,23 @@ def measure_adjoint(replicas=6):
             "speedup_at_equal_tally_error_over_components": speedups,
             "effective_segments_per_s": speedup * rate_plain,
             "timing": "wall clock of MonteCarlo.run (20 whole cycles), synchronised; handle set-up excluded"}
+
+
+def run_config3(args):
+    """--workload config3: the batched form alone (its own JSON line), the
+    uneven ensemble's first --config3-problems problems; --fixed-shape skips
+    the autotuner (block 128, collision step 32, refill 8, one flux replica),
+    which keeps the launch sequence short for a profiler."""
+    shape = ({"block_size": 128, "pool_collision_step": 32, "pool_refill": 8, "flux_replicas": 1}
+             if args.fixed_shape else None)
+    with ClockSampler(0) as clocks:
+        b = measure_batched(n_problems=args.config3_problems, fixed_shape=shape)
+    line = {"metric": METRIC, "value": b["batched_segments_per_s"], "unit": "segments/s", "n_gpus": 1,
+            "steps": 10, "warmup": 1, "ms_per_step": 1e3 * b["batched_s"] / 10, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded decks make_decks.config3)",
+            "config": {"workload": b["workload"], "step": "one whole cycle of every problem (CUDA graph)"},
+            "forms": {"batched": b}, "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
 
 
 def run_config5(args):
@@ -533,8 +553,11 @@ def main():
     ap.add_argument("--flux-replicas", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and differentiated forms")
-    ap.add_argument("--workload", default="config2", choices=["config2", "config5"],
-                    help="config5: the large batched + differentiated run (its own JSON line)")
+    ap.add_argument("--workload", default="config2", choices=["config2", "config3", "config5"],
+                    help="config3: the batched form alone; config5: the large batched + differentiated run "
+                         "(each its own JSON line)")
+    ap.add_argument("--config3-problems", type=int, default=64, help="config3: the first this many problems")
+    ap.add_argument("--fixed-shape", action="store_true", help="config3: no autotuner, the default kernel shape")
     ap.add_argument("--config5-scale", type=float, default=1.0,
                     help="particle-count scale of config5 (>= 0.3: below that no cell sources a particle)")
     ap.add_argument("--kernel", type=int, default=1, choices=[0, 1],
@@ -546,9 +569,9 @@ def main():
     if args.impl == "reference":
         run_reference_arm(args, world, rank)
         return
-    if args.workload == "config5":
+    if args.workload in ("config3", "config5"):
         if rank == 0:
-            run_config5(args)
+            (run_config3 if args.workload == "config3" else run_config5)(args)
         return
 
     import torch

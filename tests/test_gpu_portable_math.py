@@ -64,6 +64,6 @@ def test_portable_math_tracking_is_bitwise(gpu, pm_lib, deck, cycles):
     assert out["census_bitwise"] and out["flux_worst_over_tolerance"] <= 1.0
 
 
-@pytest.mark.parametrize("deck", ["t_homog", "t_escape", "t_fission", "t_nonflat", "config1"])
+@pytest.mark.parametrize("deck", ["t_homog", "t_escape", "t_fission", "t_nonflat", "config1", "config2"])
 def test_portable_math_device_cycles_are_the_reference(gpu, pm_lib, deck):
     assert _child("cycles", deck)["particles_bitwise"]

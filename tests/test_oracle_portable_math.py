@@ -26,7 +26,7 @@ import oracle_py as O
 from helpers import DECKS, assert_flux_close, load_problem, oracle_run, sort_particles
 
 GOLDEN = DECKS.parent.parent / "tests" / "golden"
-PM_DECKS = ["t_homog", "t_escape", "t_scatter_octant", "t_fission", "t_nonflat", "config1"]
+PM_DECKS = ["t_homog", "t_escape", "t_scatter_octant", "t_fission", "t_nonflat", "config1", "config2"]
 
 
 def _ulps(a, b):
@@ -62,7 +62,7 @@ def test_portable_functions_are_faithful():
     assert sn[5] == 0.0 and cs[5] == 1.0 and sn[6] == 1.0
 
 
-@pytest.mark.parametrize("name", PM_DECKS)
+@pytest.mark.parametrize("name", PM_DECKS[:-1])
 def test_portable_math_changes_no_counter_of_the_reference(name):
     pm, stock = np.load(GOLDEN / f"pm_{name}.npz"), np.load(GOLDEN / f"{name}.npz")
     np.testing.assert_array_equal(pm["balance"], stock["balance"])
@@ -86,7 +86,7 @@ def _sha(recs):
 @pytest.mark.parametrize("name", PM_DECKS)
 def test_oracle_portable_math_is_the_reference_bit_for_bit(portable_math, name):
     gold = np.load(GOLDEN / f"pm_{name}.npz")
-    _, sim, hp = load_problem(f"{name}.inp")
+    _, sim, hp = load_problem(f"{name}.inp", {"nSteps": len(gold["balance"])})
     run = oracle_run(hp, sim)
     for c in range(len(gold["balance"])):
         run.cycle_init()
@@ -97,7 +97,7 @@ def test_oracle_portable_math_is_the_reference_bit_for_bit(portable_math, name):
         np.testing.assert_array_equal(bal, gold["balance"][c], err_msg=f"{name} cycle {c}")
         assert _sha(run.processed()) == gold["census_sha"][c], f"{name} cycle {c}: census particles"
         flux = run.flux()
-        if c < len(gold["flux"]):
+        if "flux" in gold and c < len(gold["flux"]):
             assert_flux_close(flux, gold["flux"][c], rel=1e-12, scale_floor=0.0)
         assert_flux_close(flux.sum(axis=1), gold["flux_cell"][c], rel=1e-12)
         assert_flux_close(flux.sum(axis=0), gold["flux_group"][c], rel=1e-12)
