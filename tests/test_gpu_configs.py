@@ -40,7 +40,8 @@ tests/test_oracle_golden.py).
   counters bit for bit, flux totals within 1e-12, per-cell forward flux
   within 1e-8 (config2's per-cell bound), dflux and dleak within 1e-8 per
   entry (sums of terms of both signs), all moved by the retry of the facet
-  search as config2's flux is.
+  search as config2's flux is; leakage within 1e-10 (one accumulator per
+  replica summed in a different order).
 
 Reference behaviour reproduced: CycleTracking.cc:33-120, Tallies.cc:25-98,
 main.cc:96-324, MC_SourceNow.cc:28-164, PopulationControl.cc:20-171.
@@ -209,5 +210,7 @@ def test_config5_scaled_batch_with_sensitivities_matches_oracle(gpu):
         assert abs(sens["flux_cell"][rows].sum() - fc.sum()) <= 1e-12 * fc.sum()
         for k in range(df.shape[1]):
             assert_flux_close(sens["dflux"][rows, k], df[:, k], rel=1e-8, scale_floor=1e-12)
-        np.testing.assert_allclose(sens["leak"][p], leak, rtol=1e-12, atol=0)
+        # one accumulator per replica, ~1e6 escaping weights added in a
+        # different order: summation alone reaches ~1e-11 relative here
+        np.testing.assert_allclose(sens["leak"][p], leak, rtol=1e-10, atol=0)
         np.testing.assert_allclose(sens["dleak"][p], dl, rtol=1e-8, atol=1e-12 * abs(leak))
