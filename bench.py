@@ -152,42 +152,6 @@ def fp64_roofline(fp64_per_segment, segments_per_s_per_gpu, peak):
             "per_segment_source": "ncu sm__inst_executed_pipe_fp64.sum / segments, " + PROFILE_DATA.name}
 
 
-def cpu_port_rate(deck_path: Path, warmup: int, steps: int, threads: int):
-    """The CPU port (oracle) on the host cores, timed as the reference arm
-    times it: `warmup` whole cycles, then the tracking of `steps` cycles
-    with `threads` OpenMP threads, then one more cycle on one core.  Returns
-    (segments/s, segments, seconds, 1-core segments/s, 1-core segments,
-    1-core seconds)."""
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle_py
-    from quicksilver_gb300 import Deck
-    deck = Deck.from_file(deck_path)
-    sim = deck.simulation
-    hp = deck.build()
-    run = oracle_py.OracleRun(hp.ptr, hp.num_cells, hp.num_groups, hp.source_rates(), sim.n_particles,
-                              sim.e_min, sim.e_max, sim.low_weight_cutoff, sim.load_balance, keepalive=hp)
-
-    def one(nthreads):
-        run.cycle_init()
-        t0 = time.perf_counter()
-        run.cycle_tracking(nthreads)
-        dt = time.perf_counter() - t0
-        n = int(run.balance()[12])
-        run.cycle_finalize()
-        return n, dt
-
-    for _ in range(warmup):
-        one(threads)
-    seg, secs = 0, 0.0
-    for _ in range(steps):
-        n, dt = one(threads)
-        seg += n
-        secs += dt
-    seg1, secs1 = one(1)
-    run.close()
-    return seg / secs, seg, secs, seg1 / secs1, seg1, secs1
-
-
 def _sync():
     import torch
     torch.cuda.synchronize()
@@ -531,7 +495,16 @@ def run_reference_arm(args, world, rank):
         seg += int(run.balance()[12])
         run.cycle_finalize()
     value = seg / secs
-    sample = f"{args.steps} whole config2 cycles ({seg} segments) after {args.warmup} warm-up cycles"
+    # one more cycle on one core, for the scaling of the CPU path
+    run.cycle_init()
+    t0 = time.perf_counter()
+    run.cycle_tracking(1)
+    secs1 = time.perf_counter() - t0
+    seg1 = int(run.balance()[12])
+    run.cycle_finalize()
+    run.close()
+    sample = (f"{args.steps} whole config2 cycles ({seg} segments) after {args.warmup} warm-up cycles, "
+              f"{threads} OpenMP threads")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "segments/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -539,9 +512,24 @@ def run_reference_arm(args, world, rank):
             "config": {"workload": WORKLOAD, "impl": "CPU port of the reference algorithm (oracle/qs_oracle.c), "
                        "OpenMP over particles; the reference C++ sources are not present on this host"},
             "cpu_baseline": {"value": value, "unit": "segments/s", "cores": threads, "kind": "port",
-                             "sample": sample},
+                             "sample": sample, "value_1_thread": seg1 / secs1,
+                             "sample_1_thread": f"config2 cycle {args.warmup + args.steps} ({seg1} segments, "
+                                                f"{secs1:.1f} s) on one core"},
             "e2e": {"value": value, "unit": "segments/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def reference_arm_baseline(warmup: int, steps: int):
+    """cpu_baseline of the GPU line: the reference arm itself (`--impl
+    reference`, same cycles) run in a fresh child process, so that both
+    numbers come from one measurement path."""
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    res = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", str(steps),
+                          "--warmup", str(warmup)], capture_output=True, text=True, env=env, cwd=str(ROOT))
+    lines = [l for l in res.stdout.splitlines() if l.startswith("{")]
+    if res.returncode != 0 or not lines:
+        return {"value": None, "unavailable": (res.stderr or "no output")[-300:]}
+    return json.loads(lines[-1])["cpu_baseline"]
 
 
 def main():
@@ -726,16 +714,7 @@ def main():
         # the forms compare single-GPU paths; replica runs (N > 1) report the plain line only
         line["forms"] = {"batched": measure_batched(), "adjoint": measure_adjoint()}
     if not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        rate, seg, secs, rate1, seg1, secs1 = cpu_port_rate(DECK, args.warmup, args.steps, threads)
-        w, k = args.warmup, args.steps
-        line["cpu_baseline"] = {"value": rate, "unit": "segments/s", "cores": threads, "kind": "port",
-                                "sample": f"config2 cycles {w}-{w + k - 1} ({seg} segments, {secs:.1f} s tracking) "
-                                          f"after {w} warm-up cycles, {threads} OpenMP threads: the cycles the "
-                                          f"reference arm times",
-                                "value_1_thread": rate1,
-                                "sample_1_thread": f"config2 cycle {w + k} ({seg1} segments, {secs1:.1f} s) on one "
-                                                   f"core"}
+        line["cpu_baseline"] = reference_arm_baseline(args.warmup, args.steps)
     print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()
