@@ -279,6 +279,26 @@ __device__ __forceinline__ uint32_t face_facets_screen(const FaceScreen& fs, uin
     return res;
 }
 
+// Find_Nearest's rules (MCT.cc:436-479) for one facet's value, stated so that
+// the facets may be visited in any order: the smallest positive distance, a
+// later facet winning a tie (the reference's `<=` in ascending order); else the
+// largest non-positive one, an earlier facet winning a tie (its strict `>`);
+// _hugeDouble is kept apart as the highest facet holding it.  Ties compare
+// IEEE order keys, as the reference's comparisons do (-0.0 equals +0.0).
+__device__ __forceinline__ void nearest_visit(double d, int f, double& best, int& best_f, double& neg, int& neg_f,
+                                              int& huge_f)
+{
+    if (f64_eq(d, kHugeDouble)) {
+        if (f > huge_f) huge_f = f;
+    } else if (f64_gt0(d)) {
+        const long long kd = f64_key(d), kb = f64_key(best);
+        if (kd < kb || (kd == kb && f > best_f)) { best = d; best_f = f; }
+    } else {
+        const long long kd = f64_key(d), kn = f64_key(neg);
+        if (kn < kd || (kn == kd && f < neg_f)) { neg = d; neg_f = f; }
+    }
+}
+
 // MCT_Nearest_Facet (MCT.cc:86-137) with MCT_Nearest_Facet_3D_G
 // (MCT.cc:549-621) and both Find_Nearest overloads (MCT.cc:436-536).
 // Facets the FP32 screen proves to be _hugeDouble are not evaluated; the rest
@@ -286,7 +306,10 @@ __device__ __forceinline__ uint32_t face_facets_screen(const FaceScreen& fs, uin
 // to the 24 values: the smallest positive distance with `<=` (a later facet
 // wins a tie); if none, the largest non-positive one; _hugeDouble entries
 // count as positive, so when no finite positive distance exists the result is
-// _hugeDouble at the highest-numbered facet holding it.
+// _hugeDouble at the highest-numbered facet holding it.  The proven-accepted
+// facets (numerator / dot) and the facets that need the full test are visited
+// in two loops, so a warp whose lanes hold some of each runs each body once per
+// facet of the lane with most of that kind, not both bodies per facet.
 // Moves the particle toward the cell centre on a retry, as the reference
 // does through its coordinate reference (MCT.cc:510, 656-666).
 __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Particle& p, int& facet_out)
@@ -376,55 +399,50 @@ __device__ double nearest_facet(const DevTables& t, const DevTally& tally, Parti
             }
         }
 #endif
-        if (exact) {
-            uint32_t m = exact;
-            while (m) {
-                const int f = __ffs(m) - 1;
-                m &= m - 1;
-                const double2 ab = __ldg(reinterpret_cast<const double2*>(planes + 4 * f));
-                const double2 cd = __ldg(reinterpret_cast<const double2*>(planes + 4 * f + 2));
-                double d = kHugeDouble;
-                const double dot = ab.x * p.alpha + ab.y * p.beta + cd.x * p.gamma;
-                if ((accept >> f) & 1u) {
-                    const double numerator = -1.0 * (ab.x * p.x + ab.y * p.y + cd.x * p.z + cd.y);
-                    d = numerator / dot;
+        for (uint32_t m = accept; m != 0; m &= m - 1) {
+            const int f = __ffs(m) - 1;
+            const double2 ab = __ldg(reinterpret_cast<const double2*>(planes + 4 * f));
+            const double2 cd = __ldg(reinterpret_cast<const double2*>(planes + 4 * f + 2));
+            const double dot = ab.x * p.alpha + ab.y * p.beta + cd.x * p.gamma;
+            const double numerator = -1.0 * (ab.x * p.x + ab.y * p.y + cd.x * p.z + cd.y);
+            const double d = numerator / dot;
 #ifdef QSG_VERIFY_SCREEN
-                    double q0[3], q1[3], q2[3];
-                    for (int k = 0; k < 3; k++) {
-                        q0[k] = nodes[3 * kFacetLocal[f][0] + k];
-                        q1[k] = nodes[3 * kFacetLocal[f][1] + k];
-                        q2[k] = nodes[3 * kFacetLocal[f][2] + k];
-                    }
-                    const double plane_tolerance = 1e-16 * (p.x * p.x + p.y * p.y + p.z * p.z);
-                    const double full = (dot > 0.0) ? distance_to_segment(plane_tolerance, dot, ab.x, ab.y, cd.x, cd.y,
-                                                                          q0, q1, q2, p)
-                                                    : kHugeDouble;
-                    if (full != d) raise_flag(tally, QSG_DEV_SCREEN_MISS);
-#endif
-                } else if (dot > 0.0) {
-                    double q0[3], q1[3], q2[3];
-                    const double* n0 = nodes + 3 * kFacetLocal[f][0];
-                    const double* n1 = nodes + 3 * kFacetLocal[f][1];
-                    const double* n2 = nodes + 3 * kFacetLocal[f][2];
-#pragma unroll
-                    for (int k = 0; k < 3; k++) {
-                        q0[k] = __ldg(n0 + k);
-                        q1[k] = __ldg(n1 + k);
-                        q2[k] = __ldg(n2 + k);
-                    }
-                    // (1e-8 * |r|)^2 of MCT.cc:569-571, which only the full test uses
-                    const double plane_tolerance = 1e-16 * (p.x * p.x + p.y * p.y + p.z * p.z);
-                    d = distance_to_segment(plane_tolerance, dot, ab.x, ab.y, cd.x, cd.y, q0, q1, q2, p);
-                }
-                if (f64_eq(d, kHugeDouble)) {
-                    if (f > huge_f) huge_f = f;
-                } else if (f64_gt0(d)) {
-                    if (f64_le(d, best)) { best = d; best_f = f; }
-                } else if (f64_lt(neg, d)) {
-                    neg = d;
-                    neg_f = f;
-                }
+            double q0[3], q1[3], q2[3];
+            for (int k = 0; k < 3; k++) {
+                q0[k] = nodes[3 * kFacetLocal[f][0] + k];
+                q1[k] = nodes[3 * kFacetLocal[f][1] + k];
+                q2[k] = nodes[3 * kFacetLocal[f][2] + k];
             }
+            const double plane_tolerance = 1e-16 * (p.x * p.x + p.y * p.y + p.z * p.z);
+            const double full = (dot > 0.0) ? distance_to_segment(plane_tolerance, dot, ab.x, ab.y, cd.x, cd.y,
+                                                                  q0, q1, q2, p)
+                                            : kHugeDouble;
+            if (full != d) raise_flag(tally, QSG_DEV_SCREEN_MISS);
+#endif
+            nearest_visit(d, f, best, best_f, neg, neg_f, huge_f);
+        }
+        for (uint32_t m = exact & ~accept; m != 0; m &= m - 1) {
+            const int f = __ffs(m) - 1;
+            const double2 ab = __ldg(reinterpret_cast<const double2*>(planes + 4 * f));
+            const double2 cd = __ldg(reinterpret_cast<const double2*>(planes + 4 * f + 2));
+            double d = kHugeDouble;
+            const double dot = ab.x * p.alpha + ab.y * p.beta + cd.x * p.gamma;
+            if (dot > 0.0) {
+                double q0[3], q1[3], q2[3];
+                const double* n0 = nodes + 3 * kFacetLocal[f][0];
+                const double* n1 = nodes + 3 * kFacetLocal[f][1];
+                const double* n2 = nodes + 3 * kFacetLocal[f][2];
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    q0[k] = __ldg(n0 + k);
+                    q1[k] = __ldg(n1 + k);
+                    q2[k] = __ldg(n2 + k);
+                }
+                // (1e-8 * |r|)^2 of MCT.cc:569-571, which only the full test uses
+                const double plane_tolerance = 1e-16 * (p.x * p.x + p.y * p.y + p.z * p.z);
+                d = distance_to_segment(plane_tolerance, dot, ab.x, ab.y, cd.x, cd.y, q0, q1, q2, p);
+            }
+            nearest_visit(d, f, best, best_f, neg, neg_f, huge_f);
         }
         // _hugeDouble is positive and larger than any finite distance, so it
         // only wins when no finite positive distance exists
