@@ -6,7 +6,7 @@ Run by tests/test_gpu_verify_screen.py in a child process with
 QSG_LIB=verify (the library variant is chosen when quicksilver_gb300._native
 is first imported, so it cannot change within one process):
 
-    QSG_LIB=verify python tests/verify_screen_run.py DECK.inp CYCLES
+    QSG_LIB=verify python tests/verify_screen_run.py DECK.inp CYCLES [PARTICLES]
 """
 import json
 import sys
@@ -21,7 +21,8 @@ from quicksilver_gb300.monte_carlo import MonteCarlo  # noqa: E402
 
 def main() -> None:
     deck_path, cycles = Path(sys.argv[1]), int(sys.argv[2])
-    deck = Deck.from_file(deck_path)
+    overrides = {"nParticles": int(sys.argv[3])} if len(sys.argv) > 3 else None
+    deck = Deck.from_file(deck_path, overrides)
     mc = MonteCarlo(deck)
     try:
         for _ in range(cycles):
