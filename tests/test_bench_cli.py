@@ -42,3 +42,15 @@ def test_profile_figures_and_fp64_roofline(tmp_path, monkeypatch):
     r = bench.fp64_roofline(per_seg, 2.0e9, 1.5e10)
     assert abs(r["achieved"] - per_seg * 2.0e9) < 1.0 and abs(r["frac"] - r["achieved"] / 1.5e10) < 1e-12
     assert bench.fp64_roofline(None, 2.0e9, 1.5e10) is None
+
+
+def test_committed_profile_matches_kernel_sources():
+    """The committed per-segment figures were captured from the kernel sources
+    as they are: a change to track.cu / track_device.cuh needs a new capture
+    (the ncu command recorded in the profile) before bench.py's FP64 roofline
+    is reported again."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    data, current = bench.profile_figures()
+    assert current, ("kernel sources changed since the capture in " + str(bench.PROFILE_DATA.name) +
+                     "; recapture with: " + data.get("captured", "?"))
