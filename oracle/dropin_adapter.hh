@@ -33,25 +33,34 @@
 
 extern MonteCarlo* mcco;   // main.cc:36; the reference's timer macros name it
 
-// Host copies of one domain's tables in the library's layout; `problem`
-// points into them, so it stays valid while the QsgExport lives.
+// Host copies of the rank's tables in the library's layout; `problem`
+// points into them, so it stays valid while the QsgExport lives.  The rank's
+// domains are laid end to end as one mesh: domain d's cell c is cell
+// cell_offset[d] + c, its node v node node_offset[d] + v.
 struct QsgExport {
     std::vector<int32_t> iso_off{0}, rtype, mat_off{0}, mat_gid, pts, local, ev, adj_cell, adj_facet, mat;
     std::vector<double> nubar, xs, af, mass, planes, density, volume, nodes;
     std::vector<uint64_t> ids;
+    std::vector<int32_t> cell_offset{0}, cell_domain;   // [domains + 1], [cells]
     QsgProblem problem{};
 };
 
-// one domain (xDom = yDom = zDom = 1): MonteCarlo -> QsgProblem
+// MonteCarlo -> QsgProblem.  On one rank every neighbouring domain is on the
+// processor (MC_Domain.cc:262-268: Transit_On_Processor, the adjacent
+// location given as domain index and local cell), and a boundary facet names
+// its own cell, so every facet's neighbour is cell_offset[adjacent.domain] +
+// adjacent.cell; histories on the joined mesh are the reference's on its
+// domains (crossing between them only relabels the particle's domain).
 void qsgExport(MonteCarlo* mc, QsgExport& e)
 {
     NuclearData& nd = *mc->_nuclearData;
     MaterialDatabase& mdb = *mc->_materialDatabase;
-    MC_Domain& dom = mc->domain[0];
-    const int G = nd._numEnergyGroups, C = dom.cell_state.size();
+    const int D = mc->domain.size();
+    for (int d = 0; d < D; ++d) e.cell_offset.push_back(e.cell_offset.back() + (int)mc->domain[d].cell_state.size());
+    const int G = nd._numEnergyGroups, C = e.cell_offset[D];
     e.pts.resize(C * 14); e.local.resize(72); e.ev.resize(C * 24); e.adj_cell.resize(C * 24);
     e.adj_facet.resize(C * 24); e.mat.resize(C); e.planes.resize(C * 96); e.density.resize(C);
-    e.volume.resize(C); e.ids.resize(C);
+    e.volume.resize(C); e.ids.resize(C); e.cell_domain.resize(C);
     for (int i = 0; i < nd._isotopes.size(); ++i) {
         qs_vector<NuclearDataReaction>& rs = nd._isotopes[i]._species[0]._reactions;
         for (int r = 0; r < rs.size(); ++r) {
@@ -69,29 +78,36 @@ void qsgExport(MonteCarlo* mc, QsgExport& e)
         e.mat_off.push_back(e.mat_gid.size());
         e.mass.push_back(mdb._mat[m]._mass);
     }
-    for (int v = 0; v < dom.mesh._node.size(); ++v) {
-        e.nodes.push_back(dom.mesh._node[v].x);
-        e.nodes.push_back(dom.mesh._node[v].y);
-        e.nodes.push_back(dom.mesh._node[v].z);
-    }
-    for (int c = 0; c < C; ++c) {
-        MC_Facet_Adjacency_Cell& cc = dom.mesh._cellConnectivity[c];
-        for (int p = 0; p < 14; ++p) e.pts[c * 14 + p] = cc._point[p];
-        for (int f = 0; f < 24; ++f) {
-            MC_General_Plane& pl = dom.mesh._cellGeometry[c]._facet[f];
-            double* o = &e.planes[(c * 24 + f) * 4];
-            o[0] = pl.A; o[1] = pl.B; o[2] = pl.C; o[3] = pl.D;
-            e.ev[c * 24 + f] = cc._facet[f].subfacet.event;   // same numbering as QSG_ADJ_*
-            e.adj_cell[c * 24 + f] = cc._facet[f].subfacet.adjacent.cell;
-            e.adj_facet[c * 24 + f] = cc._facet[f].subfacet.adjacent.facet;
-            if (c == 0)   // facet corners as indices into the cell's 14 points
-                for (int k = 0; k < 3; ++k)
-                    e.local[f * 3 + k] = std::find(cc._point, cc._point + 14, cc._facet[f].point[k]) - cc._point;
+    for (int d = 0; d < D; ++d) {
+        MC_Domain& dom = mc->domain[d];
+        const int node0 = e.nodes.size() / 3;
+        for (int v = 0; v < dom.mesh._node.size(); ++v) {
+            e.nodes.push_back(dom.mesh._node[v].x);
+            e.nodes.push_back(dom.mesh._node[v].y);
+            e.nodes.push_back(dom.mesh._node[v].z);
         }
-        e.mat[c] = dom.cell_state[c]._material;
-        e.density[c] = dom.cell_state[c]._cellNumberDensity;
-        e.volume[c] = dom.cell_state[c]._volume;
-        e.ids[c] = dom.cell_state[c]._id;
+        for (int lc = 0; lc < (int)dom.cell_state.size(); ++lc) {
+            const int c = e.cell_offset[d] + lc;
+            MC_Facet_Adjacency_Cell& cc = dom.mesh._cellConnectivity[lc];
+            for (int p = 0; p < 14; ++p) e.pts[c * 14 + p] = node0 + cc._point[p];
+            for (int f = 0; f < 24; ++f) {
+                MC_General_Plane& pl = dom.mesh._cellGeometry[lc]._facet[f];
+                double* o = &e.planes[(c * 24 + f) * 4];
+                o[0] = pl.A; o[1] = pl.B; o[2] = pl.C; o[3] = pl.D;
+                const Subfacet_Adjacency& sf = cc._facet[f].subfacet;
+                e.ev[c * 24 + f] = sf.event;   // same numbering as QSG_ADJ_*
+                e.adj_cell[c * 24 + f] = e.cell_offset[sf.adjacent.domain] + sf.adjacent.cell;
+                e.adj_facet[c * 24 + f] = sf.adjacent.facet;
+                if (c == 0)   // facet corners as indices into the cell's 14 points
+                    for (int k = 0; k < 3; ++k)
+                        e.local[f * 3 + k] = std::find(cc._point, cc._point + 14, cc._facet[f].point[k]) - cc._point;
+            }
+            e.mat[c] = dom.cell_state[lc]._material;
+            e.density[c] = dom.cell_state[lc]._cellNumberDensity;
+            e.volume[c] = dom.cell_state[lc]._volume;
+            e.ids[c] = dom.cell_state[lc]._id;
+            e.cell_domain[c] = d;
+        }
     }
     QsgProblem& p = e.problem;
     p.num_groups = G;                   p.energies = &nd._energies[0];
@@ -115,10 +131,6 @@ static QsgExport g_export;   // qsg_create copies the tables; the cycle code bel
 
 void qsgAttach(MonteCarlo* mc)
 {
-    if (mc->domain.size() != 1) {   // xDom = yDom = zDom = 1 tracks the same histories as the 4-domain default
-        printf("qsgAttach: %d domains; the library tracks one (set xDom = yDom = zDom = 1)\n", (int)mc->domain.size());
-        return;
-    }
     qsgExport(mc, g_export);
     QsgOptions o{};
     o.flux_replicas = mc->_params.simulationParams.fluxTallyReplications;
@@ -166,7 +178,8 @@ size_t qsgGather(ParticleVaultContainer& pvc, bool processed, QsgColumns& cols)
             const double dd[12] = {b.coordinate.x, b.coordinate.y, b.coordinate.z, b.velocity.x, b.velocity.y,
                                    b.velocity.z, b.kinetic_energy, b.weight, b.time_to_census, b.age,
                                    b.num_mean_free_paths, b.num_segments};
-            const int32_t ii[6] = {b.last_event, b.num_collisions, b.breed, b.species, b.domain, b.cell};
+            const int32_t ii[6] = {b.last_event, b.num_collisions, b.breed, b.species, b.domain,
+                                   g_export.cell_offset[b.domain] + b.cell};   // the joined mesh's cell
             for (int f = 0; f < 12; ++f) cols.d[f][k] = dd[f];
             for (int f = 0; f < 6; ++f) cols.i[f][k] = ii[f];
             cols.q[0][k] = b.random_number_seed;
@@ -193,7 +206,10 @@ void qsgScatterCensus(const QsgColumns& cols, size_t n, ParticleVaultContainer& 
             b.random_number_seed = cols.q[0][k];    b.identifier = cols.q[1][k];
             b.last_event = (MC_Tally_Event::Enum)cols.i[0][k];
             b.num_collisions = cols.i[1][k];  b.breed = cols.i[2][k];   b.species = cols.i[3][k];
-            b.domain = cols.i[4][k];          b.cell = cols.i[5][k];
+            // the joined mesh's cell -> its domain and the cell within it (the
+            // domain a Transit_On_Processor crossing sets, MC_Facet_Crossing_Event.cc:29-34)
+            b.domain = g_export.cell_domain[cols.i[5][k]];
+            b.cell = cols.i[5][k] - g_export.cell_offset[b.domain];
             vault.pushBaseParticle(b);
         }
     }
@@ -209,10 +225,12 @@ void qsgAddTallies(MonteCarlo* mc, const uint64_t* bal, const double* flux)
     b._escape += bal[QSG_BAL_ESCAPE];       b._collision += bal[QSG_BAL_COLLISION];
     b._fission += bal[QSG_BAL_FISSION];     b._produce += bal[QSG_BAL_PRODUCE];
     b._scatter += bal[QSG_BAL_SCATTER];     b._numSegments += bal[QSG_BAL_NUM_SEGMENTS];
-    ScalarFluxTask& t = mc->_tallies->_scalarFluxDomain[0]._task[0];
-    const int C = g_export.problem.num_cells, G = g_export.problem.num_groups;
-    for (int c = 0; c < C; ++c)
-        for (int g = 0; g < G; ++g) t._cell[c]._group[g] += flux[(size_t)c * G + g];
+    const int G = g_export.problem.num_groups;
+    for (int d = 0; d + 1 < (int)g_export.cell_offset.size(); ++d) {
+        ScalarFluxTask& t = mc->_tallies->_scalarFluxDomain[d]._task[0];
+        for (int c = g_export.cell_offset[d]; c < g_export.cell_offset[d + 1]; ++c)
+            for (int g = 0; g < G; ++g) t._cell[c - g_export.cell_offset[d]]._group[g] += flux[(size_t)c * G + g];
+    }
 }
 
 #ifdef EXPONENTIAL_TALLY
@@ -220,8 +238,11 @@ void qsgAddTallies(MonteCarlo* mc, const uint64_t* bal, const double* flux)
 // (Tallies.hh:126-165), which cycleFinalize resets (Tallies.cc:91)
 void qsgAddCellTally(MonteCarlo* mc, const double* cell_tally)
 {
-    CellTallyTask& t = mc->_tallies->_cellTallyDomain[0]._task[0];
-    for (int c = 0; c < g_export.problem.num_cells; ++c) t._cell[c] += cell_tally[c];
+    for (int d = 0; d + 1 < (int)g_export.cell_offset.size(); ++d) {
+        CellTallyTask& t = mc->_tallies->_cellTallyDomain[d]._task[0];
+        for (int c = g_export.cell_offset[d]; c < g_export.cell_offset[d + 1]; ++c)
+            t._cell[c - g_export.cell_offset[d]] += cell_tally[c];
+    }
 }
 #endif
 

@@ -116,11 +116,7 @@ int main(int argc, char** argv)
     mpiInit(&argc, &argv);
     Parameters params = getParameters(argc, argv);
     mcco = initMC(params);
-    if (mcco->domain.size() != 1) {
-        fprintf(stderr, "dropin_harness: %d domains; the export covers one\n", (int)mcco->domain.size());
-        return 2;
-    }
-    qsgExport(mcco, g_export);
+    qsgExport(mcco, g_export);   // the rank's domains joined into one mesh
     const QsgProblem& p = g_export.problem;
     const QsgExport& e = g_export;
     const int rc = qsg_problem_check(&p);
@@ -157,8 +153,8 @@ int main(int argc, char** argv)
     put("cell_volume", 'd', p.cell_volume, C);
     put("cell_id", 'q', p.cell_id, C);
     put("time_step", 'd', &p.time_step, 1);
-    printf("dropin_harness: export accepted (%d cells, %d groups, %d isotopes, %d materials)\n",
-           p.num_cells, p.num_groups, p.num_isotopes, p.num_materials);
+    printf("dropin_harness: export accepted (%d domains, %d cells, %d groups, %d isotopes, %d materials)\n",
+           (int)mcco->domain.size(), p.num_cells, p.num_groups, p.num_isotopes, p.num_materials);
     int bad = 0;
     if (getenv("QS_VAULTS")) {
         bad = check_vaults_and_tallies(mcco, params);

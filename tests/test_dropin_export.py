@@ -17,12 +17,18 @@ with the unmodified reference's sources:
   per-cycle counters and flux totals, timer tables, figure of merit, CORAL2
   checks -- and spectrum file are the unmodified reference's; with the
   reference built with -DEXPONENTIAL_TALLY, that build's counters and cell
-  tally; a four-domain MonteCarlo is refused with a message;
+  tally; and with the reference's one-rank default of four domains
+  (xDom = yDom = zDom = 0), whose domains the adapter joins into one mesh,
+  the unmodified four-domain reference's counters and flux totals;
 * the cycle adapter's vault and tally halves around the reference's own
   first cycleInit: the particles it gathers from the processing vaults are
   the oracle's, bit for bit; scattering them into the processed vaults and
   gathering them back is exact, no vault above its size; the counters and
-  flux it hands over are what the reference's Tallies then hold.
+  flux it hands over are what the reference's Tallies then hold -- on one
+  domain and on four;
+* the export of a four-domain MonteCarlo, cells put in the reference's
+  global cell-id order, is this library's single-domain mesh table for
+  table (adjacency through the same permutation).
 
 Runs where the reference's sources and the harness built from them are
 present, and skips elsewhere."""
@@ -95,6 +101,18 @@ def test_cycle_adapter_vaults_and_tallies(name, tmp_path):
 GOLDEN = ROOT / "tests" / "golden"
 
 
+def _four_domain_deck(name, tmp_path):
+    """The deck with the reference's one-rank default decomposition
+    (xDom = yDom = zDom = 0: four domains, initMC.cc:255-270)."""
+    text = (DECKS / f"{name}.inp").read_text()
+    for key in ("xDom", "yDom", "zDom"):
+        assert f"   {key}: 1\n" in text
+        text = text.replace(f"   {key}: 1\n", f"   {key}: 0\n")
+    path = tmp_path / f"{name}_4dom.inp"
+    path.write_text(text)
+    return path
+
+
 @pytest.mark.skipif(not CYCLE.exists(), reason="the adapter's main-loop harness is absent")
 def test_reference_main_loop_through_adapter(tmp_path):
     gold = np.load(GOLDEN / "transcript_out.npz")
@@ -136,17 +154,100 @@ def test_reference_summary_through_adapter(name, tmp_path):
         assert g.split()[:14] == w.split()[:14], (g, w)
 
 
-@pytest.mark.skipif(not CYCLE.exists(), reason="the adapter's main-loop harness is absent")
-def test_adapter_refuses_more_than_one_domain(tmp_path):
-    """The reference's one-rank default (xDom = yDom = zDom = 0) builds four
-    domains; the adapter hands the library one and says so instead."""
-    text = (DECKS / "t_homog.inp").read_text()
-    for key in ("xDom", "yDom", "zDom"):
-        text = text.replace(f"   {key}: 1\n", f"   {key}: 0\n")
-    deck = tmp_path / "four_domains.inp"
-    deck.write_text(text)
-    res = subprocess.run([str(CYCLE), "-i", str(deck)], cwd=tmp_path, capture_output=True, text=True, timeout=300)
-    assert res.returncode == 2 and "qsgAttach: 4 domains" in res.stdout
+REF = ROOT / "oracle" / "_ref" / "qs_ref_harness"
+
+
+def _summary_rows(stdout):
+    lines = stdout.split("\n")
+    k = next(i for i, line in enumerate(lines) if line.startswith("cycle "))
+    return [line.split()[:14] for line in lines[k + 1:] if line[:8].strip().isdigit()]
+
+
+@pytest.mark.skipif(not (CYCLE.exists() and REF.exists()), reason="the adapter's main-loop harness is absent")
+@pytest.mark.parametrize("name", ["t_homog", "t_fission", "t_nonflat", "t_escape"])
+def test_four_domains_through_adapter(name, tmp_path):
+    """The reference's one-rank default builds four domains; the adapter joins
+    them into one mesh for the library and hands census particles and flux
+    back per domain.  Every cycle's counters and scalar-flux total printed by
+    the reference's main loop through the adapter are those printed by the
+    unmodified reference on the same four domains."""
+    deck = _four_domain_deck(name, tmp_path)
+    env = dict(os.environ, OMP_NUM_THREADS="4")
+    ref = subprocess.run([str(REF), "-i", str(deck)], cwd=tmp_path, capture_output=True, text=True, env=env,
+                         timeout=600)
+    got = subprocess.run([str(CYCLE), "-i", str(deck)], cwd=tmp_path, capture_output=True, text=True, env=env,
+                         timeout=600)
+    assert ref.returncode == 0 and got.returncode == 0, got.stdout[-2000:] + got.stderr[-2000:]
+    assert got.stdout.count("Building partition") == 4
+    want_rows, got_rows = _summary_rows(ref.stdout), _summary_rows(got.stdout)
+    assert len(got_rows) == len(want_rows) > 1 and int(want_rows[0][12]) > 0
+    for g, w in zip(got_rows, want_rows):
+        assert g == w, (g, w)
+
+
+def _by_cell_id(dump, hp):
+    """Position in the deck reader's mesh of every exported cell."""
+    ids = hp.array("cell_id")
+    order = np.argsort(ids)
+    pos = order[np.searchsorted(ids, dump["cell_id"], sorter=order)]
+    assert (ids[pos] == dump["cell_id"]).all() and len(np.unique(pos)) == len(pos) == hp.num_cells
+    return pos
+
+
+@pytest.mark.parametrize("name", ["t_homog", "t_nonflat", "t_escape", "t_scatter_octant"])
+def test_four_domain_export_is_one_mesh(name, tmp_path):
+    dump = tmp_path / "export.bin"
+    res = subprocess.run([str(HARNESS), "-i", str(_four_domain_deck(name, tmp_path))],
+                         env=dict(os.environ, QS_DUMP=str(dump)), capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr[-2000:]
+    assert "export accepted (4 domains" in res.stdout
+    got = read_dump(dump)
+    hp = Deck.from_file(DECKS / f"{name}.inp").build()
+    pos = _by_cell_id(got, hp)
+    C = hp.num_cells
+    per_cell = {"facet_planes": 96, "facet_event": 24, "facet_adjacent_facet": 24, "cell_material": 1,
+                "cell_number_density": 1, "cell_volume": 1}
+    for key, width in per_cell.items():
+        want = hp.array(key).reshape(C, width)[pos]
+        arr = got[key].reshape(C, width)
+        np.testing.assert_array_equal(arr.view(f"u{arr.dtype.itemsize}"), want.view(f"u{want.dtype.itemsize}"),
+                                      err_msg=key)
+    adj = got["facet_adjacent_cell"].reshape(C, 24)
+    np.testing.assert_array_equal(pos[adj], hp.array("facet_adjacent_cell").reshape(C, 24)[pos])
+    corners = got["nodes"].reshape(-1, 3)[got["cell_points"].reshape(-1, 14)]
+    ours = hp.array("nodes").reshape(-1, 3)[hp.array("cell_points").reshape(-1, 14)][pos]
+    np.testing.assert_array_equal(corners.view(np.uint64), ours.view(np.uint64))
+
+
+@pytest.mark.parametrize("name", ["t_homog", "t_fission"])
+def test_four_domain_vaults_and_tallies(name, tmp_path):
+    """Gathered from four domains, the first cycle's particles are the
+    oracle's (single domain) bit for bit once their joined-mesh cell is put
+    back to the deck reader's numbering (the domain field names the
+    reference's domain, so it is not compared); the round trip and the tally
+    hand-over checks of the harness pass."""
+    from helpers import load_problem, oracle_run, sort_particles
+    dump = tmp_path / "vaults.bin"
+    res = subprocess.run([str(HARNESS), "-i", str(_four_domain_deck(name, tmp_path))],
+                         env=dict(os.environ, QS_DUMP=str(dump), QS_VAULTS="1"), capture_output=True, text=True,
+                         timeout=300)
+    assert res.returncode == 0, res.stdout[-1000:] + res.stderr[-2000:]
+    got = read_dump(dump)
+    _, sim, hp = load_problem(f"{name}.inp")
+    pos = _by_cell_id(got, hp)
+    run = oracle_run(hp, sim)
+    run.cycle_init()
+    want = run.processing()
+    rec = np.zeros(len(want), want.dtype)
+    for field in want.dtype.names:
+        rec[field] = got["p_" + field]
+    rec["cell"] = pos[rec["cell"]]
+    rec["domain"] = want["domain"][0]
+    assert len(rec) == len(want)
+    a, b = sort_particles(rec), sort_particles(want)
+    for field in want.dtype.names:
+        size = a[field].dtype.itemsize
+        np.testing.assert_array_equal(a[field].view(f"u{size}"), b[field].view(f"u{size}"), err_msg=field)
 
 
 @pytest.mark.skipif(not CYCLE_EXP.exists(), reason="the adapter's main-loop harness for -DEXPONENTIAL_TALLY is absent")
