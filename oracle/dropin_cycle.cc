@@ -11,7 +11,7 @@
 // with the unmodified reference's.  Built with -DEXPONENTIAL_TALLY
 // (`make dropin_cycle_exp`) it also prints, after each cycle's tracking, the
 // cell tally the adapter handed to the reference's Tallies
-// ("cell_tally_total <sum>", summed in cell order).  Exit status 2 when
+// ("cell_tally_total <sum>", summed over domains, each in cell order).  Exit status 2 when
 // qsgAttach fails.
 
 #include <cstdio>
@@ -39,8 +39,10 @@ int main(int argc, char** argv)
         qsgCycleTracking(mcco);
 #ifdef EXPONENTIAL_TALLY
         double total = 0.0;
-        const CellTallyTask& t = mcco->_tallies->_cellTallyDomain[0]._task[0];
-        for (int c = 0; c < t._cell.size(); ++c) total += t._cell[c];
+        for (int d = 0; d < mcco->_tallies->_cellTallyDomain.size(); ++d) {
+            const CellTallyTask& t = mcco->_tallies->_cellTallyDomain[d]._task[0];
+            for (int c = 0; c < t._cell.size(); ++c) total += t._cell[c];
+        }
         printf("cell_tally_total %.17g\n", total);
 #endif
         cycleFinalize();

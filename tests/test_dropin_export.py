@@ -251,18 +251,22 @@ def test_four_domain_vaults_and_tallies(name, tmp_path):
 
 
 @pytest.mark.skipif(not CYCLE_EXP.exists(), reason="the adapter's main-loop harness for -DEXPONENTIAL_TALLY is absent")
+@pytest.mark.parametrize("domains", [1, 4])
 @pytest.mark.parametrize("name", ["t_homog", "t_fission"])
-def test_exponential_tally_build_through_adapter(name, tmp_path):
+def test_exponential_tally_build_through_adapter(name, domains, tmp_path):
     """The reference built with -DEXPONENTIAL_TALLY, the adapter switching the
     library's exponential tally on: every cycle's counters are that build's
     (tests/golden/exp_<deck>.npz, from the unmodified reference built with the
     define) and the cell tally handed to its Tallies sums to that build's
-    within 1e-12."""
+    within 1e-12 -- on one domain, and on the four-domain default, where the
+    adapter hands each domain its cells' share."""
     from quicksilver_gb300 import _native as N
     gold = np.load(GOLDEN / f"exp_{name}.npz")
-    res = subprocess.run([str(CYCLE_EXP), "-i", str(DECKS / f"{name}.inp")], cwd=tmp_path, capture_output=True,
+    deck = DECKS / f"{name}.inp" if domains == 1 else _four_domain_deck(name, tmp_path)
+    res = subprocess.run([str(CYCLE_EXP), "-i", str(deck)], cwd=tmp_path, capture_output=True,
                          text=True, timeout=600)
     assert res.returncode == 0, res.stderr[-2000:]
+    assert res.stdout.count("Building partition") == domains
     lines = res.stdout.split("\n")
     totals = [float(line.split()[1]) for line in lines if line.startswith("cell_tally_total ")]
     k = next(i for i, line in enumerate(lines) if line.startswith("cycle "))
