@@ -50,6 +50,8 @@ B_ALG_PER_SEGMENT = 288          # algorithmic HBM bytes per segment (136-B reco
 # per-segment ncu figures of the tracking kernel on this workload, with the
 # hash of the kernel sources they were captured from
 PROFILE_DATA = ROOT / "profiles" / "track_pool_kernel_config2.json"
+# the reference algorithm's FP64 operations per segment per workload (tests/golden/count_fp64_work.py)
+FP64_WORK = ROOT / "profiles" / "fp64_work_per_segment.json"
 KERNEL_SOURCES = [ROOT / "quicksilver_gb300" / "csrc" / "track.cu", ROOT / "quicksilver_gb300" / "csrc" / "track_device.cuh"]
 
 
@@ -150,6 +152,27 @@ def fp64_roofline(fp64_per_segment, segments_per_s_per_gpu, peak):
             "fp64_warp_instructions_per_segment": fp64_per_segment,
             "peak_source": "measured in this run (qsg_measure_fp64_rate: independent DFMA chains, 16 warps/SM)",
             "per_segment_source": "ncu sm__inst_executed_pipe_fp64.sum / segments, " + PROFILE_DATA.name}
+
+
+def fp64_work_roofline(workload, segments_per_s_per_gpu, peak_warp_instructions):
+    """The reference algorithm's FP64 work (its +, -, *, / and sqrt per
+    segment as written, counted by the C restatement on this workload;
+    FP64_WORK) done per second, against the device's FP64 FMA rate (the
+    measured DFMA warp-instruction rate x 32 lanes x 2 FLOP).  The kernel's
+    FP32 screen skips most of the algorithm's facet tests, so this can
+    approach or pass 1 without the FP64 pipe doing that much."""
+    if not FP64_WORK.exists() or not peak_warp_instructions:
+        return None
+    w = json.loads(FP64_WORK.read_text()).get("workloads", {}).get(workload)
+    if not w:
+        return None
+    per_seg = w["fp64_ops_per_segment"]
+    achieved = per_seg * segments_per_s_per_gpu
+    peak = 64.0 * peak_warp_instructions
+    return {"achieved": achieved, "peak": peak, "unit": "FLOP/s", "frac": achieved / peak,
+            "algorithm_fp64_ops_per_segment": per_seg,
+            "per_segment_source": FP64_WORK.name + " (" + w["workload"] + ")",
+            "peak_source": "measured in this run: qsg_measure_fp64_rate x 32 lanes x 2 FLOP per DFMA"}
 
 
 def _sync():
@@ -697,7 +720,9 @@ def main():
                      "note": "not HBM-bound: the binding roof is FP64 issue (fp64_issue)",
                      "profile": {"file": str(PROFILE_DATA.relative_to(ROOT)), "matches_kernel_source": prof_current,
                                  "captured": prof.get("captured") if prof else None},
-                     "fp64_issue": fp64_roofline(fp64_ps, seg_per_launch / (track_s / args.steps), fp64_peak)},
+                     "fp64_issue": fp64_roofline(fp64_ps, seg_per_launch / (track_s / args.steps), fp64_peak),
+                     "fp64_algorithm": fp64_work_roofline("config2", seg_per_launch / (track_s / args.steps),
+                                                          fp64_peak)},
         "e2e": {"value": e2e_seg / e2e_s, "unit": "segments/s", "h2d_bytes_per_step": h2d // e2e_steps,
                 "d2h_bytes_per_step": d2h // e2e_steps,
                 "path": "qsg_track_host (the tracking launch reads the vault from and appends the census to "

@@ -115,6 +115,10 @@ def lib() -> C.CDLL:
         h.oracle_rng_sample.restype = C.c_double
         h.oracle_rng_spawn.argtypes = [C.POINTER(C.c_uint64)]
         h.oracle_rng_spawn.restype = C.c_uint64
+        h.oracle_flop_counts.argtypes = [C.POINTER(C.c_uint64)]
+        h.oracle_flop_counts.restype = None
+        h.oracle_reset_flop_counts.argtypes = []
+        h.oracle_reset_flop_counts.restype = None
         _lib = h
     return _lib
 
@@ -307,6 +311,16 @@ def use_portable_math(on: bool):
     """Process-wide: the tracking path's log / sin / cos become the portable
     functions (quicksilver_gb300/csrc/portable_math.h) or, off, libm's."""
     lib().oracle_use_portable_math(int(bool(on)))
+
+
+def flop_counts(reset: bool = False):
+    """(FP64 operations, elementary-function calls) of the tracking path
+    since the last reset, counted as the reference writes them."""
+    out = (C.c_uint64 * 2)()
+    lib().oracle_flop_counts(out)
+    if reset:
+        lib().oracle_reset_flop_counts()
+    return int(out[0]), int(out[1])
 
 
 def pm_eval(x: np.ndarray):

@@ -29,6 +29,30 @@ void oracle_use_portable_math(int on) { g_portable_math = on != 0; }
 
 static inline double ora_log(double x) { return g_portable_math ? qsg_log(x) : log(x); }
 
+/* FP64 work of the tracking path, counted as the reference writes it: every
+ * +, -, *, / and sqrt of a double is one operation (a multiplication by -1.0
+ * included, comparisons and conversions not), log / sin / cos / exp calls
+ * are counted apart.  The macroscopic total cross section, which the
+ * reference caches per (cell, group) for the cycle, is not counted per
+ * segment.  Per thread while tracking, summed into the totals after each
+ * pass (oracle_flop_counts). */
+#ifdef _OPENMP
+static __thread uint64_t t_flops, t_elem;
+#else
+static uint64_t t_flops, t_elem;
+#endif
+static uint64_t g_flops, g_elem;
+#define FL(n) (t_flops += (uint64_t)(n))
+#define EL(n) (t_elem += (uint64_t)(n))
+
+void oracle_flop_counts(uint64_t* out2)
+{
+    out2[0] = g_flops;
+    out2[1] = g_elem;
+}
+
+void oracle_reset_flop_counts(void) { g_flops = g_elem = 0; }
+
 static inline void ora_sincos(double x, double* s, double* c)
 {
     if (g_portable_math) {
@@ -221,15 +245,17 @@ static void load_particle(const QsgProblem* pb, const OracleParticle* b, WorkPar
     w->last_event = b->last_event; w->num_collisions = b->num_collisions;
     w->species = b->species; w->breed = b->breed; w->domain = b->domain; w->cell = b->cell;
     double speed = sqrt(b->vx * b->vx + b->vy * b->vy + b->vz * b->vz);
+    FL(6);
     if (speed > 0) {
         double factor = 1.0 / speed;
         w->alpha = factor * b->vx;
         w->beta = factor * b->vy;
         w->gamma = factor * b->vz;
+        FL(4);
     } else {
         atomic_inc(warnings, 1);
     }
-    if (w->time_to_census <= 0.0) w->time_to_census += pb->time_step;
+    if (w->time_to_census <= 0.0) { w->time_to_census += pb->time_step; FL(1); }
     if (w->age < 0.0) w->age = 0.0;
     w->group = energy_group(pb, w->kinetic_energy);
 }
@@ -285,15 +311,20 @@ static double distance_to_segment(double plane_tolerance, double dot, double A, 
 {
     const double bb_tol = 1e-9;
     double numerator = -1.0 * (A * x + B * y + C * z + D);
-    if (numerator < 0.0 && numerator * numerator > plane_tolerance) return QS_HUGE_DOUBLE;
+    FL(7);
+    if (numerator < 0.0) {
+        FL(1);
+        if (numerator * numerator > plane_tolerance) return QS_HUGE_DOUBLE;
+    }
     double distance = numerator / dot;
     double ip[3];
     ip[0] = x + distance * alpha;
     ip[1] = y + distance * beta;
     ip[2] = z + distance * gamma;
+    FL(7);
 
-#define BELOW(ax) if (p0[ax] > ip[ax] + bb_tol && p1[ax] > ip[ax] + bb_tol && p2[ax] > ip[ax] + bb_tol) return QS_HUGE_DOUBLE;
-#define ABOVE(ax) if (p0[ax] < ip[ax] - bb_tol && p1[ax] < ip[ax] - bb_tol && p2[ax] < ip[ax] - bb_tol) return QS_HUGE_DOUBLE;
+#define BELOW(ax) FL(1); if (p0[ax] > ip[ax] + bb_tol && p1[ax] > ip[ax] + bb_tol && p2[ax] > ip[ax] + bb_tol) return QS_HUGE_DOUBLE;
+#define ABOVE(ax) FL(1); if (p0[ax] < ip[ax] - bb_tol && p1[ax] < ip[ax] - bb_tol && p2[ax] < ip[ax] - bb_tol) return QS_HUGE_DOUBLE;
 #define XCROSS(ax, ay, bx, by, cx, cy) ((bx - ax) * (cy - ay) - (by - ay) * (cx - ax))
     double cross0 = 0, cross1 = 0, cross2 = 0;
     int u, v;
@@ -313,12 +344,14 @@ static double distance_to_segment(double plane_tolerance, double dot, double A, 
         cross1 = XCROSS(p0[u], p0[v], p1[u], p1[v], ip[u], ip[v]);
         cross2 = XCROSS(p1[u], p1[v], p2[u], p2[v], ip[u], ip[v]);
         cross0 = XCROSS(p2[u], p2[v], p0[u], p0[v], ip[u], ip[v]);
+        FL(21);
     }
 #undef BELOW
 #undef ABOVE
 #undef XCROSS
     double s = cross0 + cross1 + cross2;
     double cross_tol = 1e-9 * (s < 0 ? -s : s);
+    FL(3);
     if ((cross0 > -cross_tol && cross1 > -cross_tol && cross2 > -cross_tol) ||
         (cross0 < cross_tol && cross1 < cross_tol && cross2 < cross_tol))
         return distance;
@@ -337,10 +370,12 @@ static double nearest_facet(const QsgProblem* pb, WorkParticle* w, int* facet_ou
     double dist[24];
     for (;;) {
         double plane_tolerance = 1e-16 * (w->x * w->x + w->y * w->y + w->z * w->z);
+        FL(6);
         for (int f = 0; f < 24; f++) {
             dist[f] = QS_HUGE_DOUBLE;
             const double* pl = planes + 4 * f;
             double dot = pl[0] * w->alpha + pl[1] * w->beta + pl[2] * w->gamma;
+            FL(5);
             if (dot <= 0.0) continue;
             dist[f] = distance_to_segment(plane_tolerance, dot, pl[0], pl[1], pl[2], pl[3],
                                           facet_point(pb, cell, f, 0), facet_point(pb, cell, f, 1),
@@ -371,6 +406,7 @@ static double nearest_facet(const QsgProblem* pb, WorkParticle* w, int* facet_ou
             w->z += move_factor * (cz - w->z);
             iteration++;
             move_factor *= 2.0;
+            FL(42 + 4 + 9 + 1);   /* the centre (MCT.cc:231-253), the move, the factor */
             if (move_factor > 1.0e-2) move_factor = 1.0e-2;
             if (iteration == 10000) { atomic_inc(warnings, 1); retry = 0; }
             else retry = 1;
@@ -393,6 +429,7 @@ static int segment_outcome(TrackCtx* ctx, WorkParticle* w)
     const QsgProblem* pb = ctx->pb;
     double distance[3];
     double speed = sqrt(w->vx * w->vx + w->vy * w->vy + w->vz * w->vz);
+    FL(6);
     int force_collision = 0;
     if (w->num_mean_free_paths < 0.0) {
         force_collision = 1;
@@ -402,14 +439,16 @@ static int segment_outcome(TrackCtx* ctx, WorkParticle* w)
     double sigma = total_macro_xs(pb, w->cell, w->group);
     w->total_xs = sigma;
     if (sigma == 0.0) w->mean_free_path = QS_HUGE_DOUBLE;
-    else w->mean_free_path = 1.0 / sigma;
+    else { w->mean_free_path = 1.0 / sigma; FL(1); }
     if (w->num_mean_free_paths == 0.0) {
         double r = oracle_rng_sample(&w->seed);
         w->num_mean_free_paths = -1.0 * ora_log(r);
+        FL(2); EL(1);
     }
     if (force_collision) distance[OUT_COLLISION] = QS_SMALL_DOUBLE;
-    else distance[OUT_COLLISION] = w->num_mean_free_paths * w->mean_free_path;
+    else { distance[OUT_COLLISION] = w->num_mean_free_paths * w->mean_free_path; FL(1); }
     distance[OUT_CENSUS] = speed * w->time_to_census;
+    FL(1);
 
     int facet = 0;
     distance[OUT_FACET] = nearest_facet(pb, w, &facet, ctx->warnings);
@@ -429,6 +468,7 @@ static int segment_outcome(TrackCtx* ctx, WorkParticle* w)
     if (distance[outcome] < 0) atomic_inc(ctx->warnings, 1);
     w->segment_path_length = distance[outcome];
     w->num_mean_free_paths -= w->segment_path_length / w->mean_free_path;
+    FL(2);
     static const int to_event[3] = {QSG_EVENT_COLLISION, QSG_EVENT_FACET_TRANSIT_EXIT, QSG_EVENT_CENSUS};
     w->last_event = to_event[outcome];
     if (outcome == OUT_COLLISION) w->num_mean_free_paths = 0.0;
@@ -445,6 +485,7 @@ static int segment_outcome(TrackCtx* ctx, WorkParticle* w)
     w->time_to_census -= seg_time;
     w->age += seg_time;
     if (w->time_to_census < 0.0) w->time_to_census = 0.0;
+    FL(6 + 3 + 2);   /* the move (MC_Particle.hh:139-146), the time, the flux tally */
     /* Tallies::TallyScalarFlux, Tallies.hh:350-354 */
     atomic_add_d(&ctx->flux[(int64_t)w->cell * pb->num_groups + w->group], w->segment_path_length * w->weight);
     return outcome;
@@ -514,12 +555,14 @@ static void rotate3d(WorkParticle* w, double sin_Theta, double cos_Theta, double
     double cos_theta = w->gamma;
     double sin_theta = sqrt((1.0 - (cos_theta * cos_theta)));
     double cos_phi, sin_phi;
+    FL(3 + 22);
     if (sin_theta < 1e-6) {
         cos_phi = 1.0;
         sin_phi = 0.0;
     } else {
         cos_phi = w->alpha / sin_theta;
         sin_phi = w->beta / sin_theta;
+        FL(2);
     }
     double a = cos_theta * cos_phi * (sin_Theta * cos_Phi) - sin_phi * (sin_Theta * sin_Phi) + sin_theta * cos_phi * cos_Theta;
     double b = cos_theta * sin_phi * (sin_Theta * cos_Phi) + cos_phi * (sin_Theta * sin_Phi) + sin_theta * sin_phi * cos_Theta;
@@ -537,6 +580,7 @@ static void update_trajectory(double energy, double angle, WorkParticle* w)
     double sinPhi, cosPhi;
     ora_sincos(phi, &sinPhi, &cosPhi);
     double sinTheta = sqrt((1.0 - (cosTheta * cosTheta)));
+    FL(2 + 3 + 8 + 3 + 2); EL(3);   /* sample, phi, sin theta, speed, velocity, the log's sample and sign */
     rotate3d(w, sinTheta, cosTheta, sinPhi, cosPhi);
     const double m = QS_NEUTRON_REST_MASS_ENERGY;
     double speed = (QS_SPEED_OF_LIGHT * sqrt((1.0 - ((m * m) / ((energy + m) * (energy + m))))));
@@ -557,6 +601,7 @@ static int collision_event(TrackCtx* ctx, WorkParticle* w)
     double nd = pb->cell_number_density[w->cell];
     double r = oracle_rng_sample(&w->seed);
     double current = w->total_xs * r;
+    FL(2);
     int sel_iso = -1, sel_r = -1;
     int k0 = pb->material_isotope_offset[mat], k1 = pb->material_isotope_offset[mat + 1];
     for (int k = k0; k < k1 && current >= 0; k++) {
@@ -566,8 +611,9 @@ static int collision_event(TrackCtx* ctx, WorkParticle* w)
         for (int rr = r0; rr < r1; rr++) {
             double macro;
             if (af == 0.0 || nd == 0.0) macro = 1e-20;
-            else macro = af * nd * pb->reaction_xs[(int64_t)rr * G + w->group];
+            else { macro = af * nd * pb->reaction_xs[(int64_t)rr * G + w->group]; FL(2); }
             current -= macro;
+            FL(1);
             if (current < 0) { sel_iso = iso; sel_r = rr; break; }
         }
     }
@@ -595,12 +641,14 @@ static int collision_event(TrackCtx* ctx, WorkParticle* w)
         energy_out[0] = w->kinetic_energy * (1.0 - (rn * (1.0 / mass)));
         rn = oracle_rng_sample(&w->seed) * 2.0 - 1.0;
         angle_out[0] = rn;
+        FL(1 + 4 + 1 + 2);
         break;
     }
     case QSG_REACT_ABSORPTION:
         break;
     case QSG_REACT_FISSION: {
         int num = (int)(pb->reaction_nubar[sel_r] + oracle_rng_sample(&w->seed));
+        FL(2);
         if (num > 4) { atomic_inc(ctx->warnings, 1); num = 4; }
         n_out = num;
         for (int o = 0; o < num; o++) {
@@ -608,6 +656,7 @@ static int collision_event(TrackCtx* ctx, WorkParticle* w)
             energy_out[o] = (20 * rn * rn);
             rn = oracle_rng_sample(&w->seed) * 2.0 - 1.0;
             angle_out[o] = rn;
+            FL(3 + 2 + 3);
         }
         break;
     }
@@ -652,8 +701,10 @@ static void reflect_particle(const QsgProblem* pb, WorkParticle* w)
         w->alpha -= dot * nx;
         w->beta -= dot * ny;
         w->gamma -= dot * nz;
+        FL(6);
     }
     double speed = sqrt(w->vx * w->vx + w->vy * w->vy + w->vz * w->vz);
+    FL(6 + 6 + 3);
     w->vx = speed * w->alpha;
     w->vy = speed * w->beta;
     w->vz = speed * w->gamma;
@@ -672,7 +723,10 @@ static void track_one(TrackCtx* ctx, const OracleParticle* in, const double* in_
         /* EXPONENTIAL_TALLY build of the reference (CycleTracking.cc:48-50,
          * Tallies.hh:357-360): one random number per segment, its exp tallied
          * in the particle's cell, before the segment outcome */
-        if (ctx->cell_tally) atomic_add_d(&ctx->cell_tally[w.cell], exp(oracle_rng_sample(&w.seed)));
+        if (ctx->cell_tally) {
+            atomic_add_d(&ctx->cell_tally[w.cell], exp(oracle_rng_sample(&w.seed)));
+            FL(2); EL(1);
+        }
         int outcome = segment_outcome(ctx, &w);
         if (ctx->sens) sens_segment(ctx, &w, outcome == OUT_COLLISION);
         atomic_inc(&ctx->bal->v[QSG_BAL_NUM_SEGMENTS], 1);
@@ -757,8 +811,17 @@ static int track_all(const QsgProblem* pb, Store* processing, Store* census, Cou
         const OracleParticle* src = processing->p;
         const double* src_sc = processing->K > 0 ? processing->sc : NULL;
         const int K = processing->K;
-#pragma omp parallel for schedule(dynamic, 64)
-        for (int64_t i = 0; i < (int64_t)n; i++) track_one(&ctx, &src[i], src_sc ? src_sc + i * (size_t)K : NULL);
+#pragma omp parallel
+        {
+            t_flops = t_elem = 0;
+#pragma omp for schedule(dynamic, 64)
+            for (int64_t i = 0; i < (int64_t)n; i++)
+                track_one(&ctx, &src[i], src_sc ? src_sc + i * (size_t)K : NULL);
+#pragma omp atomic
+            g_flops += t_flops;
+#pragma omp atomic
+            g_elem += t_elem;
+        }
         if (ctx.overflow) { status = -2; break; }
         /* swap: extras become the processing list */
         Store tmp = *processing;

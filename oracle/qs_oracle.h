@@ -124,6 +124,12 @@ int oracle_track_cell_tally(const QsgProblem* problem, const OracleParticle* in,
                             OracleParticle* census_out, uint64_t cap, uint64_t* n_census,
                             uint64_t* balance13, double* flux, double* cell_tally, int nthreads);
 
+/* FP64 operations and elementary-function calls of the tracking path since
+ * the last reset (out2[0], out2[1]), counted as the reference writes them
+ * (qs_oracle.c states the rules): the algorithm's FP64 work per segment. */
+void oracle_flop_counts(uint64_t* out2);
+void oracle_reset_flop_counts(void);
+
 /* MC_RNG_State restated (MC_RNG_State.hh:22-33, MC_RNG_State.cc:29-113). */
 double oracle_rng_sample(uint64_t* seed);
 uint64_t oracle_rng_spawn(uint64_t* parent_seed);
