@@ -492,6 +492,25 @@ def reduce_over_ranks(pg, times, counts, device):
     return t.tolist(), [int(v) for v in c.tolist()]
 
 
+def host_cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
 def run_reference_arm(args, world, rank):
     """--impl reference: the CPU port of the reference algorithm on the host cores."""
     if rank != 0:
@@ -535,6 +554,7 @@ def run_reference_arm(args, world, rank):
             "config": {"workload": WORKLOAD, "impl": "CPU port of the reference algorithm (oracle/qs_oracle.c), "
                        "OpenMP over particles; the reference C++ sources are not present on this host"},
             "cpu_baseline": {"value": value, "unit": "segments/s", "cores": threads, "kind": "port",
+                             "cpu": host_cpu_model(), "compiler": oracle_py.compiler_version(),
                              "sample": sample, "value_1_thread": seg1 / secs1,
                              "sample_1_thread": f"config2 cycle {args.warmup + args.steps} ({seg1} segments, "
                                                 f"{secs1:.1f} s) on one core"},

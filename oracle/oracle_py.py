@@ -57,6 +57,15 @@ def build() -> Path:
     return LIB_PATH
 
 
+def compiler_version() -> str:
+    """First line of the C compiler's version (the port is built by `make -C oracle port` with it)."""
+    try:
+        out = subprocess.run(["gcc", "--version"], capture_output=True, text=True, timeout=10).stdout
+        return out.splitlines()[0].strip() if out else "unknown"
+    except (OSError, subprocess.SubprocessError):
+        return "unknown"
+
+
 def lib() -> C.CDLL:
     global _lib
     if _lib is None:
