@@ -25,10 +25,17 @@ tests/test_oracle_golden.py).
   (libqsg_pm.so, tests/test_gpu_portable_math.py) config2 agrees bit for
   bit: every census particle, and every flux entry within 1e-12 with no
   floor.
+* config2 over all 20 cycles of the deck (whole device cycles, the
+  reference's run length): all 13 counters bit for bit and the scalar-flux
+  total within 1e-12 every cycle.
 * config4 (the differentiated workload: 3 materials, escape boundaries, 12
   scale parameters) at 1e5 particles x 3 cycles with sensitivities on:
   counters bit for bit every cycle, forward per-cell flux within 1e-12,
-  dflux / dleak within 1e-10 per entry (sums of terms of both signs).
+  dflux / dleak within 1e-10 per entry (sums of terms of both signs); and at
+  its full size, 1e6 particles x 20 cycles: counters bit for bit every
+  cycle, per-cell forward flux within 1e-8, dflux / dleak within 1e-8 per
+  entry (the bounds config5 needs for the same reason), flux and leakage
+  totals within 1e-10.
 * config3 (the uneven ensemble): its first 16 problems at full size in one
   batch, whole cycles replayed from CUDA graphs, per-problem seed offsets;
   each problem against its own oracle run with the same offset: 13 counters
@@ -108,6 +115,54 @@ def test_config2_device_cycles_match_oracle(gpu):
         assert mc.device_status() == 0
     finally:
         mc.close()
+
+
+def test_config2_all_cycles_match_oracle(gpu):
+    deck, sim, hp = load_problem("config2.inp")
+    assert sim.n_steps == 20
+    mc = MonteCarlo(deck, problem=hp)
+    try:
+        hist = mc.run()
+    finally:
+        mc.close()
+    run = oracle_run(hp, sim)
+    for c in range(sim.n_steps):
+        run.cycle_init()
+        run.cycle_tracking(0)
+        want_total = run.flux().sum()
+        run.cycle_finalize()
+        np.testing.assert_array_equal(hist.balance[c], run.last_balance(), err_msg=f"cycle {c}")
+        assert abs(hist.flux_total[c] - want_total) <= 1e-12 * abs(want_total), f"cycle {c}"
+    run.close()
+    assert int(hist.balance[:, 12].sum()) > 200_000_000   # the deck's whole run
+
+
+def test_config4_full_size_sensitivities_match_oracle(gpu):
+    deck, sim, hp = load_problem("config4.inp")
+    assert sim.n_particles == 1_000_000 and sim.n_steps == 20
+    params = band_params(hp.array("energies"), hp.num_materials)
+    run = oracle_run(hp, sim)
+    run.enable_sensitivity(_tuples(params))
+    mc = MonteCarlo(deck, problem=hp)
+    try:
+        mc.tracker.enable_sensitivity(params)
+        hist = mc.run()
+        got = mc.tracker.read_sensitivity()
+    finally:
+        mc.close()
+    for c in range(sim.n_steps):
+        run.cycle_init()
+        run.cycle_tracking(0)
+        run.cycle_finalize()
+        np.testing.assert_array_equal(hist.balance[c], run.last_balance(), err_msg=f"cycle {c}")
+    fc, df, leak, dl = run.read_sensitivity()
+    run.close()
+    assert_flux_close(got["flux_cell"], fc, rel=1e-8)
+    assert abs(got["flux_cell"].sum() - fc.sum()) <= 1e-10 * fc.sum()
+    for k in range(df.shape[1]):
+        assert_flux_close(got["dflux"][:, k], df[:, k], rel=1e-8, scale_floor=1e-12)
+    np.testing.assert_allclose(got["leak"][0], leak, rtol=1e-10, atol=0)
+    np.testing.assert_allclose(got["dleak"][0], dl, rtol=1e-8, atol=1e-12 * abs(leak))
 
 
 def test_config4_sensitivity_cycles_match_oracle(gpu):
