@@ -79,6 +79,38 @@ def test_gpu_tracking_lane_kernel(gpu, name):
     run_parity(name, kernel=0)
 
 
+def test_lane_kernel_equals_pool_kernel_on_config2(gpu):
+    """On a full config2 cycle (the oracle's particles after cycleInit, ~1e7
+    segments) the one-history-per-lane kernel and the particle-pool kernel
+    compute every particle with the same operations in the same order: the
+    census particle sets are equal bit for bit, every counter is equal, and
+    the flux differs only by the order of the atomic additions."""
+    import hashlib
+    _, sim, hp = load_problem("config2.inp")
+    run = oracle_run(hp, sim)
+    run.cycle_init()
+    particles = run.processing()
+    run.close()
+    out = []
+    for kernel in (1, 0):
+        trk = Tracker(hp)
+        try:
+            trk.set_track_kernel(kernel)
+            trk.set_particles(particles)
+            trk.track()
+            bal, flux = trk.tallies()
+            census = sort_particles(trk.census())
+            assert trk.device_status() == 0
+        finally:
+            trk.close()
+        out.append((bal, flux, hashlib.sha256(np.ascontiguousarray(census).tobytes()).hexdigest(), len(census)))
+    (b1, f1, h1, n1), (b0, f0, h0, n0) = out
+    np.testing.assert_array_equal(b1, b0)
+    assert int(b1[12]) > 5_000_000 and n1 == n0 > 0
+    assert h1 == h0, "census particles differ between the kernels"
+    assert_flux_close(f0, f1, rel=1e-12, scale_floor=0.0)
+
+
 def test_gpu_flux_replicas(gpu):
     run_parity("t_homog", cycles=2, flux_replicas=4)
 
