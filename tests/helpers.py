@@ -111,3 +111,17 @@ class OracleMonteCarlo:
 
     def close(self):
         pass
+
+
+def balance_identities(bal: np.ndarray, label: str = "") -> None:
+    """The identities the reference's balance counters satisfy every cycle
+    (bal [cycles, 13], QSG_BAL_* order): particles tracked = particles ended,
+    collisions = their three kinds, end = census, and each cycle starts with
+    the previous cycle's census."""
+    from quicksilver_gb300 import _native as N
+    b = {k: bal[:, i].astype(np.int64) for k, i in N.BAL.items()}
+    np.testing.assert_array_equal(b["start"] + b["source"] + b["split"] - b["rr"] + b["produce"],
+                                  b["absorb"] + b["escape"] + b["census"] + b["fission"], err_msg=label)
+    np.testing.assert_array_equal(b["collision"], b["scatter"] + b["absorb"] + b["fission"], err_msg=label)
+    np.testing.assert_array_equal(b["end"], b["census"], err_msg=label)
+    np.testing.assert_array_equal(b["start"][1:], b["census"][:-1], err_msg=label)

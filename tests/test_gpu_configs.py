@@ -50,13 +50,24 @@ tests/test_oracle_golden.py).
   search as config2's flux is; leakage within 1e-10 (one accumulator per
   replica summed in a different order).
 
+* At full size, where the oracle would take minutes to hours, through the
+  counters' identities, which the unmodified reference satisfies on every
+  golden deck and cycle: start + source + split - rr + produce = absorb +
+  escape + census + fission, collision = scatter + absorb + fission, end =
+  census, and each cycle starts with the previous cycle's census.  config3's
+  whole ensemble (64 problems, 10 cycles) in one graph-replayed batch, also
+  bit for bit against the problems run one by one; config5 at its full 8 x
+  1e7 particles x 20 cycles with its 20 tied sensitivities, where besides the
+  sensitivity run's per-cell flux, summed over cells, equals the sum of the
+  cycles' flux totals within 1e-12 (two tallies of one quantity).
+
 Reference behaviour reproduced: CycleTracking.cc:33-120, Tallies.cc:25-98,
 main.cc:96-324, MC_SourceNow.cc:28-164, PopulationControl.cc:20-171.
 """
 import numpy as np
 import pytest
 
-from helpers import DECKS, assert_flux_close, load_problem, oracle_run, sort_particles
+from helpers import DECKS, assert_flux_close, balance_identities, load_problem, oracle_run, sort_particles
 from quicksilver_gb300 import Deck
 from quicksilver_gb300.monte_carlo import BatchMonteCarlo, MonteCarlo, seed_offset
 from quicksilver_gb300.sensitivity import band_params, tie_across_problems
@@ -269,3 +280,57 @@ def test_config5_scaled_batch_with_sensitivities_matches_oracle(gpu):
         # different order: summation alone reaches ~1e-11 relative here
         np.testing.assert_allclose(sens["leak"][p], leak, rtol=1e-10, atol=0)
         np.testing.assert_allclose(sens["dleak"][p], dl, rtol=1e-8, atol=1e-12 * abs(leak))
+
+
+def test_config3_full_ensemble_batch(gpu):
+    from quicksilver_gb300.decks.make_decks import config3
+    decks = [Deck.from_string(t) for t in config3()]
+    assert len(decks) == 64
+    problems = [d.build() for d in decks]
+    offs = [seed_offset(d.simulation.seed) for d in decks]
+    cycles = decks[0].simulation.n_steps
+    bmc = BatchMonteCarlo(decks, problems=problems, seed_offsets=offs)
+    try:
+        hist = bmc.run(cycles, use_graph=True)
+        assert bmc.device_status() == 0
+    finally:
+        bmc.close()
+    busy = 0
+    for p, (d, hp, off) in enumerate(zip(decks, problems, offs)):
+        balance_identities(hist.balance[:, p], f"problem {p}")
+        mc = MonteCarlo(d, problem=hp, seed_offset=off)
+        try:
+            one = mc.run(cycles)
+        finally:
+            mc.close()
+        np.testing.assert_array_equal(hist.balance[:, p], one.balance, err_msg=f"problem {p}")
+        busy += int(one.balance[:, 12].sum() > 0)
+    assert busy >= 32
+
+
+def test_config5_full_size_batch_with_sensitivities(gpu):
+    from quicksilver_gb300.decks.make_decks import config5
+    decks = [Deck.from_string(t) for t in config5()]
+    assert len(decks) == 8 and decks[0].simulation.n_particles == 10_000_000
+    problems = [d.build() for d in decks]
+    offs = [seed_offset(d.simulation.seed) for d in decks]
+    cycles = decks[0].simulation.n_steps
+    n_part = decks[0].simulation.n_particles
+    cap = int(1.3 * (n_part + n_part // 10)) + 1024
+    base = band_params(problems[0].array("energies"), problems[0].num_materials)
+    bmc = BatchMonteCarlo(decks, problems=problems, seed_offsets=offs, store_capacity=cap, max_passes=2)
+    try:
+        bmc.tracker.enable_sensitivity(tie_across_problems(base, bmc.tracker.material_offsets()))
+        hist = bmc.run(cycles, use_graph=True)
+        sens = bmc.tracker.read_sensitivity()
+        coff = bmc.tracker.cell_offsets
+        assert bmc.device_status() == 0
+    finally:
+        bmc.close()
+    assert int(hist.balance[:, :, 12].sum()) > 5_000_000_000
+    for p in range(len(decks)):
+        balance_identities(hist.balance[:, p], f"replica {p}")
+        cells = sens["flux_cell"][int(coff[p]):int(coff[p + 1])].sum()
+        total = hist.flux_total[:, p].sum()
+        assert total > 0 and abs(cells - total) <= 1e-12 * total, p
+        assert sens["leak"][p] > 0 and np.abs(sens["dleak"][p]).sum() > 0
