@@ -7,7 +7,8 @@ quicksilver_gb300/decks it runs the reference harness and stores in
 
 * ``balance``        [cycles, 13] uint64, Tallies.cc:400-414 order
 * ``flux``           [cycles, cells, groups] float64 (small decks only)
-* ``flux_cell``      [cycles, cells]  per-cell sums, gid order
+* ``flux_cell``      [cycles, cells]  per-cell sums, gid order (not for config2, which
+  is stored for its first three cycles)
 * ``flux_group``     [cycles, groups] per-group sums
 * ``flux_proj``      [cycles, 4] projections on fixed pseudo-random weights
 * ``init_sha``/``census_sha``  sha256 of the sorted 136-byte particle records
@@ -163,7 +164,16 @@ def run_deck(deck: Path, workdir: Path, harness: Path = HARNESS) -> dict:
     return read_dump(dump)
 
 
+STOCK_CYCLES = {"config2": 3}   # the benchmark deck: its first three cycles
+LARGE_FLUX = 1_000_000          # above this many (cell, group) entries, no per-cell sums either
+
+
 def make(deck: Path, workdir: Path) -> None:
+    if deck.stem in STOCK_CYCLES:
+        import re
+        text = deck.read_text()
+        deck = workdir / deck.name
+        deck.write_text(re.sub(r"nSteps: \d+", f"nSteps: {STOCK_CYCLES[deck.stem]}", text))
     d = run_deck(deck, workdir)
     cycles = sum(1 for k in d if k.startswith("balance_c"))
     G = len(d["energies"]) - 1
@@ -172,7 +182,8 @@ def make(deck: Path, workdir: Path) -> None:
     flux = np.stack([d[f"flux_c{c}"] for c in range(cycles)])
     if C * G <= FULL_FLUX_LIMIT:
         out["flux"] = flux.reshape(cycles, C, G)
-    out["flux_cell"] = flux.reshape(cycles, C, G).sum(axis=2)
+    if C * G <= LARGE_FLUX:
+        out["flux_cell"] = flux.reshape(cycles, C, G).sum(axis=2)
     out["flux_group"] = flux.reshape(cycles, C, G).sum(axis=1)
     out["flux_proj"] = flux @ projection_weights(C, G).T
     out["flux_total"] = flux.sum(axis=1)

@@ -5,7 +5,9 @@ tests/test_oracle_golden.py).
 * config2 (the 40^3-cell three-shell deck every bench.py number is quoted
   on): three whole cycles on the device (qsg_cycle_init / qsg_track_cycle /
   qsg_cycle_finalize) beside the oracle's cycleInit / cycleTracking /
-  cycleFinalize. Each cycle: all 13 balance counters bit for bit; scalar
+  cycleFinalize, and against the unmodified reference's own counters for
+  those cycles (tests/golden/config2.npz). Each cycle: all 13 balance
+  counters bit for bit; scalar
   flux per group and in total within 1e-12 relative; census particles
   matched one to one by identifier and seed (integer fields exactly,
   floating fields to 1e-7 relative). Per cell the flux is held to 1e-8
@@ -124,6 +126,9 @@ def test_config2_device_cycles_match_oracle(gpu):
             np.testing.assert_array_equal(mc.history(c, 1).balance[0], run.last_balance(), err_msg=f"cycle {c}")
             assert int(run.last_balance()[12]) > 10_000_000   # the full workload, not a trivial cycle
         assert mc.device_status() == 0
+        # and the unmodified reference's own counters for these cycles
+        gold = np.load(DECKS.parent.parent / "tests" / "golden" / "config2.npz")["balance"]
+        np.testing.assert_array_equal(mc.history(0, 3).balance, gold)
     finally:
         mc.close()
 

@@ -46,7 +46,8 @@ def run_against_golden(name, threads=4):
         flux = run.flux()
         if "flux" in gold:
             assert_flux_close(flux, gold["flux"][c])
-        assert_flux_close(flux.sum(axis=1), gold["flux_cell"][c])
+        if "flux_cell" in gold:
+            assert_flux_close(flux.sum(axis=1), gold["flux_cell"][c])
         assert_flux_close(flux.sum(axis=0), gold["flux_group"][c])
         assert_flux_close(w @ flux.ravel(), gold["flux_proj"][c])
         cen = sort_particles(run.processed())
@@ -62,6 +63,11 @@ def test_oracle_matches_reference_small(name):
 
 def test_oracle_matches_reference_config1():
     run_against_golden("config1", threads=8)
+
+
+def test_oracle_matches_reference_config2():
+    """The benchmark deck's first three cycles (43.8 M segments)."""
+    run_against_golden("config2", threads=8)
 
 
 def test_limit_invariants():
