@@ -7,8 +7,8 @@ quicksilver_gb300/decks it runs the reference harness and stores in
 
 * ``balance``        [cycles, 13] uint64, Tallies.cc:400-414 order
 * ``flux``           [cycles, cells, groups] float64 (small decks only)
-* ``flux_cell``      [cycles, cells]  per-cell sums, gid order (not for config2, which
-  is stored for its first three cycles)
+* ``flux_cell``      [cycles, cells]  per-cell sums, gid order (not for config2;
+  config2 and config4 are stored for their first three cycles)
 * ``flux_group``     [cycles, groups] per-group sums
 * ``flux_proj``      [cycles, 4] projections on fixed pseudo-random weights
 * ``init_sha``/``census_sha``  sha256 of the sorted 136-byte particle records
@@ -164,7 +164,7 @@ def run_deck(deck: Path, workdir: Path, harness: Path = HARNESS) -> dict:
     return read_dump(dump)
 
 
-STOCK_CYCLES = {"config2": 3}   # the benchmark deck: its first three cycles
+STOCK_CYCLES = {"config2": 3, "config4": 3}   # the benchmark decks: their first three cycles
 LARGE_FLUX = 1_000_000          # above this many (cell, group) entries, no per-cell sums either
 
 

@@ -171,6 +171,8 @@ def test_config4_full_size_sensitivities_match_oracle(gpu):
         run.cycle_tracking(0)
         run.cycle_finalize()
         np.testing.assert_array_equal(hist.balance[c], run.last_balance(), err_msg=f"cycle {c}")
+    gold = np.load(DECKS.parent.parent / "tests" / "golden" / "config4.npz")["balance"]
+    np.testing.assert_array_equal(hist.balance[:len(gold)], gold)   # the unmodified reference's own counters
     fc, df, leak, dl = run.read_sensitivity()
     run.close()
     assert_flux_close(got["flux_cell"], fc, rel=1e-8)

@@ -70,6 +70,11 @@ def test_oracle_matches_reference_config2():
     run_against_golden("config2", threads=8)
 
 
+def test_oracle_matches_reference_config4():
+    """The differentiated workload's deck (escape boundaries), first three cycles."""
+    run_against_golden("config4", threads=8)
+
+
 def test_limit_invariants():
     """Analytic invariants of the limit decks (cf. the reference's example physics)."""
     B = {n: i for i, n in enumerate(("absorb", "census", "escape", "collision", "end", "fission", "produce",
