@@ -65,8 +65,12 @@ deck, ``pm_<deck>.npz``: the counters, the flux (whole when small, otherwise
 per cell / per group / projections / total) and the sha256 of the sorted
 particle sets after each cycleInit and cycleTracking.
 
+With ``--config5`` it stores ``config5_r0.npz``: the first replica of the config5
+ensemble (its 64^3 slab geometry, 3e6 particles, 2 cycles).
+
 Usage: python tests/golden/make_golden.py [--exponential-tally | --portable-math | --echo | --xsec |
-                                           --spectrum | --coral | --summary | --timers | --transcript]
+                                           --spectrum | --coral | --summary | --timers | --transcript |
+                                           --config5]
 """
 from __future__ import annotations
 
@@ -391,8 +395,26 @@ def make_transcript(workdir: Path) -> None:
     print("transcript_out.npz: t_coral1")
 
 
+def make_config5(workdir: Path) -> None:
+    """config5's first replica (make_decks.config5, 3e6 particles -- the smallest
+    count at which every cell sources -- and 2 cycles), the benchmark's slab
+    geometry, as ``config5_r0.npz``."""
+    sys.path.insert(0, str(ROOT))
+    from quicksilver_gb300.decks.make_decks import config5
+    import re
+    text = re.sub(r"nSteps: \d+", "nSteps: 2", config5(n_particles=3_000_000)[0])
+    deck = workdir / "config5_r0.inp"
+    deck.write_text(text)
+    make(deck, workdir)
+
+
 def main(argv: list[str]) -> None:
     import tempfile
+    if "--config5" in argv:
+        ensure_harness("ref")
+        with tempfile.TemporaryDirectory() as tmp:
+            make_config5(Path(tmp))
+        return
     if "--transcript" in argv:
         ensure_harness("ref")
         with tempfile.TemporaryDirectory() as tmp:

@@ -26,9 +26,12 @@ def _proj(cells, groups):
     return np.random.default_rng(20240601).uniform(0.5, 1.5, size=(4, cells * groups))
 
 
-def run_against_golden(name, threads=4):
+def run_against_golden(name, threads=4, deck=None):
     gold = np.load(GOLDEN / f"{name}.npz")
-    _, sim, hp = load_problem(f"{name}.inp")
+    if deck is None:
+        _, sim, hp = load_problem(f"{name}.inp")
+    else:
+        sim, hp = deck.simulation, deck.build()
     run = oracle_run(hp, sim)
     cycles = gold["balance"].shape[0]
     w = _proj(hp.num_cells, hp.num_groups)
@@ -96,3 +99,13 @@ def test_limit_invariants():
         gains = g[:, B["start"]] + g[:, B["source"]] + g[:, B["produce"]] + g[:, B["split"]]
         losses = g[:, B["absorb"]] + g[:, B["census"]] + g[:, B["escape"]] + g[:, B["rr"]] + g[:, B["fission"]]
         np.testing.assert_array_equal(gains, losses, err_msg=name)
+
+
+def test_oracle_matches_reference_config5_replica():
+    """config5's first replica (64^3 cells in five slabs, five materials,
+    escape boundaries) at 3e6 particles, two cycles."""
+    import re
+    from quicksilver_gb300 import Deck
+    from quicksilver_gb300.decks.make_decks import config5
+    deck = Deck.from_string(re.sub(r"nSteps: \d+", "nSteps: 2", config5(n_particles=3_000_000)[0]))
+    run_against_golden("config5_r0", threads=8, deck=deck)
