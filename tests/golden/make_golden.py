@@ -65,12 +65,15 @@ deck, ``pm_<deck>.npz``: the counters, the flux (whole when small, otherwise
 per cell / per group / projections / total) and the sha256 of the sorted
 particle sets after each cycleInit and cycleTracking.
 
+With ``--config3`` it stores ``config3_pNN.npz`` for five problems of the config3
+ensemble (one per mesh edge), two cycles each.
+
 With ``--config5`` it stores ``config5_r0.npz``: the first replica of the config5
 ensemble (its 64^3 slab geometry, 3e6 particles, 2 cycles).
 
 Usage: python tests/golden/make_golden.py [--exponential-tally | --portable-math | --echo | --xsec |
                                            --spectrum | --coral | --summary | --timers | --transcript |
-                                           --config5]
+                                           --config3 | --config5]
 """
 from __future__ import annotations
 
@@ -408,8 +411,30 @@ def make_config5(workdir: Path) -> None:
     make(deck, workdir)
 
 
+CONFIG3_PROBLEMS = [4, 6, 15, 26, 33]   # one per mesh edge 48 / 32 / 24 / 8 / 16, 1-3 materials
+
+
+def make_config3(workdir: Path) -> None:
+    """A few problems of the config3 ensemble (make_decks.config3), one per mesh
+    edge, two cycles each with the reference's own seeding, as
+    ``config3_pNN.npz``."""
+    sys.path.insert(0, str(ROOT))
+    from quicksilver_gb300.decks.make_decks import config3
+    import re
+    decks = config3()
+    for p in CONFIG3_PROBLEMS:
+        deck = workdir / f"config3_p{p:02d}.inp"
+        deck.write_text(re.sub(r"nSteps: \d+", "nSteps: 2", decks[p]))
+        make(deck, workdir)
+
+
 def main(argv: list[str]) -> None:
     import tempfile
+    if "--config3" in argv:
+        ensure_harness("ref")
+        with tempfile.TemporaryDirectory() as tmp:
+            make_config3(Path(tmp))
+        return
     if "--config5" in argv:
         ensure_harness("ref")
         with tempfile.TemporaryDirectory() as tmp:

@@ -9,7 +9,8 @@ from helpers import DECKS, balance_identities
 GOLDEN = DECKS.parent.parent / "tests" / "golden"
 
 
-@pytest.mark.parametrize("name", sorted(p.stem for p in GOLDEN.glob("t_*.npz")) + ["config1", "config2", "config4", "config5_r0"])
+@pytest.mark.parametrize("name", sorted(p.stem for p in GOLDEN.glob("t_*.npz")) + ["config1", "config2", "config4", "config5_r0"]
+                         + sorted(p.stem for p in GOLDEN.glob("config3_p*.npz")))
 def test_identities_hold_on_the_reference_counters(name):
     balance_identities(np.load(GOLDEN / f"{name}.npz")["balance"], name)
 

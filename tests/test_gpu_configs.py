@@ -42,9 +42,10 @@ tests/test_oracle_golden.py).
   batch, whole cycles replayed from CUDA graphs, per-problem seed offsets;
   each problem against its own oracle run with the same offset: 13 counters
   bit for bit and the flux total within 1e-12, every cycle.
-* config5's first replica deck at 3e6 particles, two cycles with the
-  reference's own seeding: its 13 counters equal the unmodified reference's
-  (tests/golden/config5_r0.npz).
+* five config3 problems (one per mesh edge) and config5's first replica
+  deck at 3e6 particles, two cycles each with the reference's own seeding:
+  their 13 counters equal the unmodified reference's
+  (tests/golden/config3_pNN.npz, config5_r0.npz).
 * config5 (the large batched + differentiated run) at 0.3 of its particles
   (3e6 per replica, the smallest count at which every cell sources) x 2
   cycles: 8 replicas with distinct seed offsets and 20 parameters tied across
@@ -244,6 +245,24 @@ def test_config3_subset_batch_matches_oracle(gpu):
     # the subset holds empty problems (fewer particles than the source's
     # per-cell floor needs) and busy ones; both kinds must match
     assert 4 <= busy < 16
+
+
+def test_config3_problems_match_reference_counters(gpu):
+    """Five problems of the config3 ensemble (one per mesh edge), two whole
+    device cycles each with the reference's own seeding: all 13 counters
+    equal the unmodified reference's (tests/golden/config3_pNN.npz)."""
+    import re
+    from quicksilver_gb300.decks.make_decks import config3
+    texts = config3()
+    for p in (4, 6, 15, 26, 33):
+        deck = Deck.from_string(re.sub(r"nSteps: \d+", "nSteps: 2", texts[p]))
+        gold = np.load(DECKS.parent.parent / "tests" / "golden" / f"config3_p{p:02d}.npz")["balance"]
+        mc = MonteCarlo(deck)
+        try:
+            hist = mc.run(2)
+        finally:
+            mc.close()
+        np.testing.assert_array_equal(hist.balance, gold, err_msg=f"problem {p}")
 
 
 def test_config5_replica_matches_reference_counters(gpu):

@@ -109,3 +109,15 @@ def test_oracle_matches_reference_config5_replica():
     from quicksilver_gb300.decks.make_decks import config5
     deck = Deck.from_string(re.sub(r"nSteps: \d+", "nSteps: 2", config5(n_particles=3_000_000)[0]))
     run_against_golden("config5_r0", threads=8, deck=deck)
+
+
+@pytest.mark.parametrize("problem", [4, 6, 15, 26, 33])
+def test_oracle_matches_reference_config3_problem(problem):
+    """Problems of the config3 ensemble, one per mesh edge (48 / 32 / 24 / 8 /
+    16; problem 4 sources nothing: fewer particles than the per-cell floor
+    needs), two cycles with the reference's own seeding."""
+    import re
+    from quicksilver_gb300 import Deck
+    from quicksilver_gb300.decks.make_decks import config3
+    deck = Deck.from_string(re.sub(r"nSteps: \d+", "nSteps: 2", config3()[problem]))
+    run_against_golden(f"config3_p{problem:02d}", threads=8, deck=deck)
