@@ -516,6 +516,10 @@ def run_reference_arm(args, world, rank):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
+    # one OpenMP thread per core, kept there (set before the port's OpenMP
+    # runtime loads; a caller's own settings win)
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    os.environ.setdefault("OMP_PLACES", "cores")
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle_py
     from quicksilver_gb300 import Deck
@@ -555,6 +559,7 @@ def run_reference_arm(args, world, rank):
                        "OpenMP over particles; the reference C++ sources are not present on this host"},
             "cpu_baseline": {"value": value, "unit": "segments/s", "cores": threads, "kind": "port",
                              "cpu": host_cpu_model(), "compiler": oracle_py.compiler_version(),
+                             "omp": f"OMP_PROC_BIND={os.environ['OMP_PROC_BIND']} OMP_PLACES={os.environ['OMP_PLACES']}",
                              "sample": sample, "value_1_thread": seg1 / secs1,
                              "sample_1_thread": f"config2 cycle {args.warmup + args.steps} ({seg1} segments, "
                                                 f"{secs1:.1f} s) on one core"},
