@@ -115,9 +115,11 @@ class OracleMonteCarlo:
 
 def balance_identities(bal: np.ndarray, label: str = "") -> None:
     """The identities the reference's balance counters satisfy every cycle
-    (bal [cycles, 13], QSG_BAL_* order): particles tracked = particles ended,
-    collisions = their three kinds, end = census, and each cycle starts with
-    the previous cycle's census."""
+    (bal [cycles, 13], QSG_BAL_* order): particles tracked = particles ended
+    (the reference's own particle-conservation check, CoralBenchmark.cc:152-174,
+    and its test for done, MC_Particle_Buffer.cc:176-188), collisions = their
+    three kinds (CollisionEvent.cc:103-116), end = census, and each cycle
+    starts with the previous cycle's census."""
     from quicksilver_gb300 import _native as N
     b = {k: bal[:, i].astype(np.int64) for k, i in N.BAL.items()}
     np.testing.assert_array_equal(b["start"] + b["source"] + b["split"] - b["rr"] + b["produce"],
